@@ -1,0 +1,75 @@
+import json
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+GOLDEN = ROOT / "tests" / "golden"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "slow: large sizes (seconds of CPU oracle work)")
+
+
+def _has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def pytest_collection_modifyitems(config, items):
+    if _has_gpu():
+        return
+    skip = pytest.mark.skip(reason="no CUDA device")
+    for it in items:
+        if "gpu" in it.keywords:
+            it.add_marker(skip)
+
+
+class Golden:
+    """The reference's outputs on seeded inputs (tests/golden/make_golden.py)."""
+
+    def __init__(self):
+        with open(GOLDEN / "eigen_dense.json") as f:
+            self.meta = json.load(f)
+        self.arrays = np.load(GOLDEN / "eigen_dense.npz")
+
+    def cases(self, kind):
+        return [c for c in self.meta["cases"] if c["kind"] == kind]
+
+    def arr(self, case, key):
+        k = case["name"] + key
+        return self.arrays[k] if k in self.arrays.files else None
+
+    @staticmethod
+    def input(case):
+        from tests.golden.make_golden import gen
+        return gen(case)
+
+    @staticmethod
+    def rhs(case, nrhs):
+        from tests.golden.make_golden import rhs
+        return rhs(case, nrhs)
+
+
+@pytest.fixture(scope="session")
+def golden():
+    return Golden()
+
+
+def case_id(c):
+    s = f"{c['kind']}-{c['gen']}-{c['m']}x{c['n']}"
+    if c.get("dtype") == "f32":
+        s += "-f32"
+    if c.get("upper"):
+        s += "-upper"
+    return s

@@ -1,0 +1,205 @@
+"""Generate the golden fixtures for the dense factor-and-solve path by running
+the reference itself (Eigen, built from the reference tree into
+oracle/_ref/libeigen_ref.so) on seeded, byte-stable inputs.
+
+    python tests/golden/make_golden.py
+
+Writes tests/golden/eigen_dense.json (case list + scalars) and
+tests/golden/eigen_dense.npz (arrays).  Inputs are not stored: every case
+records the generator (oracle.gauss / oracle.uniform / oracle.spd with its
+seed), whose bytes are identical on every host.  Small cases store the full
+factors; large cases store pivots, solutions and a fixed sample of factor
+entries.
+
+What each case pins (reference API used):
+  lu    PartialPivLU<MatrixX?>(A): matrixLU(), permutationP().indices(),
+        solve(B), transpose().solve(B), rcond(), determinant();
+        partial_lu_impl::blocked_lu transpositions + count + first zero pivot;
+        ?getrf_ ipiv (1-based) and info from the reference's LAPACK shim.
+  llt   LLT<MatrixX?, Lower|Upper>(A): matrixLLT(), info(), solve(B), rcond();
+        llt_inplace::blocked failing column; ?potrf_ info.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+FULL_MAX = 129          # store whole factors up to this size
+SAMPLE = 2048           # otherwise this many factor entries at fixed positions
+
+
+def sample_idx(n: int) -> np.ndarray:
+    rng = np.random.default_rng(1000 + n)  # positions only; stored in the fixture
+    return np.sort(rng.choice(n * n, size=min(SAMPLE, n * n), replace=False)).astype(np.int64)
+
+
+def gen(spec: dict) -> np.ndarray:
+    k = spec["gen"]
+    if k == "gauss":
+        a = O.gauss(spec["seed"], spec["m"], spec["n"])
+    elif k == "uniform":
+        a = O.uniform(spec["seed"], spec["m"], spec["n"])
+    elif k == "spd":
+        a = O.spd(spec["seed"], spec["n"], spec.get("scale"), spec.get("shift", 1.0))
+    elif k == "int":   # small integers in [-2, 2]: exact arithmetic, many exact pivot ties
+        a = np.asfortranarray(np.rint(O.uniform(spec["seed"], spec["m"], spec["n"]) * 2.49))
+    elif k == "neg_spd":
+        a = -O.spd(spec["seed"], spec["n"])
+    elif k == "late_fail":  # SPD except one diagonal entry made too small: fails at column `col`
+        a = O.spd(spec["seed"], spec["n"])
+        a[spec["col"], spec["col"]] = -1.0
+    elif k == "zero_col":  # exactly singular: column `col` is zero
+        a = O.gauss(spec["seed"], spec["m"], spec["n"])
+        a[:, spec["col"]] = 0.0
+    elif k == "ones":
+        a = np.ones((spec["m"], spec["n"]), order="F")
+    else:
+        raise ValueError(k)
+    if spec.get("dtype", "f64") == "f32":
+        a = np.asfortranarray(a.astype(np.float32))
+    return a
+
+
+def rhs(spec: dict, nrhs: int) -> np.ndarray:
+    b = O.gauss(spec["seed"] + 7919, spec["n"], nrhs)
+    return np.asfortranarray(b.astype(np.float32)) if spec.get("dtype", "f64") == "f32" else b
+
+
+def lu_case(spec: dict, arrays: dict, name: str) -> dict:
+    a = gen(spec)
+    n = spec["n"]
+    nrhs = spec.get("nrhs", 3)
+    b = rhs(spec, nrhs)
+    fact, perm, x, xt, rc, det = O.ref_lu(a, b)
+    _, tr, nbt, fz = O.ref_lu_blocked(a)
+    # the reference's LAPACK shim (1-based ipiv, info = first zero pivot + 1)
+    lib = O.ref()
+    pre = "d" if a.dtype == np.float64 else "s"
+    ag = np.array(a, order="F", copy=True)
+    ipiv = np.zeros(max(n, 1), dtype=np.int32)
+    m_ = C.c_int(n); n_ = C.c_int(n); lda = C.c_int(max(n, 1)); info = C.c_int(0)
+    getattr(lib, pre + "getrf_")(C.byref(m_), C.byref(n_), ag, C.byref(lda), ipiv, C.byref(info))
+    out = dict(spec, kind="lu", rcond=rc, det=det, nb_transpositions=nbt, first_zero_pivot=fz,
+               getrf_info=int(info.value), l1_norm=O.l1_norm(a))
+    arrays[name + "perm"] = perm.astype(np.int32)
+    arrays[name + "tr"] = tr.astype(np.int32)
+    arrays[name + "ipiv"] = ipiv[:n].astype(np.int32)
+    arrays[name + "x"] = x
+    arrays[name + "xt"] = xt
+    if n <= FULL_MAX:
+        arrays[name + "lu"] = fact
+    else:
+        idx = sample_idx(n)
+        arrays[name + "lu_idx"] = idx
+        arrays[name + "lu_val"] = fact.reshape(-1, order="F")[idx]
+        arrays[name + "lu_diag"] = np.diag(fact).copy()
+    return out
+
+
+def lu_rect_case(spec: dict, arrays: dict, name: str) -> dict:
+    """?getrf_ on an m x n (m > n) matrix: factors, 1-based ipiv, info."""
+    a = gen(spec)
+    m, n = a.shape
+    lib = O.ref()
+    pre = "d" if a.dtype == np.float64 else "s"
+    ag = np.array(a, order="F", copy=True)
+    ipiv = np.zeros(max(min(m, n), 1), dtype=np.int32)
+    m_ = C.c_int(m); n_ = C.c_int(n); lda = C.c_int(max(m, 1)); info = C.c_int(0)
+    getattr(lib, pre + "getrf_")(C.byref(m_), C.byref(n_), ag, C.byref(lda), ipiv, C.byref(info))
+    arrays[name + "lu"] = ag
+    arrays[name + "ipiv"] = ipiv[: min(m, n)]
+    return dict(spec, kind="getrf", getrf_info=int(info.value))
+
+
+def llt_case(spec: dict, arrays: dict, name: str) -> dict:
+    a = gen(spec)
+    n = spec["n"]
+    upper = spec.get("upper", False)
+    nrhs = spec.get("nrhs", 2)
+    b = rhs(spec, nrhs)
+    fact, info, x, rc = O.ref_llt(a, b, upper=upper)
+    lib = O.ref()
+    pre = "d" if a.dtype == np.float64 else "s"
+    ag = np.array(a, order="F", copy=True)
+    n_ = C.c_int(n); lda = C.c_int(max(n, 1)); pinfo = C.c_int(0)
+    getattr(lib, pre + "potrf_")(b"U" if upper else b"L", C.byref(n_), ag, C.byref(lda), C.byref(pinfo))
+    out = dict(spec, kind="llt", info=info, potrf_info=int(pinfo.value),
+               rcond=(rc if info == 0 else None), l1_norm=O.sym_l1_norm(a, upper))
+    tri = np.triu(fact) if upper else np.tril(fact)
+    if info == 0:
+        arrays[name + "x"] = x
+    if n <= FULL_MAX:
+        arrays[name + "fact"] = tri
+    else:
+        idx = sample_idx(n)
+        arrays[name + "fact_idx"] = idx
+        arrays[name + "fact_val"] = tri.reshape(-1, order="F")[idx]
+        arrays[name + "fact_diag"] = np.diag(fact).copy()
+    return out
+
+
+def cases():
+    lu_sizes = [1, 2, 3, 4, 5, 8, 15, 16, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 256, 257, 300,
+                512, 1000, 2048]
+    for n in lu_sizes:
+        yield "lu", dict(gen="gauss", seed=100 + n, m=n, n=n)
+    for n in [7, 33, 129, 300]:
+        yield "lu", dict(gen="uniform", seed=200 + n, m=n, n=n, dtype="f32")
+    for n in [8, 16, 24, 40]:
+        yield "lu", dict(gen="int", seed=300 + n, m=n, n=n)
+    for n, col in [(5, 2), (40, 0), (100, 57), (300, 299)]:
+        yield "lu", dict(gen="zero_col", seed=400 + n, m=n, n=n, col=col)
+    yield "lu", dict(gen="ones", seed=0, m=20, n=20)
+    yield "lu", dict(gen="gauss", seed=8192, m=8192, n=8192, nrhs=2)
+    for m, n in [(10, 4), (100, 37), (300, 129), (400, 70)]:
+        yield "getrf", dict(gen="gauss", seed=500 + m, m=m, n=n)
+    llt_sizes = [1, 2, 3, 5, 8, 16, 17, 31, 32, 33, 64, 65, 100, 128, 129, 200, 257, 512, 1000, 2048]
+    for n in llt_sizes:
+        yield "llt", dict(gen="spd", seed=600 + n, m=n, n=n)
+    for n in [3, 33, 129, 257]:
+        yield "llt", dict(gen="spd", seed=700 + n, m=n, n=n, upper=True)
+    for n in [9, 65, 200]:
+        yield "llt", dict(gen="spd", seed=800 + n, m=n, n=n, dtype="f32")
+    for n in [4, 40]:
+        yield "llt", dict(gen="neg_spd", seed=900 + n, m=n, n=n)
+    for n, col in [(10, 6), (100, 77), (300, 130)]:
+        yield "llt", dict(gen="late_fail", seed=950 + n, m=n, n=n, col=col)
+    yield "llt", dict(gen="late_fail", seed=990, m=150, n=150, col=20, upper=True)
+
+
+def main() -> None:
+    arrays: dict[str, np.ndarray] = {}
+    meta = []
+    t0 = time.time()
+    for i, (kind, spec) in enumerate(cases()):
+        name = f"c{i}_"
+        if kind == "lu":
+            rec = lu_case(spec, arrays, name)
+        elif kind == "getrf":
+            rec = lu_rect_case(spec, arrays, name)
+        else:
+            rec = llt_case(spec, arrays, name)
+        rec["name"] = name
+        meta.append(rec)
+        print(f"{name:6s} {kind:5s} n={spec['n']:5d} {spec['gen']:9s} {time.time() - t0:6.1f}s", flush=True)
+    np.savez_compressed(OUT / "eigen_dense.npz", **arrays)
+    with open(OUT / "eigen_dense.json", "w") as f:
+        json.dump({"generator": "oracle.gauss/uniform/spd (counter-based splitmix64, Irwin-Hall(12))",
+                   "reference": "Eigen 3.3.90 (PX4/eigen), g++ -O3 -mavx2 -mfma",
+                   "sample_positions": "numpy default_rng(1000+n).choice(n*n, 2048) -- stored as *_idx",
+                   "cases": meta}, f, indent=1)
+    print("wrote", OUT / "eigen_dense.npz", (OUT / "eigen_dense.npz").stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,135 @@
+"""Pin the CPU oracle (the plain-C restatement in oracle/) to the reference's
+own outputs stored in tests/golden (made by running Eigen itself).
+
+These run on CPU only.  The GPU parity tests then compare the CUDA path with
+both the fixtures and this pinned oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.conftest import Golden, case_id
+
+G = Golden()
+MAX_N_CPU = 2048   # the 8192 case is exercised by the GPU tests
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def tol(case):
+    return 2e-5 if case.get("dtype") == "f32" else 1e-12
+
+
+LU = [c for c in G.cases("lu") if c["n"] <= MAX_N_CPU]
+LLT = [c for c in G.cases("llt") if c["n"] <= MAX_N_CPU]
+
+
+@pytest.mark.parametrize("case", LU, ids=[case_id(c) for c in LU])
+def test_oracle_lu_matches_reference(case):
+    a = G.input(case)
+    f, tr, nbt, fz = O.lu(a)
+    assert np.array_equal(tr, G.arr(case, "tr")), "pivot sequence differs from the reference"
+    assert np.array_equal(O.perm_from_transpositions(tr), G.arr(case, "perm"))
+    assert np.array_equal(tr + 1, G.arr(case, "ipiv"))
+    assert nbt == case["nb_transpositions"]
+    assert fz == case["first_zero_pivot"]
+    assert (fz + 1 if fz >= 0 else 0) == case["getrf_info"]
+    full = G.arr(case, "lu")
+    if full is not None:
+        assert rel(f, full) <= tol(case) * max(1, case["n"] / 64)
+    else:
+        idx = G.arr(case, "lu_idx")
+        assert rel(f.reshape(-1, order="F")[idx], G.arr(case, "lu_val")) <= tol(case) * 10
+        assert rel(np.diag(f), G.arr(case, "lu_diag")) <= tol(case) * 10
+    if case["first_zero_pivot"] < 0:
+        nrhs = G.arr(case, "x").shape[1]
+        b = G.rhs(case, nrhs)
+        x = O.lu_solve(f, tr, b)
+        xt = O.lu_solve(f, tr, b, transpose=True)
+        # LU solutions carry the conditioning of A; compare by backward error
+        # and, loosely, by forward difference to the reference's solution
+        if a.dtype == np.float64:
+            assert O.backward_error(a, x, b) < 1e-14
+            assert O.backward_error(np.asfortranarray(a.T), xt, b) < 1e-14
+        assert rel(x, G.arr(case, "x")) < (1e-3 if a.dtype == np.float32 else 1e-9)
+        rc = O.lu_rcond(f, tr, O.l1_norm(a))
+        assert abs(rc - case["rcond"]) <= 1e-6 * abs(case["rcond"]) + (1e-3 * case["rcond"] if a.dtype == np.float32 else 0)
+        assert O.l1_norm(a) == pytest.approx(case["l1_norm"], rel=1e-6)
+
+
+@pytest.mark.parametrize("case", G.cases("getrf"), ids=[case_id(c) for c in G.cases("getrf")])
+def test_oracle_rectangular_getrf(case):
+    a = G.input(case)
+    f, tr, nbt, fz = O.lu(a)
+    assert np.array_equal(tr + 1, G.arr(case, "ipiv"))
+    assert rel(f, G.arr(case, "lu")) < 1e-12
+    assert case["getrf_info"] == (fz + 1 if fz >= 0 else 0)
+
+
+@pytest.mark.parametrize("case", LLT, ids=[case_id(c) for c in LLT])
+def test_oracle_llt_matches_reference(case):
+    a = G.input(case)
+    upper = case.get("upper", False)
+    f, info = O.llt(a, upper=upper)
+    # LLT::info(): Success/NumericalIssue; ?potrf_: first failing column + 1
+    assert (info >= 0) == (case["info"] != 0)
+    assert (info + 1 if info >= 0 else 0) == case["potrf_info"]
+    if case.get("gen") == "late_fail":
+        assert info == case["col"]
+    # the untouched triangle keeps the input bytes (LLT.h: "upper part not used")
+    if upper:
+        assert np.array_equal(np.tril(f, -1), np.tril(a, -1))
+    else:
+        assert np.array_equal(np.triu(f, 1), np.triu(a, 1))
+    if info >= 0:
+        return
+    tri = np.triu(f) if upper else np.tril(f)
+    full = G.arr(case, "fact")
+    if full is not None:
+        assert rel(tri, full) <= tol(case)
+    else:
+        idx = G.arr(case, "fact_idx")
+        assert rel(tri.reshape(-1, order="F")[idx], G.arr(case, "fact_val")) <= tol(case)
+    nrhs = G.arr(case, "x").shape[1]
+    b = G.rhs(case, nrhs)
+    x = O.llt_solve(f, b, upper=upper)
+    assert rel(x, G.arr(case, "x")) <= tol(case) * 100
+    rc = O.llt_rcond(f, O.sym_l1_norm(a, upper), upper=upper)
+    assert rc == pytest.approx(case["rcond"], rel=1e-9 if a.dtype == np.float64 else 1e-4)
+    assert O.sym_l1_norm(a, upper) == pytest.approx(case["l1_norm"], rel=1e-12)
+
+
+def test_generators_are_byte_stable():
+    """The fixtures store generator specs, not inputs: pin a few bytes."""
+    g = O.gauss(123, 4, 3)
+    u = O.uniform(123, 4, 3)
+    assert g.dtype == np.float64 and g.flags.f_contiguous
+    # Irwin-Hall(12): values are multiples of 2^-17 in (-6, 6)
+    assert np.all(np.abs(g) < 6) and np.all((g * 131072) == np.rint(g * 131072))
+    assert np.all(np.abs(u) <= 1) and np.all((u * 2**31) == np.rint(u * 2**31))
+    big = O.gauss(5, 300, 300)
+    assert abs(big.mean()) < 0.02 and abs(big.std() - 1) < 0.02
+    s = O.spd(9, 50)
+    assert np.array_equal(s, s.T)
+    assert np.linalg.eigvalsh(s).min() > 0.9
+
+
+def test_rcond_within_10x_of_truth():
+    """test/cholesky.cpp:94-116 and test/lu.cpp:200-203: the estimate is within a
+    factor 10 of 1/(||A||_1 ||A^-1||_1)."""
+    for n in [5, 40, 200]:
+        a = O.gauss(31 + n, n, n)
+        f, tr, _, _ = O.lu(a)
+        inv = O.lu_solve(f, tr, np.asfortranarray(np.eye(n)))
+        truth = 1.0 / (O.l1_norm(a) * O.l1_norm(inv))
+        est = O.lu_rcond(f, tr, O.l1_norm(a))
+        assert truth / 10 < est < truth * 10
+        s = O.spd(77 + n, n)
+        fl, info = O.llt(s)
+        inv = O.llt_solve(fl, np.asfortranarray(np.eye(n)))
+        truth = 1.0 / (O.sym_l1_norm(s) * O.l1_norm(inv))
+        est = O.llt_rcond(fl, O.sym_l1_norm(s))
+        assert truth / 10 < est < truth * 10
