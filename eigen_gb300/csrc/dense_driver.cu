@@ -1,0 +1,518 @@
+// Host drivers of the plain factor-and-solve path: the blocked LU and LLT
+// loops, triangular solves, ||A||_1 and the Hager/Higham rcond estimator,
+// all stream-ordered on device buffers.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "dense_driver.cuh"
+#include "dense_kernels.cuh"
+#include "gbs_profile.cuh"
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error = "";
+
+void gbs_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line)
+{
+  char buf[512];
+  snprintf(buf, sizeof(buf), "CUDA error %d (%s) in %s at %s:%d", (int)e, cudaGetErrorString(e), what, file, line);
+  g_last_error = buf;
+}
+
+void gbs_set_last_message(const char* msg) { g_last_error = msg; }
+
+extern "C" const char* gbs_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* gbs_version(void) { return "gb300solve 0.1 (sm_103a)"; }
+
+namespace gbs {
+
+// ------------------------------------------------------------------ device
+static std::once_flag g_dev_once;
+static int g_dev_status = GBS_NO_DEVICE;
+static int g_sm_count = 0;
+
+static void probe_devices()
+{
+  int cnt = 0;
+  if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt <= 0) {
+    cudaGetLastError();
+    gbs_set_last_message("no CUDA device");
+    return;
+  }
+  int usable = 0;
+  for (int d = 0; d < cnt; ++d) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, d) != cudaSuccess) continue;
+    if (p.major == 10 && p.minor == 3) {
+      ++usable;
+      if (g_sm_count == 0) g_sm_count = p.multiProcessorCount;
+    }
+  }
+  if (usable > 0) g_dev_status = GBS_SUCCESS;
+  else gbs_set_last_message("no sm_103 (GB300) device: this library is built for sm_103a only");
+}
+
+int ensure_device()
+{
+  std::call_once(g_dev_once, probe_devices);
+  if (g_dev_status != GBS_SUCCESS) gbs_set_last_message("no usable sm_103a device");
+  return g_dev_status;
+}
+
+int device_sm_count()
+{
+  ensure_device();
+  return g_sm_count > 0 ? g_sm_count : 1;
+}
+
+// ------------------------------------------------------------------ buffers
+int DevBuf::reserve(size_t b)
+{
+  if (b <= bytes && p) return GBS_SUCCESS;
+  release();
+  size_t want = std::max<size_t>(b, 256);
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    bytes = 0;
+    gbs_set_last_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+    return e == cudaErrorMemoryAllocation ? GBS_OUT_OF_MEMORY : GBS_CUDA_ERROR;
+  }
+  bytes = want;
+  return GBS_SUCCESS;
+}
+
+void DevBuf::release()
+{
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+int HostBuf::reserve(size_t b)
+{
+  if (b <= bytes && p) return GBS_SUCCESS;
+  release();
+  size_t want = std::max<size_t>(b, 256);
+  cudaError_t e = cudaMallocHost(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    bytes = 0;
+    gbs_set_last_cuda_error(e, "cudaMallocHost", __FILE__, __LINE__);
+    return GBS_OUT_OF_MEMORY;
+  }
+  bytes = want;
+  return GBS_SUCCESS;
+}
+
+void HostBuf::release()
+{
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+static std::mutex g_pool_mu;
+static std::vector<Workspace*> g_pool;
+
+WorkspaceLease::WorkspaceLease()
+{
+  status = ensure_device();
+  if (status != GBS_SUCCESS) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool.empty()) {
+      ws = g_pool.back();
+      g_pool.pop_back();
+    }
+  }
+  if (!ws) {
+    ws = new Workspace();
+    cudaError_t e = cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      gbs_set_last_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
+      delete ws;
+      ws = nullptr;
+      status = GBS_CUDA_ERROR;
+    }
+  }
+}
+
+WorkspaceLease::~WorkspaceLease()
+{
+  if (!ws) return;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_pool.push_back(ws);
+}
+
+// ------------------------------------------------------------------ status
+int reset_status(DeviceStatus* d_st, cudaStream_t s)
+{
+  DeviceStatus h;
+  memset(&h, 0, sizeof(h));
+  h.info = -1;
+  // the status word is tiny: a kernel-free 32-byte upload per factorization
+  GBS_CUDA_TRY(cudaMemcpyAsync(d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBS_SUCCESS;
+}
+
+int read_status(const DeviceStatus* d_st, DeviceStatus* h_st, cudaStream_t s)
+{
+  GBS_CUDA_TRY(cudaMemcpyAsync(h_st, d_st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h_st->timeout) {
+    gbs_set_last_message("an inter-CTA wait timed out; the factorization was abandoned");
+    return GBS_TIMEOUT;
+  }
+  return GBS_SUCCESS;
+}
+
+static inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// ------------------------------------------------------------------ GEMM launch
+template <typename T>
+static int gemm_sub(cudaStream_t s, int phase, int M, int N, int K, const T* A, int64_t a_rs, int64_t a_cs,
+                    const T* B, int64_t b_rs, int64_t b_cs, T* C, int64_t ldc, int lower, const int* stop_flag)
+{
+  if (M <= 0 || N <= 0 || K <= 0) return GBS_SUCCESS;
+  constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
+  dim3 grid(ceil_div(N, BN), ceil_div(M, BM));
+  if (grid.y > 65535) {
+    gbs_set_last_message("matrix too tall for the GEMM grid");
+    return GBS_INVALID_ARGUMENT;
+  }
+  const double flops = (lower ? 1.0 : 2.0) * M * (double)N * K + (lower ? (double)M * K : 0.0);
+  const double bytes = sizeof(T) * ((double)M * K + (double)K * N + (lower ? 1.0 : 2.0) * M * (double)N);
+  PhaseScope ps(s, phase, flops, bytes);
+  gemm_sub_kernel<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(
+      M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower, stop_flag);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ LU
+template <typename T>
+int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, int i0, int i1, int reverse)
+{
+  if (ncols <= 0 || i1 <= i0) return GBS_SUCCESS;
+  PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)ncols * (i1 - i0));
+  laswp_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(B, ldb, dTr, i0, i1, 0, ncols, 0, 0, reverse);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, DeviceStatus* dSt, DevBuf& scratch)
+{
+  const int size = std::min(m, n);
+  for (int k = 0; k < size; k += kPanelNB) {
+    const int kb = std::min(kPanelNB, size - k);
+    T* Akk = dA + (int64_t)k * lda + k;
+    GBS_TRY(panel_factor<T>(s, Akk, lda, m - k, kb, k, dTr + k, scratch, dSt));
+    // apply the panel's interchanges to A_0 (left) and A_2 (right)
+    const int left = k, right0 = k + kb, nright = n - right0;
+    if (left + nright > 0) {
+      PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)(left + nright) * kb);
+      laswp_kernel<T><<<ceil_div(left + nright, 128), 128, 0, s>>>(dA, lda, dTr, k, k + kb, 0, left, right0, n, 0);
+      GBS_CUDA_TRY(cudaGetLastError());
+    }
+    if (nright > 0) {
+      T* A12 = dA + (int64_t)right0 * lda + k;
+      {
+        PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * nright, sizeof(T) * 2.0 * kb * nright);
+        trsm_lunit_kernel<T, kPanelNB><<<ceil_div(nright, 128), 128, 0, s>>>(Akk, lda, kb, A12, lda, nright);
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
+      const int trows = m - k - kb;
+      if (trows > 0) {
+        const T* A21 = Akk + kb;
+        T* A22 = dA + (int64_t)right0 * lda + k + kb;
+        GBS_TRY(gemm_sub<T>(s, PH_GEMM, trows, nright, kb, A21, 1, lda, A12, 1, lda, A22, lda, 0, nullptr));
+      }
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ LLT
+template <typename T>
+static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* dSt)
+{
+  static bool attr_set = false;
+  const int max_bs = 128;
+  if (!attr_set) {
+    size_t diag = sizeof(T) * max_bs * (max_bs + 1);
+    GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag));
+    size_t trs = sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 64);
+    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trs));
+    attr_set = true;
+  }
+  if (n < 32) {
+    PhaseScope ps(s, PH_POTRF_DIAG, (double)n * n * n / 3.0, sizeof(T) * (double)n * n);
+    potrf_diag_kernel<T><<<1, 256, sizeof(T) * n * (n + 1), s>>>(dA, lda, n, 0, dSt);
+    GBS_CUDA_TRY(cudaGetLastError());
+    return GBS_SUCCESS;
+  }
+  // the reference's block size (LLT.h:338-340): identical blocking keeps the
+  // matrix contents identical to the reference's after an early failure
+  int bs = n / 8;
+  bs = (bs / 16) * 16;
+  bs = std::min(std::max(bs, 8), max_bs);
+  for (int k = 0; k < n; k += bs) {
+    const int b = std::min(bs, n - k);
+    const int rs = n - k - b;
+    T* Akk = dA + (int64_t)k * lda + k;
+    {
+      PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, sizeof(T) * (double)b * b);
+      potrf_diag_kernel<T><<<1, 256, sizeof(T) * b * (b + 1), s>>>(Akk, lda, b, k, dSt);
+      GBS_CUDA_TRY(cudaGetLastError());
+    }
+    if (rs > 0) {
+      T* A21 = Akk + b;
+      {
+      PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, sizeof(T) * 2.0 * rs * b);
+      trsm_rlt_kernel<T, 64><<<ceil_div(rs, 64), 64, sizeof(T) * (b * (b + 1) + b * 64), s>>>(Akk, lda, b, A21, lda,
+                                                                                             rs, dSt);
+      GBS_CUDA_TRY(cudaGetLastError());
+      }
+      T* A22 = A21 + (int64_t)b * lda;
+      GBS_TRY(gemm_sub<T>(s, PH_SYRK, rs, rs, b, A21, 1, lda, A21, lda, 1, A22, lda, 1, &dSt->info));
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceStatus* dSt, DevBuf& tmp)
+{
+  if (n <= 0) return GBS_SUCCESS;
+  if (!upper) return potrf_lower<T>(s, n, dA, lda, dSt);
+  // Upper: the reference factors the transposed view with the lower
+  // algorithm (LLT.h:362-383); same here on a transposed copy.
+  GBS_TRY(tmp.reserve(sizeof(T) * (size_t)n * n));
+  T* L = tmp.as<T>();
+  int64_t tot = (int64_t)n * n;
+  int grid = (int)std::min<int64_t>((tot + 255) / 256, 65535 * 4);
+  {
+    PhaseScope ps(s, PH_COPY, 0.0, sizeof(T) * (double)n * n);
+    transpose_triangle_kernel<T><<<grid, 256, 0, s>>>(dA, lda, L, n, n, 1);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  GBS_TRY(potrf_lower<T>(s, n, L, n, dSt));
+  {
+    PhaseScope ps(s, PH_COPY, 0.0, sizeof(T) * (double)n * n);
+    transpose_triangle_kernel<T><<<grid, 256, 0, s>>>(L, n, dA, lda, n, 0);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ solves
+template <typename T>
+int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
+                     T* B, int64_t ldb)
+{
+  if (n <= 0 || nrhs <= 0) return GBS_SUCCESS;
+  constexpr int NBK = 32;
+  const int64_t rs = trans ? ld : 1, cs = trans ? 1 : ld;   // op(Tri)(i,j) = tri[i*rs + j*cs]
+  const int forward = (lower != 0) != (trans != 0);
+  const int nblk = ceil_div(n, NBK);
+  for (int bb = 0; bb < nblk; ++bb) {
+    const int b = forward ? bb : nblk - 1 - bb;
+    const int j0 = b * NBK, jb = std::min(NBK, n - j0);
+    const T* diag = tri + j0 * rs + j0 * cs;
+    {
+    PhaseScope ps(s, PH_TRI_SOLVE, (double)jb * jb * nrhs, sizeof(T) * ((double)jb * jb + 2.0 * jb * nrhs));
+    trsv_block_kernel<T, NBK><<<ceil_div(nrhs, 128), 128, 0, s>>>(diag, rs, cs, jb, forward, unit, B + j0, ldb, nrhs);
+    GBS_CUDA_TRY(cudaGetLastError());
+    }
+    if (forward) {
+      const int r0 = j0 + jb, mr = n - r0;
+      if (mr > 0)
+        GBS_TRY(gemm_sub<T>(s, PH_TRI_SOLVE, mr, nrhs, jb, tri + r0 * rs + j0 * cs, rs, cs, B + j0, 1, ldb, B + r0, ldb, 0,
+                            nullptr));
+    } else {
+      const int mr = j0;
+      if (mr > 0)
+        GBS_TRY(gemm_sub<T>(s, PH_TRI_SOLVE, mr, nrhs, jb, tri + j0 * cs, rs, cs, B + j0, 1, ldb, B, ldb, 0, nullptr));
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+int lu_solve_device(cudaStream_t s, int n, int nrhs, const T* dLU, int64_t ld, const int* dTr, T* B, int64_t ldb,
+                    int transpose)
+{
+  if (!transpose) {
+    GBS_TRY(laswp_device<T>(s, B, ldb, nrhs, dTr, 0, n, 0));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 0, 1, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 0, 0, B, ldb));
+  } else {
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 1, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 1, 1, B, ldb));
+    GBS_TRY(laswp_device<T>(s, B, ldb, nrhs, dTr, 0, n, 1));
+  }
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb)
+{
+  if (!upper) {
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 0, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 1, 0, B, ldb));
+  } else {
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 1, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 0, 0, B, ldb));
+  }
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+int copy_matrix_device(cudaStream_t s, const T* a, int64_t lda, T* b, int64_t ldb, int m, int n)
+{
+  if (m <= 0 || n <= 0) return GBS_SUCCESS;
+  GBS_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * sizeof(T), a, lda * sizeof(T), (size_t)m * sizeof(T), n,
+                                 cudaMemcpyDeviceToDevice, s));
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ norms
+template <typename T>
+int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int sym, int upper, double* d_out,
+                   double* h_out)
+{
+  GBS_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(double), s));
+  if (m > 0 && n > 0) {
+    PhaseScope ps(s, PH_NORM, (double)m * n, sizeof(T) * (double)m * n);
+    const int wpb = 8;
+    if (sym) sym_l1_norm_kernel<T><<<ceil_div(n, wpb), 32 * wpb, 0, s>>>(dA, lda, n, upper, d_out);
+    else l1_norm_kernel<T><<<ceil_div(n, wpb), 32 * wpb, 0, s>>>(dA, lda, m, n, d_out);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  if (h_out) {
+    GBS_CUDA_TRY(cudaMemcpyAsync(h_out, d_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ rcond
+// ConditionEstimator.h:56-142.  The control flow (sign vectors, argmax, bound
+// comparisons) runs on the host on n-vectors read back after each solve.
+template <typename T>
+static int dec_solve(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr, T* v, int adjoint)
+{
+  if (kind == 0) return lu_solve_device<T>(s, n, 1, dF, ld, dTr, v, n, adjoint);
+  return llt_solve_device<T>(s, n, 1, dF, ld, kind == 2, v, n);
+}
+
+template <typename T>
+int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr, DevBuf& vec,
+                           HostBuf& hvec, double* est)
+{
+  if (n == 0) { *est = 0; return GBS_SUCCESS; }
+  GBS_TRY(vec.reserve(sizeof(T) * (size_t)n));
+  GBS_TRY(hvec.reserve(sizeof(T) * (size_t)n * 3));
+  T* dv = vec.as<T>();
+  T* hv = (T*)hvec.p;
+  T* sgn = hv + n;
+  T* old_sgn = hv + 2 * (size_t)n;
+  auto upload = [&]() -> int {
+    GBS_CUDA_TRY(cudaMemcpyAsync(dv, hv, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    return GBS_SUCCESS;
+  };
+  auto download = [&]() -> int {
+    GBS_CUDA_TRY(cudaMemcpyAsync(hv, dv, sizeof(T) * n, cudaMemcpyDeviceToHost, s));
+    GBS_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBS_SUCCESS;
+  };
+  auto l1 = [&]() {
+    T acc = 0;
+    for (int i = 0; i < n; ++i) acc += hv[i] < 0 ? -hv[i] : hv[i];
+    return acc;
+  };
+  for (int i = 0; i < n; ++i) hv[i] = T(1) / T(n);
+  GBS_TRY(upload());
+  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+  GBS_TRY(download());
+  T lower_bound = l1();
+  if (n == 1) { *est = (double)lower_bound; return GBS_SUCCESS; }
+  T old_lower_bound = lower_bound;
+  int vmax = -1, old_vmax = -1;
+  for (int k = 0; k < 4; ++k) {
+    for (int i = 0; i < n; ++i) sgn[i] = hv[i] < T(0) ? T(-1) : T(1);
+    if (k > 0 && memcmp(sgn, old_sgn, sizeof(T) * n) == 0) break;
+    for (int i = 0; i < n; ++i) hv[i] = sgn[i];
+    GBS_TRY(upload());
+    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 1));
+    GBS_TRY(download());
+    vmax = 0;
+    T best = hv[0] < 0 ? -hv[0] : hv[0];
+    for (int i = 1; i < n; ++i) {
+      T t = hv[i] < 0 ? -hv[i] : hv[i];
+      if (t > best) { best = t; vmax = i; }
+    }
+    if (vmax == old_vmax) break;
+    for (int i = 0; i < n; ++i) hv[i] = T(0);
+    hv[vmax] = T(1);
+    GBS_TRY(upload());
+    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+    GBS_TRY(download());
+    lower_bound = l1();
+    if (lower_bound <= old_lower_bound) break;
+    memcpy(old_sgn, sgn, sizeof(T) * n);
+    old_vmax = vmax;
+    old_lower_bound = lower_bound;
+  }
+  T alt = 1;
+  for (int i = 0; i < n; ++i) {
+    hv[i] = alt * (T(1) + (T(i) / T(n - 1)));
+    alt = -alt;
+  }
+  GBS_TRY(upload());
+  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+  GBS_TRY(download());
+  T alternate = (T(2) * l1()) / (T(3) * T(n));
+  *est = (double)(lower_bound > alternate ? lower_bound : alternate);
+  return GBS_SUCCESS;
+}
+
+// ConditionEstimator.h:157-169, evaluated in the scalar type of the factor.
+double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool single)
+{
+  if (n == 0) return 1.0;
+  if (single) {
+    float mn = (float)matrix_norm, inv = (float)inv_norm;
+    if (mn == 0.0f) return 0.0;
+    if (n == 1) return 1.0;
+    return inv == 0.0f ? 0.0 : (double)((1.0f / inv) / mn);
+  }
+  if (matrix_norm == 0.0) return 0.0;
+  if (n == 1) return 1.0;
+  return inv_norm == 0.0 ? 0.0 : (1.0 / inv_norm) / matrix_norm;
+}
+
+// ------------------------------------------------------------------ instantiations
+#define GBS_INSTANTIATE(T)                                                                                      \
+  template int getrf_device<T>(cudaStream_t, int, int, T*, int64_t, int*, DeviceStatus*, DevBuf&);               \
+  template int potrf_device<T>(cudaStream_t, int, T*, int64_t, int, DeviceStatus*, DevBuf&);                     \
+  template int tri_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, int, int, T*, int64_t);       \
+  template int laswp_device<T>(cudaStream_t, T*, int64_t, int, const int*, int, int, int);                       \
+  template int lu_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, T*, int64_t, int);      \
+  template int llt_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, T*, int64_t);                 \
+  template int l1_norm_device<T>(cudaStream_t, const T*, int64_t, int, int, int, int, double*, double*);         \
+  template int inv_l1_estimate_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, DevBuf&, HostBuf&, \
+                                         double*);                                                               \
+  template int copy_matrix_device<T>(cudaStream_t, const T*, int64_t, T*, int64_t, int, int);
+
+GBS_INSTANTIATE(double)
+GBS_INSTANTIATE(float)
+
+}  // namespace gbs

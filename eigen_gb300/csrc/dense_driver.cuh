@@ -1,0 +1,109 @@
+// Host-side drivers of the plain factor-and-solve path (declarations shared by
+// the C-ABI translation unit and the mixed-precision / batched units).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <vector>
+
+#include "gbs_common.cuh"
+
+namespace gbs {
+
+int ensure_device();
+int device_sm_count();
+
+// Growable device buffer; never shrinks.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t b);
+  void release();
+  template <typename U> U* as() const { return (U*)p; }
+  ~DevBuf() { release(); }
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+// Pinned host staging buffer; never shrinks.
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t b);
+  void release();
+  ~HostBuf() { release(); }
+  HostBuf() = default;
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+};
+
+// Per-call workspace for the stateless (plug-in / LAPACK) entry points: a
+// stream plus buffers, taken from a process-wide pool so concurrent host
+// threads never share one.
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  DevBuf a, piv, status, scratch, b, vec;
+  HostBuf hvec;
+};
+struct WorkspaceLease {
+  Workspace* ws = nullptr;
+  int status = GBS_SUCCESS;
+  WorkspaceLease();
+  ~WorkspaceLease();
+};
+
+// ---- plain-path drivers (device pointers, stream-ordered; the status word
+// must be zero-initialised with info = -1 before a factorization)
+int reset_status(DeviceStatus* d_st, cudaStream_t s);
+int read_status(const DeviceStatus* d_st, DeviceStatus* h_st, cudaStream_t s);
+
+constexpr int kPanelNB = 32;   // columns factored per panel launch
+
+// Unblocked partial-pivoting LU of the m x nbc panel at `a` (nbc <= kPanelNB);
+// writes absolute pivot rows k0 + p into tr[0..nbc).  Cooperative launch.
+template <typename T>
+int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
+                 DeviceStatus* st);
+
+template <typename T>
+int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, DeviceStatus* dSt, DevBuf& scratch);
+
+template <typename T>
+int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceStatus* dSt, DevBuf& tmp);
+
+// op(Tri) X = B in place on B (n x nrhs, ldb).  lower: which triangle of tri
+// holds the factor; trans: solve with its transpose; unit: unit diagonal.
+template <typename T>
+int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
+                     T* B, int64_t ldb);
+
+template <typename T>
+int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, int i0, int i1, int reverse);
+
+// A x = b with PA = LU (transpose: A^T x = b), in place on B.
+template <typename T>
+int lu_solve_device(cudaStream_t s, int n, int nrhs, const T* dLU, int64_t ld, const int* dTr, T* B, int64_t ldb,
+                    int transpose);
+
+template <typename T>
+int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb);
+
+template <typename T>
+int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int sym, int upper, double* d_out,
+                   double* h_out);
+
+// Hager/Higham estimate of ||A^{-1}||_1 (ConditionEstimator.h:56-142); kind 0 = LU,
+// 1 = LLT lower, 2 = LLT upper.  `vec` holds 2n scalars of device scratch.
+template <typename T>
+int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr,
+                           DevBuf& vec, HostBuf& hvec, double* est);
+
+double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool single);
+
+template <typename T>
+int copy_matrix_device(cudaStream_t s, const T* a, int64_t lda, T* b, int64_t ldb, int m, int n);
+
+}  // namespace gbs

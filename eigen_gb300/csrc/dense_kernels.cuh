@@ -1,0 +1,525 @@
+// Kernels of the plain (FP64 / FP32) factor-and-solve path.  All matrices are
+// column-major with a leading dimension, as the reference stores them.
+//
+//   panel_lu_kernel      unblocked partial-pivoting LU of an m x NB panel
+//                        (PartialPivLU.h:365-409): rows live in registers, pivot
+//                        search is a warp-shuffle argmax + a grid-wide reduction
+//   laswp_kernel         row interchanges on column ranges (PartialPivLU.h:477-487)
+//   trsm_lunit_kernel    A12 <- L11^{-1} A12, unit lower (PartialPivLU.h:490)
+//   gemm_sub_kernel      C -= op(A) op(B), optional lower-triangle-only mode for
+//                        SYRK (PartialPivLU.h:492, LLT.h:357)
+//   potrf_diag_kernel    left-looking Cholesky of one diagonal block (LLT.h:305-328)
+//   trsm_rlt_kernel      A21 <- A21 L11^{-T} (LLT.h:356)
+//   trsv_block_kernel    one diagonal block of a triangular solve (LLT.h:499-505,
+//                        PartialPivLU.h:224-271)
+//   norm kernels         ||A||_1 (PartialPivLU.h:522, LLT.h:434-445)
+#pragma once
+
+#include <math.h>
+
+#include "gbs_common.cuh"
+
+namespace gbs {
+
+// --------------------------------------------------------------------- panel LU
+// Grid-cooperative: every CTA owns a slice of the panel's rows, each thread
+// RPT rows, each row NB values in registers.  One grid barrier per column.
+// Scratch layout (global): cand_val[2][P], cand_idx[2][P], cand_row[2][P][NB],
+// rowj[2][NB] -- double-buffered by column parity so CTA c can publish column
+// j+1's candidate while others still read column j's.
+template <typename T, int NB>
+struct PanelScratchView {
+  T* cand_val;
+  int* cand_idx;
+  T* cand_row;
+  T* rowj;
+  __device__ PanelScratchView(void* base, int P)
+  {
+    char* p = (char*)base;
+    cand_val = (T*)p;            p += sizeof(T) * 2 * P;
+    cand_row = (T*)p;            p += sizeof(T) * 2 * (size_t)P * NB;
+    rowj = (T*)p;                p += sizeof(T) * 2 * NB;
+    cand_idx = (int*)p;
+  }
+};
+
+template <typename T, int NB>
+inline size_t panel_scratch_bytes(int P)
+{
+  return sizeof(T) * (2 * (size_t)P + 2 * (size_t)P * NB + 2 * NB) + sizeof(int) * 2 * (size_t)P + 256;
+}
+
+constexpr int kPanelThreads = 256;
+
+template <typename T, int NB, int RPT>
+__global__ void __launch_bounds__(kPanelThreads)
+panel_lu_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, int* __restrict__ tr,
+                void* scratch, DeviceStatus* st)
+{
+  const int P = gridDim.x;
+  PanelScratchView<T, NB> w(scratch, P);
+  const int tid = threadIdx.x;
+  const int g = blockIdx.x * kPanelThreads + tid;
+  const int G = P * kPanelThreads;
+  const int lane = tid & 31, warp = tid >> 5;
+
+  __shared__ T s_u[NB];
+  __shared__ T s_oldj[NB];
+  __shared__ T s_wval[kPanelThreads / 32];
+  __shared__ int s_widx[kPanelThreads / 32];
+  __shared__ int s_piv, s_win;
+
+  T v[RPT][NB];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const int r = g + q * G;
+#pragma unroll
+    for (int c = 0; c < NB; ++c) v[q][c] = (r < m && c < nbc) ? a[(int64_t)c * lda + r] : T(0);
+  }
+
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    if (j >= nbc) break;
+    const int par = j & 1;
+    // ---- local candidate: first max of |a(r,j)|, r >= j (Visitor.h:173-186)
+    T bs = T(-2);
+    int bi = 0x7fffffff;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int r = g + q * G;
+      if (r < m && r >= j) {
+        T x = v[q][j];
+        T s = (r == j) ? ((x != x) ? T(INFINITY) : gbs_abs(x)) : pivot_score(x);
+        if (better(s, r, bs, bi)) { bs = s; bi = r; }
+      }
+    }
+    warp_argmax(bs, bi);
+    if (lane == 0) { s_wval[warp] = bs; s_widx[warp] = bi; }
+    __syncthreads();
+    if (warp == 0) {
+      bs = lane < kPanelThreads / 32 ? s_wval[lane] : T(-2);
+      bi = lane < kPanelThreads / 32 ? s_widx[lane] : 0x7fffffff;
+      warp_argmax(bs, bi);
+      if (lane == 0) {
+        w.cand_val[par * P + blockIdx.x] = bs;
+        w.cand_idx[par * P + blockIdx.x] = bi;
+        s_win = bi;
+      }
+    }
+    __syncthreads();
+    {
+      const int winner = s_win;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int r = g + q * G;
+        if (r < m && r == winner) {
+#pragma unroll
+          for (int c = 0; c < NB; ++c) w.cand_row[((size_t)par * P + blockIdx.x) * NB + c] = v[q][c];
+        }
+        if (r < m && r == j) {
+#pragma unroll
+          for (int c = 0; c < NB; ++c) w.rowj[par * NB + c] = v[q][c];
+        }
+      }
+    }
+    if (!grid_barrier(st, P)) return;
+    // ---- global pivot: every CTA reduces the P candidates itself
+    if (warp == 0) {
+      T s = T(-2);
+      int i = 0x7fffffff, cw = 0;
+      for (int c = lane; c < P; c += 32) {
+        T sc = ((volatile T*)w.cand_val)[par * P + c];
+        int ic = ((volatile int*)w.cand_idx)[par * P + c];
+        if (better(sc, ic, s, i)) { s = sc; i = ic; cw = c; }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        T so = __shfl_xor_sync(0xffffffffu, s, off);
+        int io = __shfl_xor_sync(0xffffffffu, i, off);
+        int co = __shfl_xor_sync(0xffffffffu, cw, off);
+        if (better(so, io, s, i)) { s = so; i = io; cw = co; }
+      }
+      if (lane == 0) { s_piv = i; s_win = cw; }
+    }
+    __syncthreads();
+    const int p = s_piv;
+    for (int c = tid; c < NB; c += kPanelThreads) {
+      s_u[c] = ((volatile T*)w.cand_row)[((size_t)par * P + s_win) * NB + c];
+      s_oldj[c] = ((volatile T*)w.rowj)[par * NB + c];
+    }
+    __syncthreads();
+    const T piv = s_u[j];
+    const bool nz = (piv != T(0));   // biggest_in_corner != 0 (NaN counts as nonzero)
+    if (blockIdx.x == 0 && tid == 0) {
+      tr[j] = k0 + p;
+      if (nz && p != j) st->nb_transpositions += 1;
+      if (!nz && st->info < 0) st->info = k0 + j;
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int r = g + q * G;
+      if (r >= m) continue;
+      if (nz && p != j) {
+        if (r == j) {
+#pragma unroll
+          for (int c = 0; c < NB; ++c) v[q][c] = s_u[c];
+        } else if (r == p) {
+#pragma unroll
+          for (int c = 0; c < NB; ++c) v[q][c] = s_oldj[c];
+        }
+      }
+      if (r > j) {
+        if (nz) v[q][j] = v[q][j] / piv;
+        const T l = v[q][j];
+#pragma unroll
+        for (int c = j + 1; c < NB; ++c) v[q][c] = fma(-l, s_u[c], v[q][c]);
+      }
+    }
+    // s_u / s_oldj are rewritten next column only after the next barrier
+  }
+
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const int r = g + q * G;
+    if (r < m) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c)
+        if (c < nbc) a[(int64_t)c * lda + r] = v[q][c];
+    }
+  }
+}
+
+// --------------------------------------------------------------------- laswp
+// Applies the interchanges tr[i0..i1) (absolute row indices, in order, or in
+// reverse order when reverse != 0) to the columns [c0, c1) and [c2, c3).
+template <typename T>
+__global__ void laswp_kernel(T* __restrict__ a, int64_t lda, const int* __restrict__ tr, int i0, int i1,
+                             int c0, int c1, int c2, int c3, int reverse)
+{
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int n1 = c1 - c0;
+  int col;
+  if (t < n1) col = c0 + (int)t;
+  else if (t < n1 + (c3 - c2)) col = c2 + (int)(t - n1);
+  else return;
+  T* ac = a + (int64_t)col * lda;
+  if (!reverse) {
+    for (int i = i0; i < i1; ++i) {
+      int p = tr[i];
+      if (p != i) { T x = ac[i]; ac[i] = ac[p]; ac[p] = x; }
+    }
+  } else {
+    for (int i = i1 - 1; i >= i0; --i) {
+      int p = tr[i];
+      if (p != i) { T x = ac[i]; ac[i] = ac[p]; ac[p] = x; }
+    }
+  }
+}
+
+// --------------------------------------------------------------------- TRSM (LU)
+// B(nb x ncols) <- L^{-1} B, L unit lower nb x nb (nb <= NB).  One thread per
+// column of B, the column in registers, L in shared memory.
+template <typename T, int NB>
+__global__ void __launch_bounds__(128)
+trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int nb, T* __restrict__ B, int64_t ldb, int ncols)
+{
+  __shared__ T sL[NB][NB + 1];
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    int i = e % NB, p = e / NB;
+    sL[i][p] = (i < nb && p < nb) ? L[(int64_t)p * ldl + i] : T(0);
+  }
+  __syncthreads();
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  T* b = B + (int64_t)col * ldb;
+  T x[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) x[i] = i < nb ? b[i] : T(0);
+#pragma unroll
+  for (int p = 0; p < NB; ++p) {
+#pragma unroll
+    for (int i = p + 1; i < NB; ++i) x[i] = fma(-sL[i][p], x[p], x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+    if (i < nb) b[i] = x[i];
+}
+
+// --------------------------------------------------------------------- GEMM
+// C(M x N) -= op(A)(M x K) * op(B)(K x N) with op given by element strides:
+// A(i,k) = A[i*a_rs + k*a_cs], B(k,j) = B[k*b_rs + j*b_cs].  lower != 0 keeps
+// only the lower triangle of C (i >= j; SYRK).  Skips all work when
+// `stop_flag` is non-null and >= 0 (an earlier LLT block failed).
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+gemm_sub_kernel(int M, int N, int K, const T* __restrict__ A, int64_t a_rs, int64_t a_cs,
+                const T* __restrict__ B, int64_t b_rs, int64_t b_cs, T* __restrict__ C, int64_t ldc,
+                int lower, const int* stop_flag)
+{
+  constexpr int TX = BN / TN, TY = BM / TM, NT = TX * TY;
+  const int bm = blockIdx.y * BM, bn = blockIdx.x * BN;
+  if (lower && bn >= bm + BM) return;                 // tile strictly above the diagonal
+  if (stop_flag && ld_volatile_i32(stop_flag) >= 0) return;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += NT) {
+      int i = e % BM, kk = e / BM;
+      int gi = bm + i, gk = k0 + kk;
+      As[kk][i] = (gi < M && gk < K) ? A[(int64_t)gi * a_rs + (int64_t)gk * a_cs] : T(0);
+    }
+    for (int e = tid; e < BN * BK; e += NT) {
+      int kk = e % BK, j = e / BK;
+      int gj = bn + j, gk = k0 + kk;
+      Bs[kk][j] = (gj < N && gk < K) ? B[(int64_t)gk * b_rs + (int64_t)gj * b_cs] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T af[TM], bf[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) af[i] = As[kk][ty + i * TY];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) bf[j] = Bs[kk][tx + j * TX];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(af[i], bf[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < TN; ++j) {
+    int gj = bn + tx + j * TX;
+    if (gj >= N) continue;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      int gi = bm + ty + i * TY;
+      if (gi >= M) continue;
+      if (lower && gi < gj) continue;
+      T* c = C + (int64_t)gj * ldc + gi;
+      *c = *c - acc[i][j];
+    }
+  }
+}
+
+// --------------------------------------------------------------------- LLT diag
+// Left-looking Cholesky of the bs x bs diagonal block in shared memory,
+// exactly the order of LLT.h:305-328: x = a_kk - ||A10||^2, fail if x <= 0,
+// x = sqrt(x), A21 = (A21 - A20 A10^T) / x.  On failure writes k0 + k into
+// st->info and leaves later columns untouched (as the reference returns).
+// Only the lower triangle is read or written.  Dynamic smem: bs*(bs+1)*sizeof(T).
+template <typename T>
+__global__ void __launch_bounds__(256)
+potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* st)
+{
+  if (st->info >= 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s = (T*)smem_raw;
+  const int ld = bs + 1;
+  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
+    int i = e % bs, j = e / bs;
+    if (i >= j) s[j * ld + i] = a[(int64_t)j * lda + i];
+  }
+  __syncthreads();
+  __shared__ T s_x;
+  __shared__ int s_fail;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < bs; ++k) {
+    if (warp == 0) {
+      T acc = T(0);
+      for (int j = lane; j < k; j += 32) acc = fma(s[j * ld + k], s[j * ld + k], acc);
+      acc = warp_sum(acc);
+      if (lane == 0) {
+        T x = s[k * ld + k] - acc;
+        s_fail = !(x > T(0)) && !(x != x) ? 1 : 0;   // x <= 0 (a NaN does not fail, as in the reference)
+        s_x = x;
+      }
+    }
+    __syncthreads();
+    if (s_fail) {
+      if (threadIdx.x == 0) st->info = k0 + k;
+      // write back the columns already final (0..k-1); column k.. untouched
+      for (int e = threadIdx.x; e < bs * k; e += blockDim.x) {
+        int i = e % bs, j = e / bs;
+        if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
+      }
+      return;
+    }
+    const T x = sqrt(s_x);
+    // rows i > k: one warp per row, dot product over j < k
+    for (int i = k + 1 + warp; i < bs; i += nw) {
+      T acc = T(0);
+      for (int j = lane; j < k; j += 32) acc = fma(s[j * ld + i], s[j * ld + k], acc);
+      acc = warp_sum(acc);
+      if (lane == 0) s[k * ld + i] = (s[k * ld + i] - acc) / x;
+    }
+    if (threadIdx.x == 0) s[k * ld + k] = x;
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
+    int i = e % bs, j = e / bs;
+    if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
+  }
+}
+
+// --------------------------------------------------------------------- LLT TRSM
+// X(m x bs) <- X L^{-T}, L lower bs x bs.  One thread per row of X; the CTA's
+// rows and L live in shared memory.  Dynamic smem: (bs*(bs+1) + bs*RT)*sizeof(T).
+template <typename T, int RT>
+__global__ void __launch_bounds__(RT)
+trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X, int64_t ldx, int m,
+                const DeviceStatus* st)
+{
+  if (st && ld_volatile_i32(&st->info) >= 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sL = (T*)smem_raw;              // sL[j*(bs+1) + l] = L(j,l)
+  T* sX = sL + bs * (bs + 1);        // sX[c*RT + t]
+  const int ldL = bs + 1;
+  for (int e = threadIdx.x; e < bs * bs; e += RT) {
+    int j = e % bs, l = e / bs;
+    if (j >= l) sL[j * ldL + l] = L[(int64_t)l * ldl + j];
+  }
+  const int r0 = blockIdx.x * RT;
+  for (int e = threadIdx.x; e < bs * RT; e += RT) {
+    int t = e % RT, c = e / RT;
+    int r = r0 + t;
+    sX[c * RT + t] = r < m ? X[(int64_t)c * ldx + r] : T(0);
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  for (int j = 0; j < bs; ++j) {
+    T s = sX[j * RT + t];
+    for (int l = 0; l < j; ++l) s = fma(-sX[l * RT + t], sL[j * ldL + l], s);
+    sX[j * RT + t] = s / sL[j * ldL + j];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < bs * RT; e += RT) {
+    int tt = e % RT, c = e / RT;
+    int r = r0 + tt;
+    if (r < m) X[(int64_t)c * ldx + r] = sX[c * RT + tt];
+  }
+}
+
+// --------------------------------------------------------------------- TRSV block
+// Solves one nb x nb diagonal block (nb <= NB) of op(Tri) X = B for all nrhs
+// columns, one thread per column.  op(Tri)(i,j) = tri[i*rs + j*cs].  forward:
+// lower-triangular op (rows top to bottom); else upper (bottom to top).
+template <typename T, int NB>
+__global__ void __launch_bounds__(128)
+trsv_block_kernel(const T* __restrict__ tri, int64_t rs, int64_t cs, int nb, int forward, int unit,
+                  T* __restrict__ B, int64_t ldb, int nrhs)
+{
+  __shared__ T sT[NB][NB + 1];
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    int i = e % NB, j = e / NB;
+    sT[i][j] = (i < nb && j < nb) ? tri[(int64_t)i * rs + (int64_t)j * cs] : T(0);
+  }
+  __syncthreads();
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= nrhs) return;
+  T* b = B + (int64_t)col * ldb;
+  T x[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) x[i] = i < nb ? b[i] : T(0);
+  if (forward) {
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      if (j < nb) {
+        if (!unit) x[j] = x[j] / sT[j][j];
+#pragma unroll
+        for (int i = j + 1; i < NB; ++i) x[i] = fma(-sT[i][j], x[j], x[i]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int jj = NB - 1; jj >= 0; --jj) {
+      if (jj < nb) {
+        if (!unit) x[jj] = x[jj] / sT[jj][jj];
+#pragma unroll
+        for (int i = 0; i < jj; ++i) x[i] = fma(-sT[i][jj], x[jj], x[i]);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+    if (i < nb) b[i] = x[i];
+}
+
+// --------------------------------------------------------------------- norms
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v)
+{
+  if (!(v >= 0.0)) return;
+  atomicMax((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// max_j sum_i |a(i,j)| (one warp per column); out must start at 0.
+template <typename T>
+__global__ void l1_norm_kernel(const T* __restrict__ a, int64_t lda, int m, int n, double* out)
+{
+  int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (col >= n) return;
+  const T* c = a + (int64_t)col * lda;
+  T s = T(0);
+  for (int i = lane; i < m; i += 32) s += gbs_abs(c[i]);
+  s = warp_sum(s);
+  if (lane == 0) atomic_max_nonneg(out, (double)s);
+}
+
+// Symmetric ||A||_1 reading only the stored triangle (LLT.h:434-445).
+template <typename T>
+__global__ void sym_l1_norm_kernel(const T* __restrict__ a, int64_t lda, int n, int upper, double* out)
+{
+  int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (col >= n) return;
+  T s = T(0);
+  if (!upper) {
+    for (int i = col + lane; i < n; i += 32) s += gbs_abs(a[(int64_t)col * lda + i]);
+    for (int j = lane; j < col; j += 32) s += gbs_abs(a[(int64_t)j * lda + col]);
+  } else {
+    for (int i = lane; i < col; i += 32) s += gbs_abs(a[(int64_t)col * lda + i]);
+    for (int j = col + lane; j < n; j += 32) s += gbs_abs(a[(int64_t)j * lda + col]);
+  }
+  s = warp_sum(s);
+  if (lane == 0) atomic_max_nonneg(out, (double)s);
+}
+
+// Copies an m x n column-major block (lda -> ldb), optionally converting type.
+template <typename TI, typename TO>
+__global__ void copy_matrix_kernel(const TI* __restrict__ a, int64_t lda, TO* __restrict__ b, int64_t ldb,
+                                   int m, int n)
+{
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = (int64_t)m * n;
+  for (; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % m), j = (int)(t / m);
+    b[(int64_t)j * ldb + i] = (TO)a[(int64_t)j * lda + i];
+  }
+}
+
+// out(j,i) = in(i,j) for i,j in the stored triangle: moves the upper triangle
+// of `a` to the lower triangle of `b` (to_lower) or back.
+template <typename T>
+__global__ void transpose_triangle_kernel(const T* __restrict__ a, int64_t lda, T* __restrict__ b, int64_t ldb,
+                                          int n, int to_lower)
+{
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = (int64_t)n * n;
+  for (; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % n), j = (int)(t / n);
+    if (to_lower) { if (i >= j) b[(int64_t)j * ldb + i] = a[(int64_t)i * lda + j]; }
+    else          { if (i <= j) b[(int64_t)j * ldb + i] = a[(int64_t)i * lda + j]; }
+  }
+}
+
+}  // namespace gbs

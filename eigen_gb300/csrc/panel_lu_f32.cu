@@ -1,0 +1,6 @@
+// Panel LU instantiation for float.
+#include "panel_lu_impl.cuh"
+
+namespace gbs {
+template int panel_factor<float>(cudaStream_t, float*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*);
+}  // namespace gbs

@@ -1,0 +1,6 @@
+// Panel LU instantiation for double.
+#include "panel_lu_impl.cuh"
+
+namespace gbs {
+template int panel_factor<double>(cudaStream_t, double*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*);
+}  // namespace gbs

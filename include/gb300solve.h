@@ -1,0 +1,175 @@
+/*
+ * libgb300solve -- GB300 (sm_103a) dense factor-and-solve behind a C ABI.
+ *
+ * Drop-in boundary for Eigen's dense factor-and-solve path (Eigen 3.3.90):
+ * plain pointers and sizes, column-major storage with a leading dimension,
+ * no C++ or torch types.  Three layers, each mirroring an existing reference
+ * interface:
+ *
+ *   1. Plug-in level -- the two functions Eigen's LAPACKE backend replaces
+ *      (Eigen/src/Cholesky/LLT_LAPACKE.h:42-93,
+ *       Eigen/src/LU/PartialPivLU_LAPACKE.h:42-77).  Same return values as
+ *      llt_inplace<>::blocked (LLT.h:331-360) and
+ *      partial_lu_impl<>::blocked_lu (PartialPivLU.h:426-496).
+ *   2. LAPACK level -- same semantics as the reference's own LAPACK shim
+ *      (lapack/lu.cpp:14-89, lapack/cholesky.cpp:14-72): 1-based ipiv,
+ *      info < 0 for a bad argument, info = k+1 for the first zero pivot /
+ *      failing column.  Bad arguments are reported through info only.
+ *   3. Decomposition objects -- device-resident factors mirroring
+ *      Eigen::LLT / Eigen::PartialPivLU (compute, info, solve, rcond,
+ *      matrixLLT / matrixLU, permutationP, determinant), with host-buffer and
+ *      device-buffer variants.
+ *
+ * All entry points return a gbs_status.  There is no CPU fallback: if no
+ * usable sm_103a device is present every call returns GBS_NO_DEVICE.
+ * Objects are not thread-safe; distinct objects may be used from distinct host
+ * threads concurrently (each owns its stream and workspace).
+ */
+#ifndef GB300SOLVE_H
+#define GB300SOLVE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbs_status {
+  GBS_SUCCESS = 0,
+  GBS_NUMERICAL_ISSUE = 1,    /* Eigen::NumericalIssue (Constants.h:434-444) */
+  GBS_INVALID_ARGUMENT = 2,   /* Eigen::InvalidInput */
+  GBS_NO_CONVERGENCE = 3,     /* Eigen::NoConvergence: refinement stalled */
+  GBS_CUDA_ERROR = 4,
+  GBS_NO_DEVICE = 5,
+  GBS_TIMEOUT = 6,            /* an inter-CTA wait ran out of time; context stays usable */
+  GBS_NOT_INITIALIZED = 7,
+  GBS_OUT_OF_MEMORY = 8
+} gbs_status;
+
+typedef enum gbs_dtype { GBS_F64 = 0, GBS_F32 = 1 } gbs_dtype;
+typedef enum gbs_uplo { GBS_LOWER = 0, GBS_UPPER = 1 } gbs_uplo;
+
+/* Last error text of the calling thread (never NULL). */
+const char* gbs_last_error(void);
+/* Library version string. */
+const char* gbs_version(void);
+/* Number of usable sm_103a devices (0 when none). */
+int gbs_device_count(void);
+
+/* ------------------------------------------------------------------ 1. plug-in
+ * Replaces internal::llt_inplace<Scalar,Lower|Upper>::blocked(m)
+ * (Eigen/src/Cholesky/LLT.h:331-360; LAPACKE form LLT_LAPACKE.h:64-88).
+ * a: host, column-major n x n, lda >= n; the lower (upper) triangle is read
+ * and overwritten by L (U = L^T); the other triangle is left untouched.
+ * Returns -1 on success, else the 0-based first column whose pivot is not
+ * positive (the matrix is then left as the reference leaves it: columns before
+ * that block factored, later blocks untouched).  A negative status below -1 is
+ * -(100 + gbs_status) on a library error. */
+int64_t gbs_llt_blocked_d(int64_t n, double* a, int64_t lda, int upper);
+int64_t gbs_llt_blocked_s(int64_t n, float* a, int64_t lda, int upper);
+
+/* Replaces internal::partial_lu_impl<Scalar,ColMajor,int>::blocked_lu
+ * (Eigen/src/LU/PartialPivLU.h:426-496; LAPACKE form PartialPivLU_LAPACKE.h:47-71).
+ * a: host, column-major rows x cols, lda >= rows.  Writes 0-based row
+ * transpositions (min(rows,cols) of them) and the number of actual swaps.
+ * Returns the first exactly-zero pivot or -1; below -1 as above. */
+int64_t gbs_partial_lu_blocked_d(int64_t rows, int64_t cols, double* a, int64_t lda,
+                                 int* row_transpositions, int* nb_transpositions);
+int64_t gbs_partial_lu_blocked_s(int64_t rows, int64_t cols, float* a, int64_t lda,
+                                 int* row_transpositions, int* nb_transpositions);
+
+/* ------------------------------------------------------------------ 2. LAPACK
+ * Same arguments and results as the reference's shim, lapack/lu.cpp:14-41
+ * (getrf) and :46-89 (getrs, trans = 'N'|'T'|'C'), lapack/cholesky.cpp:14-36
+ * (potrf, uplo = 'L'|'U') and :41-72 (potrs).  Host buffers. */
+int gbs_dgetrf(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info);
+int gbs_sgetrf(const int* m, const int* n, float* a, const int* lda, int* ipiv, int* info);
+int gbs_dgetrs(const char* trans, const int* n, const int* nrhs, const double* a, const int* lda,
+               const int* ipiv, double* b, const int* ldb, int* info);
+int gbs_sgetrs(const char* trans, const int* n, const int* nrhs, const float* a, const int* lda,
+               const int* ipiv, float* b, const int* ldb, int* info);
+int gbs_dpotrf(const char* uplo, const int* n, double* a, const int* lda, int* info);
+int gbs_spotrf(const char* uplo, const int* n, float* a, const int* lda, int* info);
+int gbs_dpotrs(const char* uplo, const int* n, const int* nrhs, const double* a, const int* lda,
+               double* b, const int* ldb, int* info);
+int gbs_spotrs(const char* uplo, const int* n, const int* nrhs, const float* a, const int* lda,
+               float* b, const int* ldb, int* info);
+
+/* ------------------------------------------------------------------ 3. objects
+ * gbs_llt mirrors Eigen::LLT<Matrix<S,Dynamic,Dynamic>, UpLo> (LLT.h:56-230):
+ *   compute   LLT::compute (LLT.h:424-452): copy, ||A||_1 (symmetric, stored
+ *             triangle read), blocked factorization, info.
+ *   info      LLT::info(): GBS_SUCCESS or GBS_NUMERICAL_ISSUE.
+ *   solve     LLT::solve / _solve_impl (LLT.h:477-505).
+ *   rcond     LLT::rcond (LLT.h:161-166, ConditionEstimator.h:157-169).
+ *   matrix    LLT::matrixLLT (LLT.h:172-176).
+ * Scalars are double for GBS_F64 objects and float for GBS_F32 objects. */
+typedef struct gbs_llt gbs_llt;
+int gbs_llt_create(gbs_llt** out, int dtype, int uplo);
+int gbs_llt_destroy(gbs_llt* llt);
+int gbs_llt_compute(gbs_llt* llt, int64_t n, const void* a, int64_t lda);            /* host A */
+int gbs_llt_compute_device(gbs_llt* llt, int64_t n, const void* d_a, int64_t lda);   /* device A, not modified */
+int gbs_llt_info(const gbs_llt* llt);
+int64_t gbs_llt_failed_column(const gbs_llt* llt);  /* -1 when info() is Success */
+int gbs_llt_solve(gbs_llt* llt, int64_t nrhs, const void* b, int64_t ldb, void* x, int64_t ldx);
+int gbs_llt_solve_device(gbs_llt* llt, int64_t nrhs, const void* d_b, int64_t ldb, void* d_x, int64_t ldx);
+int gbs_llt_rcond(gbs_llt* llt, double* rcond);
+int gbs_llt_l1_norm(const gbs_llt* llt, double* l1);
+int gbs_llt_matrix(gbs_llt* llt, void* out, int64_t ld);   /* whole n x n working matrix (matrixLLT) */
+void* gbs_llt_device_matrix(gbs_llt* llt, int64_t* ld);     /* device pointer of the factor */
+int gbs_llt_synchronize(gbs_llt* llt);
+/* Use a caller-owned CUDA stream (cudaStream_t) instead of the object's own. */
+int gbs_llt_set_stream(gbs_llt* llt, void* stream);
+
+/* gbs_lu mirrors Eigen::PartialPivLU<Matrix<S,Dynamic,Dynamic>> (PartialPivLU.h:75-311):
+ *   compute        PartialPivLU::compute (PartialPivLU.h:514-536)
+ *   matrix         matrixLU()
+ *   permutation    permutationP().indices() (PermutationMatrix.h:82-88)
+ *   transpositions the 0-based row transpositions (m_rowsTranspositions)
+ *   solve          _solve_impl (PartialPivLU.h:224-244); transpose != 0 gives
+ *                  _solve_impl_transposed (PartialPivLU.h:246-271), i.e. A^T x = b
+ *   rcond          PartialPivLU::rcond (PartialPivLU.h:184-188)
+ *   determinant    PartialPivLU::determinant (PartialPivLU.h:539-543) */
+typedef struct gbs_lu gbs_lu;
+int gbs_lu_create(gbs_lu** out, int dtype);
+int gbs_lu_destroy(gbs_lu* lu);
+int gbs_lu_compute(gbs_lu* lu, int64_t n, const void* a, int64_t lda);
+int gbs_lu_compute_device(gbs_lu* lu, int64_t n, const void* d_a, int64_t lda);
+int64_t gbs_lu_first_zero_pivot(const gbs_lu* lu);   /* -1 when none */
+int gbs_lu_nb_transpositions(const gbs_lu* lu);
+int gbs_lu_solve(gbs_lu* lu, int64_t nrhs, const void* b, int64_t ldb, void* x, int64_t ldx, int transpose);
+int gbs_lu_solve_device(gbs_lu* lu, int64_t nrhs, const void* d_b, int64_t ldb, void* d_x, int64_t ldx,
+                        int transpose);
+int gbs_lu_rcond(gbs_lu* lu, double* rcond);
+int gbs_lu_l1_norm(const gbs_lu* lu, double* l1);
+int gbs_lu_determinant(gbs_lu* lu, double* det);
+int gbs_lu_matrix(gbs_lu* lu, void* out, int64_t ld);
+int gbs_lu_transpositions(gbs_lu* lu, int* out);
+int gbs_lu_permutation(gbs_lu* lu, int* out);
+void* gbs_lu_device_matrix(gbs_lu* lu, int64_t* ld);
+int gbs_lu_synchronize(gbs_lu* lu);
+int gbs_lu_set_stream(gbs_lu* lu, void* stream);
+
+/* ------------------------------------------------------------------ tracing
+ * The reference has no runtime tracing (bench/BenchTimer.h times whole calls
+ * from the host).  Here every kernel launch is counted, and when profiling is
+ * on each phase launch is bracketed by CUDA events on its stream and tagged
+ * with its algorithmic flops and bytes. */
+typedef enum gbs_phase {
+  GBS_PHASE_PANEL = 0, GBS_PHASE_LASWP = 1, GBS_PHASE_TRSM_LU = 2, GBS_PHASE_GEMM = 3,
+  GBS_PHASE_POTRF_DIAG = 4, GBS_PHASE_TRSM_LLT = 5, GBS_PHASE_SYRK = 6, GBS_PHASE_TRI_SOLVE = 7,
+  GBS_PHASE_NORM = 8, GBS_PHASE_MIXED = 9, GBS_PHASE_TC_GEMM = 10, GBS_PHASE_RESIDUAL = 11,
+  GBS_PHASE_BATCHED = 12, GBS_PHASE_ROUTER = 13, GBS_PHASE_COPY = 14, GBS_PHASE_COUNT = 15
+} gbs_phase;
+uint64_t gbs_kernel_launch_count(void);
+int gbs_profile_enable(int on);
+int gbs_profile_reset(void);
+/* Sums, over the phase's recorded launches, device time (ms), launch count,
+ * algorithmic flops and bytes.  Waits for the recorded events. */
+int gbs_profile_collect(int phase, double* ms_total, int64_t* launches, double* flops, double* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300SOLVE_H */
