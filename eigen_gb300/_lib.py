@@ -52,6 +52,7 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_spotrf": (c_int, [C.c_char_p, c_ip, c_vp, c_ip, c_ip]),
     "gbs_dpotrs": (c_int, [C.c_char_p, c_ip, c_ip, c_vp, c_ip, c_vp, c_ip, c_ip]),
     "gbs_spotrs": (c_int, [C.c_char_p, c_ip, c_ip, c_vp, c_ip, c_vp, c_ip, c_ip]),
+    "gbs_dgetrf_noalloc": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),
     # LLT object
     "gbs_llt_create": (c_int, [C.POINTER(c_vp), c_int, c_int]),
     "gbs_llt_destroy": (c_int, [c_vp]),

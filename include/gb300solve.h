@@ -95,6 +95,37 @@ int gbs_dpotrs(const char* uplo, const int* n, const int* nrhs, const double* a,
 int gbs_spotrs(const char* uplo, const int* n, const int* nrhs, const float* a, const int* lda,
                float* b, const int* ldb, int* info);
 
+/* Allocation-free LU.  This entry point has no counterpart in the reference.
+ *
+ * For callers that must not let a library allocate device memory: a real-time
+ * control loop that runs under a no-allocation rule (the GPU analogue of the
+ * reference's EIGEN_RUNTIME_NO_MALLOC mode), or an application that hands all
+ * device memory to its own pool and a fixed budget.  cudaMalloc can block,
+ * can synchronize the device and can fail when memory is short, so such a
+ * caller cannot use gbs_dgetrf, which allocates its workspace on demand.
+ *
+ * Same factorization and results as gbs_dgetrf (1-based ipiv, LAPACK info),
+ * but on DEVICE buffers, stream-ordered on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream), and without calling cudaMalloc, cudaFree or any
+ * allocating routine.  The scratch it needs (256 KiB: the panel's
+ * candidate-exchange buffers and a status word) is a fixed array inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits.
+ *   d_a     device, column-major m x n, lda >= max(1, m); overwritten by L\U
+ *   d_ipiv  device, min(m, n) ints; receives 1-based pivot rows
+ *   d_info  device, one int; receives 0, or k+1 for the first exactly-zero
+ *           pivot k, or -106 if an inter-CTA wait timed out
+ * Returns GBS_SUCCESS once the work is enqueued, GBS_INVALID_ARGUMENT for bad
+ * arguments or for m or n above 65536 (the limit of the fixed scratch).
+ * All calls share the one scratch array, which keeps the last call's contents
+ * (each call resets what must start at zero): calls whose work overlaps on the
+ * GPU (different streams, or several host threads) race on it and must be
+ * serialized by the caller.  The first call on a device does the set-up for
+ * that device (loading the kernels and looking up the array's device address),
+ * so make it before any section that must not allocate.  Profiling
+ * (gbs_profile_enable) must stay off, since it creates CUDA events. */
+int gbs_dgetrf_noalloc(int m, int n, double* d_a, int lda, int* d_ipiv, int* d_info, void* stream);
+
 /* ------------------------------------------------------------------ 3. objects
  * gbs_llt mirrors Eigen::LLT<Matrix<S,Dynamic,Dynamic>, UpLo> (LLT.h:56-230):
  *   compute   LLT::compute (LLT.h:424-452): copy, ||A||_1 (symmetric, stored
