@@ -42,6 +42,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Solves/s and TFLOP/s at ≤1e-13 backward err: mixed/batched vs plain FP64"
 BE_BAR = 1e-13
+# measured DRAM traffic / algorithmic bytes of the dominant kernel (ncu, see profiles/)
+TRAFFIC_OVER_ALGORITHMIC = {"fp64": 533.6 / 588.4}
 
 
 def args_parse():
@@ -55,6 +57,8 @@ def args_parse():
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--factor-once", action="store_true",
+                   help="factor one seeded n x n system on the chosen path and exit (small ncu captures)")
     return p.parse_args()
 
 
@@ -282,13 +286,11 @@ def run_ours(args):
     gm = prof.get("gemm", {"ms": 0, "launches": 1, "flops": 0, "bytes": 0})
     peak = fp64_gemm_peak()
     achieved = gm["flops"] / (gm["ms"] / 1e3) / 1e12 if gm["ms"] else 0.0
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.load(open(tfile)).get(path, {}).get("gemm_bytes_per_launch")
-        except Exception:
-            traffic = None
+    # DRAM bytes per launch: ncu capture of a smaller case of the same kernel
+    # (profiles/gemm_sub_kernel_fp64_lu6144.md: read + write = 0.907 x the
+    # launch's algorithmic bytes), scaled to this run's launches by their
+    # algorithmic bytes, since the traffic grows in proportion to them.
+    traffic = TRAFFIC_OVER_ALGORITHMIC[path] * gm["bytes"] / max(gm["launches"], 1)
     roofline = {"bound": "fp64", "kernel": "gemm_sub_kernel<double> (trailing update A22 -= A21 A12)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                 "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
@@ -352,8 +354,24 @@ def run_ours(args):
 import ctypes as C  # noqa: E402
 
 
+def factor_once(args):
+    import numpy as np
+    import torch
+
+    import eigen_gb300 as gb
+    n = args.n
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(3)).t()
+    torch.cuda.synchronize()
+    lu = gb.PartialPivLU(a)
+    torch.cuda.synchronize()
+    print(json.dumps({"factor_once": n, "path": args.path, "first_zero_pivot": lu.first_zero_pivot()}))
+    return 0 if lu.first_zero_pivot() < 0 else 1
+
+
 def main():
     args = args_parse()
+    if args.factor_once:
+        return factor_once(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -81,7 +81,7 @@ extern "C" int gbs_llt_create(gbs_llt** out, int dtype, int uplo)
   gbs_llt* o = new gbs_llt();
   o->dtype = dtype;
   o->uplo = uplo;
-  cudaError_t e = cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&o->stream, cudaStreamDefault);
   if (e != cudaSuccess) {
     gbs_set_last_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
     delete o;
@@ -296,7 +296,7 @@ extern "C" int gbs_lu_create(gbs_lu** out, int dtype)
   GBS_TRY(ensure_device());
   gbs_lu* o = new gbs_lu();
   o->dtype = dtype;
-  cudaError_t e = cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&o->stream, cudaStreamDefault);
   if (e != cudaSuccess) {
     gbs_set_last_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
     delete o;

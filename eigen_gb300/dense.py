@@ -72,8 +72,14 @@ class _Decomposition:
     def cols(self):
         return self._n
 
+    def _bind_torch_stream(self):
+        """Order device-buffer calls after the torch work that produced the data."""
+        import torch
+        self._fn("set_stream")(self._h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
     def _compute(self, a):
         if _is_torch_cuda(a):
+            self._bind_torch_stream()
             n = a.shape[0]
             assert a.shape[0] == a.shape[1], "square matrix expected"
             ld = _torch_colmajor_ld(a)
@@ -90,6 +96,7 @@ class _Decomposition:
     def _solve(self, b, *extra):
         if _is_torch_cuda(b):
             import torch
+            self._bind_torch_stream()
             vec = b.dim() == 1
             bb = b.reshape(-1, 1) if vec else b
             x = torch.empty((bb.shape[1], bb.shape[0]), dtype=b.dtype, device=b.device).t()

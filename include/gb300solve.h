@@ -24,6 +24,13 @@
  * usable sm_103a device is present every call returns GBS_NO_DEVICE.
  * Objects are not thread-safe; distinct objects may be used from distinct host
  * threads concurrently (each owns its stream and workspace).
+ *
+ * Stream ordering of the device-buffer variants (*_compute_device,
+ * *_solve_device): the work runs on the object's stream.  By default that is a
+ * blocking stream of its own, which waits for work queued earlier on the
+ * legacy default stream; data produced on any other stream must be made ready
+ * by the caller first, or the object bound to the producing stream with
+ * gbs_*_set_stream.
  */
 #ifndef GB300SOLVE_H
 #define GB300SOLVE_H

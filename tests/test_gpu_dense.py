@@ -291,6 +291,22 @@ def test_inplace_semantics_device_buffers(n):
     assert O.backward_error(s, xs, b) < 1e-14
 
 
+def test_device_input_freshly_produced_on_a_torch_stream():
+    """compute() on a tensor whose producing kernel may still be running must
+    see the finished data (the object is bound to the producer's stream)."""
+    torch = pytest.importorskip("torch")
+    n = 3000
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        for seed in range(3):
+            g = torch.Generator(device="cuda").manual_seed(seed)
+            a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g).t()
+            lu = PartialPivLU(a)               # queued right behind randn on `side`
+            assert lu.first_zero_pivot() == -1
+            host = np.asfortranarray(a.cpu().numpy())
+            assert np.array_equal(lu.transpositions(), O.lu(host)[1])
+
+
 def test_nonfinite_input_returns_without_hang():
     """NaN / Inf entries must neither trap nor hang: the factorization finishes
     and NaN propagates as in the reference (a NaN pivot is not an exact zero)."""
