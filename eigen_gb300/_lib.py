@@ -86,6 +86,8 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_lu_device_matrix": (c_vp, [c_vp, C.POINTER(c_i64)]),
     "gbs_lu_synchronize": (c_int, [c_vp]),
     "gbs_lu_set_stream": (c_int, [c_vp, c_vp]),
+    # tensor cores
+    "gbs_tc_gemm_sub": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_int, c_vp]),
     # tracing
     "gbs_kernel_launch_count": (C.c_uint64, []),
     "gbs_profile_enable": (c_int, [c_int]),

@@ -1,0 +1,487 @@
+// tcgen05 trailing-update GEMM (see tc_gemm.cuh).
+//
+// Kernel layout (one CTA per SM, persistent over output tiles of 128 x 256):
+//   warp 0      TMA producer: one 128-byte K-slice of A (128 rows) and of B
+//               (256 rows) per pipeline stage, 128B-swizzled, 4-stage ring
+//   warp 1      TMEM allocator + MMA issuer: 4 x tcgen05.mma (M=128, N=256,
+//               32 bytes of K each) per stage, accumulating in TMEM; commits
+//               free the smem stage / publish the finished accumulator
+//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns, C -= acc with
+//               column-coalesced FP32 loads/stores (lane = row)
+// Two TMEM accumulators (2 x 256 columns) let the epilogue of tile i overlap
+// the MMAs of tile i+1.  Every wait is bounded (2 s); on expiry the kernel
+// sets the status word's timeout flag, waits for its own copies in flight,
+// frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <mutex>
+
+#include "gbs_common.cuh"
+#include "gbs_profile.cuh"
+#include "tc_gemm.cuh"
+
+namespace gbs {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int ATOM = 128;                          // bytes of K per stage (one swizzle atom)
+constexpr int STAGES = 4;
+constexpr int NUM_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr int A_STAGE = BM * ATOM;                 // 16 KiB
+constexpr int B_STAGE = BN * ATOM;                 // 32 KiB
+constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init()
+{
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the completion of the phase with parity `parity`.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns)
+{
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  uint32_t spins = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if ((++spins & 63u) == 0) {
+      if (ld_volatile_i32(err)) return false;
+      if (globaltimer_ns() - t0 > limit_ns) {
+        atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, uint64_t* bar, int c0, int c1)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+          "r"(smem_u32(dst)),
+      "l"((uint64_t)tm), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols)
+{
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), LBO unused for swizzled K-major (encoded 1).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;      // descriptor version of tcgen05
+  d |= (uint64_t)2 << 61;      // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D = F32, A/B format, both K-major, N >> 3, M >> 4.
+__host__ __device__ constexpr uint32_t idesc_for(int fmt, int M, int N)
+{
+  return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+struct TcParams {
+  int M, N, kiters;         // kiters = K slices of ATOM bytes
+  int tiles_m, tiles_n;
+  float* C;
+  int64_t ldc;
+  int lower;
+  int tf32;                 // 1: kind::tf32, 0: kind::f16
+  uint32_t idesc;
+  int* err;
+};
+
+__device__ __forceinline__ bool skip_tile(const TcParams& p, int tm, int tn)
+{
+  return p.lower && (tn * BN >= tm * BM + BM);    // tile strictly above the diagonal
+}
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint32_t* tmem_slot = (uint32_t*)(tempty + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int num_tiles = p.tiles_m * p.tiles_n;
+  const uint64_t LIMIT = kSpinDeadlineNs;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < num_tiles && ok; t += gridDim.x) {
+        const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+        if (skip_tile(p, tm, tn)) continue;
+        for (int kk = 0; kk < p.kiters; ++kk, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, p.err, LIMIT)) { ok = false; break; }
+          unsigned char* sa = smem + s * STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+          const int kcoord = kk * (p.tf32 ? ATOM / 4 : ATOM / 2);
+          tma_load_2d(sa, &tmA, &full[s], kcoord, tm * BM);
+          tma_load_2d(sa + A_STAGE, &tmB, &full[s], kcoord, tn * BN);
+        }
+      }
+      if (!ok) {
+        // wait (bounded) for this CTA's copies still in flight before teardown
+        for (int i = it > STAGES ? it - STAGES : 0; i < it; ++i)
+          mbar_wait(&full[i % STAGES], (uint32_t)(i / STAGES) & 1u, p.err, 100000000ull);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int it = 0, tc = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < num_tiles && ok; t += gridDim.x) {
+        const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+        if (skip_tile(p, tm, tn)) continue;
+        const int b = tc & 1;
+        const uint32_t tph = (uint32_t)(tc >> 1) & 1u;
+        if (!mbar_wait(&tempty[b], tph ^ 1u, p.err, LIMIT)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem_base + (uint32_t)(b * BN);
+        for (int kk = 0; kk < p.kiters; ++kk, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+          if (!mbar_wait(&full[s], ph, p.err, LIMIT)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+          const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + A_STAGE);
+#pragma unroll
+          for (int k4 = 0; k4 < 4; ++k4) {      // 4 x 32 bytes of K per 128-byte slice
+            const uint64_t off = (uint64_t)((k4 * 32) >> 4);
+            const uint32_t acc = (kk > 0 || k4 > 0) ? 1u : 0u;
+            if (p.tf32) mma_tf32(d, da + off, db + off, p.idesc, acc);
+            else mma_f16(d, da + off, db + off, p.idesc, acc);
+          }
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&tfull[b]);
+        ++tc;
+      }
+      if (tc > 0) {
+        // the last accumulator must be complete before TMEM is released
+        const int b = (tc - 1) & 1;
+        mbar_wait(&tfull[b], (uint32_t)((tc - 1) >> 1) & 1u, p.err, 100000000ull);
+      }
+    }
+  } else {
+    const int q = warp & 3;                 // TMEM lane quadrant of this warp
+    int tc = 0;
+    for (int t = blockIdx.x; t < num_tiles; t += gridDim.x) {
+      const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+      if (skip_tile(p, tm, tn)) continue;
+      const int b = tc & 1;
+      const uint32_t tph = (uint32_t)(tc >> 1) & 1u;
+      // one lane waits, the warp follows: tcgen05.ld below is .sync.aligned
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(&tfull[b], tph, p.err, LIMIT) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      __syncwarp();
+      tc_fence_after();
+      const int row = tm * BM + 32 * q + lane;
+      const bool row_ok = row < p.M;
+      const uint32_t tbase = tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN);
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tbase + (uint32_t)c, v);
+        const int col0 = tn * BN + c;
+        if (row_ok) {
+          float* cp = p.C + (int64_t)col0 * p.ldc + row;
+          float old[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = col0 + j;
+            const bool ok = col < p.N && (!p.lower || row >= col);
+            old[j] = ok ? cp[(int64_t)j * p.ldc] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = col0 + j;
+            if (col < p.N && (!p.lower || row >= col)) cp[(int64_t)j * p.ldc] = old[j] - v[j];
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[b]);
+      ++tc;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, TMEM_COLS);
+  }
+}
+
+// ------------------------------------------------------------------ packing
+__device__ __forceinline__ float round_tf32(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// out[r * ldk + k] (K-major) from src(r, k) = src[r*rs + k*cs], r < R, k < K,
+// converted to the tier's type; x3 tiers write three K-blocks per row with
+// `pattern` selecting hi (0) or lo (1) for each block.  Zero padding up to Kp.
+template <typename TO>
+__global__ void pack_kmajor_kernel(const float* __restrict__ src, int64_t rs, int64_t cs, int R, int K, int Kp,
+                                   TO* __restrict__ out, int64_t ldk, int kind, int pattern)
+{
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+  const int nblk = (kind == TC_TF32X3) ? 3 : 1;
+  const int Kt = K * nblk;
+  // load a 32 (r) x 32 (source k) tile; threads run along the unit-stride dimension
+  const int kb0 = k0 % (K > 0 ? K : 1);
+  (void)kb0;
+  for (int yy = ty; yy < 32; yy += 8) {
+    int r, k;
+    if (rs == 1) { r = r0 + tx; k = k0 + yy; }
+    else { r = r0 + yy; k = k0 + tx; }
+    float v = 0.f;
+    const int ks = (nblk == 1) ? k : (K > 0 ? k % K : 0);
+    if (r < R && k < Kt) v = src[(int64_t)r * rs + (int64_t)ks * cs];
+    if (rs == 1) tile[tx][yy] = v;
+    else tile[yy][tx] = v;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int r = r0 + yy, k = k0 + tx;
+    if (r >= R || k >= Kp) continue;
+    float v = tile[yy][tx];
+    float o = 0.f;
+    if (k < Kt) {
+      if (kind == TC_TF32X3) {
+        const int blk = k / K;
+        const int lo = (pattern >> blk) & 1;
+        const float hi = round_tf32(v);
+        o = lo ? round_tf32(v - hi) : hi;
+      } else if (kind == TC_TF32) {
+        o = round_tf32(v);
+      } else {
+        o = v;
+      }
+    }
+    if constexpr (sizeof(TO) == 4) out[(int64_t)r * ldk + k] = o;
+    else if (kind == TC_BF16) ((__nv_bfloat16*)out)[(int64_t)r * ldk + k] = __float2bfloat16_rn(o);
+    else ((__half*)out)[(int64_t)r * ldk + k] = __float2half_rn(o);
+  }
+}
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+int make_tmap(CUtensorMap* tm, const void* base, int esize, int64_t rows, int64_t kp, int64_t ldk, int box_rows)
+{
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) {
+    gbs_set_last_message("cuTensorMapEncodeTiled unavailable");
+    return GBS_CUDA_ERROR;
+  }
+  CUtensorMapDataType dt = esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ldk * esize)};
+  cuuint32_t box[2] = {(cuuint32_t)(ATOM / esize), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(tm, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    gbs_set_last_message("cuTensorMapEncodeTiled failed");
+    return GBS_CUDA_ERROR;
+  }
+  return GBS_SUCCESS;
+}
+
+}  // namespace
+
+int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs,
+                const float* B, int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int lower, DeviceStatus* st,
+                TcWorkspace& ws)
+{
+  if (M <= 0 || N <= 0 || K <= 0) return GBS_SUCCESS;
+  if (kind < TC_BF16 || kind > TC_TF32X3) return GBS_INVALID_ARGUMENT;
+  const int esize = (kind == TC_TF32 || kind == TC_TF32X3) ? 4 : 2;
+  const int atom_elems = ATOM / esize;
+  const int Kt = K * (kind == TC_TF32X3 ? 3 : 1);
+  const int Kp = (Kt + atom_elems - 1) / atom_elems * atom_elems;
+  const int64_t ldk = Kp;                        // rows 128-byte multiples: TMA strides 16-byte aligned
+  GBS_TRY(ws.ak.reserve((size_t)M * ldk * esize));
+  GBS_TRY(ws.bk.reserve((size_t)N * ldk * esize));
+  {
+    PhaseScope ps(s, PH_COPY, 0.0, (double)(M + N) * (4.0 * K + esize * (double)Kp));
+    dim3 blk(32, 8);
+    dim3 ga((Kp + 31) / 32, (M + 31) / 32), gb((Kp + 31) / 32, (N + 31) / 32);
+    // x3 pattern bits (block -> lo?): A = [hi, hi, lo] (0b100), B = [hi, lo, hi] (0b010)
+    if (esize == 4) {
+      pack_kmajor_kernel<float><<<ga, blk, 0, s>>>(A, a_rs, a_cs, M, K, Kp, ws.ak.as<float>(), ldk, kind, 4);
+      pack_kmajor_kernel<float><<<gb, blk, 0, s>>>(B, b_cs, b_rs, N, K, Kp, ws.bk.as<float>(), ldk, kind, 2);
+    } else {
+      pack_kmajor_kernel<uint16_t><<<ga, blk, 0, s>>>(A, a_rs, a_cs, M, K, Kp, ws.ak.as<uint16_t>(), ldk, kind, 0);
+      pack_kmajor_kernel<uint16_t><<<gb, blk, 0, s>>>(B, b_cs, b_rs, N, K, Kp, ws.bk.as<uint16_t>(), ldk, kind, 0);
+    }
+    GBS_CUDA_TRY(cudaGetLastError());
+    count_launch();
+  }
+  CUtensorMap tmA, tmB;
+  GBS_TRY(make_tmap(&tmA, ws.ak.p, esize, M, Kp, ldk, BM));
+  GBS_TRY(make_tmap(&tmB, ws.bk.p, esize, N, Kp, ldk, BN));
+  static bool attr = false;
+  if (!attr) {
+    GBS_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr = true;
+  }
+  TcParams p;
+  p.M = M;
+  p.N = N;
+  p.kiters = Kp / atom_elems;
+  p.tiles_m = (M + BM - 1) / BM;
+  p.tiles_n = (N + BN - 1) / BN;
+  p.C = C;
+  p.ldc = ldc;
+  p.lower = lower;
+  p.tf32 = esize == 4;
+  p.idesc = idesc_for(kind == TC_BF16 ? 1 : kind == TC_FP16 ? 0 : 2, BM, BN);
+  p.err = &st->timeout;
+  const int tiles = p.tiles_m * p.tiles_n;
+  const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
+  const double flops = 2.0 * M * (double)N * K * (kind == TC_TF32X3 ? 3 : 1) * (lower ? 0.5 : 1.0);
+  const double bytes = 8.0 * M * (double)N * (lower ? 0.5 : 1.0) + (double)(M + N) * Kp * esize;
+  PhaseScope ps(s, PH_TC_GEMM, flops, bytes);
+  tc_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+}  // namespace gbs

@@ -188,6 +188,22 @@ void* gbs_lu_device_matrix(gbs_lu* lu, int64_t* ld);
 int gbs_lu_synchronize(gbs_lu* lu);
 int gbs_lu_set_stream(gbs_lu* lu, void* stream);
 
+/* ------------------------------------------------------------------ tensor cores
+ * The trailing update of the low-precision tiers as a standalone GEMM,
+ * C (m x n, FP32) -= A (m x k) * B (k x n), all column-major on the device,
+ * on the tcgen05 tensor cores with FP32 accumulation.  Replaces, for the
+ * mixed tiers, the products A22 -= A21*A12 (PartialPivLU.h:492) and
+ * A22 -= A21*A21^T (LLT.h:357, lower != 0: only the lower triangle of C is
+ * written, B must then be A^T and m == n).  kind: operand rounding. */
+typedef enum gbs_tc_kind {
+  GBS_TC_BF16 = 0,    /* bfloat16 operands */
+  GBS_TC_FP16 = 1,    /* float16 operands (caller scales against overflow) */
+  GBS_TC_TF32 = 2,    /* tf32 operands */
+  GBS_TC_TF32X3 = 3   /* FP32 operands split hi+lo: hi*hi + hi*lo + lo*hi (FP32 accuracy) */
+} gbs_tc_kind;
+int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, int64_t lda, const float* d_b, int64_t ldb,
+                    float* d_c, int64_t ldc, int lower, void* stream);
+
 /* ------------------------------------------------------------------ tracing
  * The reference has no runtime tracing (bench/BenchTimer.h times whole calls
  * from the host).  Here every kernel launch is counted, and when profiling is
