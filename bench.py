@@ -1,33 +1,39 @@
 #!/usr/bin/env python
 """Benchmark of the dense factor-and-solve hot path on GB300.
 
-Workload (one step): PartialPivLU<MatrixXd> of one n = 8192 FP64 matrix with
-entries iid N(0,1) and a solve with 16 right-hand sides iid N(0,1) -- the
-configuration the headline metric is quoted on.  A step counts as one solve
+Workload (one step): solve A X = B for one n = 8192 FP64 matrix with entries
+iid N(0,1) and 16 right-hand sides iid N(0,1) -- PartialPivLU<MatrixXd> n=8192
+with 16 RHS, the configuration the headline metric is quoted on.  A step counts
 only if its normwise backward error max_j ||b_j - A x_j||_inf /
-(||A||_inf ||x_j||_inf + ||b_j||_inf) is <= 1e-13 (checked on the GPU in FP64
-after the timed region).
+(||A||_inf ||x_j||_inf + ||b_j||_inf) is <= 1e-13, recomputed on the GPU in
+FP64 after the timed region.
 
-  value     solves/s with A and B resident in HBM (device-buffer C ABI)
-  e2e       solves/s through the host-buffer C ABI (gbs_lu_compute on host A,
-            gbs_lu_solve host B -> host X): the host->device copy of A and B and
-            the device->host copy of X are inside the timed region
-  roofline  the dominant kernel's achieved rate (algorithmic work per launch /
-            CUDA-event duration, measured live in the timed region) against
-            the peak of its unit
-  cpu_baseline  the CPU oracle (oracle/, a C restatement of the reference
-            algorithm) on the host cores, one full factor + 16-RHS solve
+  value        solves/s of the headline path (default: 3xTF32 tensor-core LU +
+               FP64 iterative refinement, FP64 fallback built in) with A and B
+               resident in HBM (device-buffer C ABI gbs_dgesv_mixed_device)
+  plain_fp64   the plain GPU FP64 path (PartialPivLU compute + solve, pivots
+               identical to the reference) timed in the same run; the metric
+               compares the two
+  e2e          the same metric through the host-buffer C ABI (gbs_dgesv_mixed):
+               the host->device copy of A and B and the device->host copy of X
+               are inside the timed region
+  roofline     the dominant kernel's achieved rate (algorithmic work / CUDA-event
+               duration of its launches, measured live in the timed region)
+               against the peak of its unit
+  cpu_baseline the CPU oracle (oracle/, the reference algorithm restated in C,
+               OpenMP GEMM) on the host cores: one full factor + 16-RHS solve
 
 --impl reference runs the reference's algorithm on the host cores for the
-same workload (the oracle port, since the reference is header-only C++ that
-is not present on the GPU host) and prints the same JSON line.
+same workload (the C restatement: the reference is header-only C++ that is not
+present on the GPU host) and prints the same JSON line.
 
-Replicas only across GPUs: under torchrun every rank factors its own system;
+Replicas only across GPUs: under torchrun every rank solves its own system;
 value is the sum over ranks, time the max over ranks.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -42,8 +48,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Solves/s and TFLOP/s at ≤1e-13 backward err: mixed/batched vs plain FP64"
 BE_BAR = 1e-13
-# measured DRAM traffic / algorithmic bytes of the dominant kernel (ncu, see profiles/)
-TRAFFIC_OVER_ALGORITHMIC = {"fp64": 533.6 / 588.4}
+# measured DRAM traffic / algorithmic bytes of a kernel (ncu captures, profiles/)
+TRAFFIC_OVER_ALGORITHMIC = {"gemm": 533.6 / 588.4}
 
 
 def args_parse():
@@ -52,9 +58,10 @@ def args_parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--path", default="auto", choices=["auto", "fp64"])
+    p.add_argument("--path", default="tf32x3", choices=["fp64", "tf32x3", "tf32", "bf16", "fp16"])
     p.add_argument("--n", type=int, default=8192)
     p.add_argument("--nrhs", type=int, default=16)
+    p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
@@ -144,7 +151,6 @@ def max_over_ranks(world, v: float) -> float:
 
 def backward_error_gpu(A, X, B) -> float:
     """max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf), FP64 on the GPU."""
-    import torch
     R = B - A @ X
     an = A.abs().sum(dim=1).max()
     num = R.abs().amax(dim=0)
@@ -152,12 +158,14 @@ def backward_error_gpu(A, X, B) -> float:
     return float((num / den).max().item())
 
 
-def fp64_gemm_peak(n=8192):
-    """Measured FP64 GEMM throughput of this GPU (cuBLAS DGEMM via torch), the
-    denominator for the DFMA-bound plain path."""
+def gemm_peak(dtype, n=8192, tf32=False):
+    """Measured cuBLAS GEMM throughput (TFLOP/s) of this GPU for a unit that
+    MEASURED_PEAKS.json does not list (FP64 DFMA, TF32 tensor)."""
     import torch
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = tf32
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     torch.matmul(a, b)
     torch.cuda.synchronize()
     best = 1e30
@@ -168,8 +176,22 @@ def fp64_gemm_peak(n=8192):
         e1.record()
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1) / 1e3)
+    torch.backends.cuda.matmul.allow_tf32 = old
     del a, b
     return 2.0 * n ** 3 / best / 1e12
+
+
+def collect_phases(L, steps):
+    from eigen_gb300 import _lib
+    prof = {}
+    for name, ph in _lib.PHASES.items():
+        ms = C.c_double(); cnt = C.c_int64(); fl = C.c_double(); by = C.c_double()
+        L.gbs_profile_collect(ph, C.byref(ms), C.byref(cnt), C.byref(fl), C.byref(by))
+        if cnt.value:
+            prof[name] = {"ms": ms.value / steps, "launches": cnt.value / steps,
+                          "flops": fl.value / steps, "bytes": by.value / steps}
+    L.gbs_profile_reset()
+    return prof
 
 
 # ----------------------------------------------------------------- CPU oracle
@@ -178,8 +200,7 @@ def cpu_oracle_solve(a_np, b_np):
     t0 = time.perf_counter()
     f, tr, _, _ = O.lu(a_np)
     x = O.lu_solve(f, tr, b_np)
-    dt = time.perf_counter() - t0
-    return x, dt
+    return x, time.perf_counter() - t0
 
 
 def cpu_baseline(args, A_host, B_host):
@@ -194,12 +215,9 @@ def cpu_baseline(args, A_host, B_host):
 
 # ----------------------------------------------------------------- reference arm
 def run_reference(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import numpy as np
-
     import oracle as O
     n, nrhs = args.n, args.nrhs
     a = O.gauss(1, n, n)
@@ -233,6 +251,7 @@ def run_ours(args):
 
     import eigen_gb300 as gb
     from eigen_gb300 import _lib
+    from eigen_gb300.mixed import RefineInfo, TIERS
     world, rank, local = dist_setup(args)
     L = gb.lib()
     n, nrhs = args.n, args.nrhs
@@ -240,77 +259,109 @@ def run_ours(args):
     g = torch.Generator(device="cuda").manual_seed(1000 + rank)
     A = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g).t()      # column-major view
     B = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=g).t()
+    X = torch.empty(nrhs, n, dtype=torch.float64, device="cuda").t()
+    tier = TIERS[args.path]
+    info = RefineInfo()
     lu = gb.PartialPivLU(dtype=np.float64)
-    L.gbs_lu_set_stream(lu._h, torch.cuda.current_stream().cuda_stream)
-    path = "fp64"
+    L.gbs_lu_set_stream(lu._h, C.c_void_p(stream.cuda_stream))
 
-    def step():
+    def step_mixed():
+        _lib.check(L.gbs_dgesv_mixed_device(n, nrhs, C.c_void_p(A.data_ptr()), n, C.c_void_p(B.data_ptr()), n,
+                                            C.c_void_p(X.data_ptr()), n, tier, BE_BAR, 30, C.byref(info),
+                                            C.c_void_p(stream.cuda_stream)), "gbs_dgesv_mixed_device")
+
+    def step_plain():
         lu.compute(A)
-        return lu.solve(B)
+        X.copy_(lu.solve(B))
 
-    for _ in range(args.warmup):
-        X = step()
-    torch.cuda.synchronize()
-    barrier(world)
+    step = step_plain if args.path == "fp64" else step_mixed
+
+    def timed(fn, steps, profile):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        if profile:
+            L.gbs_profile_reset()
+            L.gbs_profile_enable(1)
+        l0 = L.gbs_kernel_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches = L.gbs_kernel_launch_count() - l0
+        if profile:
+            L.gbs_profile_enable(0)
+        return e0.elapsed_time(e1) / 1e3, launches
+
     clocks = ClockSampler(local)
     clocks.start()
-    L.gbs_profile_reset()
-    L.gbs_profile_enable(1)
-    launches0 = L.gbs_kernel_launch_count()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        X = step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    launches = L.gbs_kernel_launch_count() - launches0
-    L.gbs_profile_enable(0)
+    dt, launches = timed(step, args.steps, True)
     clk = clocks.stop()
-    dt = e0.elapsed_time(e1) / 1e3
+    prof = collect_phases(L, args.steps)
     dt_max = max_over_ranks(world, dt)
-    barrier(world)
     be = backward_error_gpu(A, X, B)
     ok = be <= BE_BAR
     value = world * args.steps / dt_max if ok else 0.0
+    refine = {"tier_used": {v: k for k, v in TIERS.items()}[info.tier_used], "iterations": info.iterations,
+              "fell_back": bool(info.fell_back), "reported_backward_error": info.backward_error}
 
-    # dominant kernel: the FP64 trailing update
-    prof = {}
-    for name, ph in _lib.PHASES.items():
-        ms = C.c_double(); cnt = C.c_int64(); fl = C.c_double(); by = C.c_double()
-        L.gbs_profile_collect(ph, C.byref(ms), C.byref(cnt), C.byref(fl), C.byref(by))
-        if cnt.value:
-            prof[name] = {"ms": ms.value / args.steps, "launches": cnt.value // args.steps,
-                          "flops": fl.value / args.steps, "bytes": by.value / args.steps}
-    L.gbs_profile_reset()
-    gm = prof.get("gemm", {"ms": 0, "launches": 1, "flops": 0, "bytes": 0})
-    peak = fp64_gemm_peak()
-    achieved = gm["flops"] / (gm["ms"] / 1e3) / 1e12 if gm["ms"] else 0.0
-    # DRAM bytes per launch: ncu capture of a smaller case of the same kernel
-    # (profiles/gemm_sub_kernel_fp64_lu6144.md: read + write = 0.907 x the
-    # launch's algorithmic bytes), scaled to this run's launches by their
-    # algorithmic bytes, since the traffic grows in proportion to them.
-    traffic = TRAFFIC_OVER_ALGORITHMIC[path] * gm["bytes"] / max(gm["launches"], 1)
-    roofline = {"bound": "fp64", "kernel": "gemm_sub_kernel<double> (trailing update A22 -= A21 A12)",
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-                "traffic": traffic, "share_of_step": gm["ms"] / (1e3 * dt / args.steps),
-                "launches_per_step": gm["launches"]}
+    plain = None
+    if args.path != "fp64" and args.plain_steps > 0:
+        pdt, _ = timed(step_plain, args.plain_steps, False)
+        pbe = backward_error_gpu(A, X, B)
+        pdt = max_over_ranks(world, pdt)
+        plain = {"value": world * args.plain_steps / pdt, "unit": "solves/s",
+                 "ms_per_step": 1e3 * pdt / args.plain_steps, "backward_error": pbe,
+                 "tflops": lu_flops(n, nrhs) * world * args.plain_steps / pdt / 1e12}
+
+    # dominant kernel of the timed path
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else ("none", None)
+    roofline = None
+    if dom is not None:
+        achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12 if dom["ms"] else 0.0
+        if dom_name in ("tc_gemm",):
+            peak = gemm_peak(torch.float32, tf32=True)
+            roofline = {"bound": "tensor", "kernel": "tc_gemm_kernel (tcgen05 kind::tf32, trailing update)",
+                        "peak_source": "cuBLAS TF32 GEMM 8192^3 measured in this run"}
+        elif dom_name in ("gemm", "residual", "syrk"):
+            peak = gemm_peak(torch.float64)
+            roofline = {"bound": "fp64", "kernel": {"gemm": "gemm_sub_kernel<double> (trailing update)",
+                                                    "residual": "residual_partial_kernel (FP64 r = b - A x)",
+                                                    "syrk": "gemm_sub_kernel<double> lower (SYRK)"}[dom_name],
+                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in "
+                                       "MEASURED_PEAKS.json)"}
+        else:
+            peak = gemm_peak(torch.float64)
+            roofline = {"bound": "latency", "kernel": dom_name,
+                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
+        ratio = TRAFFIC_OVER_ALGORITHMIC.get(dom_name)
+        roofline.update({"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": (ratio * dom["bytes"] / max(dom["launches"], 1)) if ratio else None,
+                         "phase": dom_name, "share_of_step": dom["ms"] / (1e3 * dt / args.steps),
+                         "launches_per_step": dom["launches"]})
 
     # end to end through the host-buffer C ABI
     e2e = None
     if not args.no_e2e:
         Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
-        Ah.copy_(A.t())                    # row-major of A^T == column-major of A
+        Ah.copy_(A.t())                    # row-major A^T == column-major A
         Bh = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
         Bh.copy_(B.t())
         Xh = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
-        h = lu._h
         pa, pb, px = C.c_void_p(Ah.data_ptr()), C.c_void_p(Bh.data_ptr()), C.c_void_p(Xh.data_ptr())
+        einfo = RefineInfo()
+        h = lu._h
 
         def e2e_step():
-            _lib.check(L.gbs_lu_compute(h, n, pa, n), "compute")
-            _lib.check(L.gbs_lu_solve(h, nrhs, pb, n, px, n, 0), "solve")
+            if args.path == "fp64":
+                _lib.check(L.gbs_lu_compute(h, n, pa, n), "compute")
+                _lib.check(L.gbs_lu_solve(h, nrhs, pb, n, px, n, 0), "solve")
+            else:
+                _lib.check(L.gbs_dgesv_mixed(n, nrhs, pa, n, pb, n, px, n, tier, BE_BAR, 30, C.byref(einfo)),
+                           "gbs_dgesv_mixed")
 
         for _ in range(max(1, args.warmup)):
             e2e_step()
@@ -321,17 +372,16 @@ def run_ours(args):
             e2e_step()
         torch.cuda.synchronize()
         t_e2e = max_over_ranks(world, time.perf_counter() - t0)
-        Xd = Xh.to("cuda").t()
-        be2 = backward_error_gpu(A, Xd, B)
+        be2 = backward_error_gpu(A, Xh.to("cuda").t(), B)
         e2e = {"value": (world * args.steps / t_e2e) if be2 <= BE_BAR else 0.0, "unit": "solves/s",
                "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs,
-               "backward_error": be2, "api": "gbs_lu_compute(host A) + gbs_lu_solve(host B -> host X), pinned"}
+               "backward_error": be2,
+               "api": ("gbs_dgesv_mixed" if args.path != "fp64" else "gbs_lu_compute + gbs_lu_solve") +
+                      " on pinned host buffers"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        a_np = np.asfortranarray(A.cpu().numpy())
-        b_np = np.asfortranarray(B.cpu().numpy())
-        cpu = cpu_baseline(args, a_np, b_np)
+        cpu = cpu_baseline(args, np.asfortranarray(A.cpu().numpy()), np.asfortranarray(B.cpu().numpy()))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -339,9 +389,10 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic: A iid N(0,1), B iid N(0,1) (torch.randn on the GPU, seeded)",
                 "config": {"workload": f"PartialPivLU<MatrixXd> n={n} FP64 + solve {nrhs} RHS", "n": n,
-                           "nrhs": nrhs, "path": path, "parallelism": f"replicas x{world}",
+                           "nrhs": nrhs, "path": args.path, "parallelism": f"replicas x{world}",
                            "l2": "inputs (512 MB) larger than L2 (129 MB); no flush needed"},
-                "tflops": lu_flops(n, nrhs) * value / 1e12, "backward_error": be,
+                "tflops": lu_flops(n, nrhs) * value / 1e12, "backward_error": be, "refinement": refine,
+                "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": int(launches), "phases_ms_per_step": {k: round(v["ms"], 3) for k, v in prof.items()}}
         print(json.dumps(line), flush=True)
@@ -351,9 +402,6 @@ def run_ours(args):
     return 0
 
 
-import ctypes as C  # noqa: E402
-
-
 def factor_once(args):
     import numpy as np
     import torch
@@ -361,11 +409,20 @@ def factor_once(args):
     import eigen_gb300 as gb
     n = args.n
     a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(3)).t()
+    b = torch.randn(1, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(4)).t()
     torch.cuda.synchronize()
-    lu = gb.PartialPivLU(a)
-    torch.cuda.synchronize()
-    print(json.dumps({"factor_once": n, "path": args.path, "first_zero_pivot": lu.first_zero_pivot()}))
-    return 0 if lu.first_zero_pivot() < 0 else 1
+    if args.path == "fp64":
+        lu = gb.PartialPivLU(a)
+        torch.cuda.synchronize()
+        ok = lu.first_zero_pivot() < 0
+        out = {"first_zero_pivot": lu.first_zero_pivot()}
+    else:
+        x, info = gb.solve_mixed(a, b, tier=args.path)
+        torch.cuda.synchronize()
+        ok = info["backward_error"] <= BE_BAR
+        out = info
+    print(json.dumps({"factor_once": n, "path": args.path, **out}))
+    return 0 if ok else 1
 
 
 def main():

@@ -88,6 +88,10 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_lu_set_stream": (c_int, [c_vp, c_vp]),
     # tensor cores
     "gbs_tc_gemm_sub": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_int, c_vp]),
+    # mixed precision
+    "gbs_dgesv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int,
+                                       c_vp, c_vp]),
+    "gbs_dgesv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int, c_vp]),
     # tracing
     "gbs_kernel_launch_count": (C.c_uint64, []),
     "gbs_profile_enable": (c_int, [c_int]),

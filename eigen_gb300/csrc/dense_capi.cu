@@ -66,6 +66,7 @@ struct gbs_llt {
   int64_t n = 0;
   DevBuf A, st, tmp, vec, rhs, norm;
   HostBuf hvec;
+  SolveWork sw;
   double l1 = 0;
   bool initialized = false;
   int info = GBS_NOT_INITIALIZED;
@@ -197,8 +198,8 @@ static int llt_solve_inplace(gbs_llt* o, int nrhs, void* dX, int64_t ldx)
   const int n = (int)o->n;
   const int up = o->uplo == GBS_UPPER;
   if (o->dtype == GBS_F64)
-    return llt_solve_device<double>(o->stream, n, nrhs, o->A.as<double>(), n, up, (double*)dX, ldx);
-  return llt_solve_device<float>(o->stream, n, nrhs, o->A.as<float>(), n, up, (float*)dX, ldx);
+    return llt_solve_device<double>(o->stream, n, nrhs, o->A.as<double>(), n, up, (double*)dX, ldx, o->sw);
+  return llt_solve_device<float>(o->stream, n, nrhs, o->A.as<float>(), n, up, (float*)dX, ldx, o->sw);
 }
 
 extern "C" int gbs_llt_solve(gbs_llt* o, int64_t nrhs, const void* b, int64_t ldb, void* x, int64_t ldx)
@@ -211,6 +212,7 @@ extern "C" int gbs_llt_solve(gbs_llt* o, int64_t nrhs, const void* b, int64_t ld
   GBS_TRY(o->rhs.reserve(es * (size_t)n * nrhs));
   GBS_TRY(upload_matrix(o->stream, b, ldb, o->rhs.p, n, n, nrhs, es));
   GBS_TRY(llt_solve_inplace(o, (int)nrhs, o->rhs.p, n));
+  GBS_TRY(solve_status(o->stream, o->sw));
   GBS_TRY(download_matrix(o->stream, o->rhs.p, n, x, ldx, n, nrhs, es));
   return sync(o->stream);
 }
@@ -240,9 +242,9 @@ extern "C" int gbs_llt_rcond(gbs_llt* o, double* rcond)
   }
   double est = 0;
   if (o->dtype == GBS_F64)
-    GBS_TRY(inv_l1_estimate_device<double>(o->stream, kind, n, o->A.as<double>(), n, nullptr, o->vec, o->hvec, &est));
+    GBS_TRY(inv_l1_estimate_device<double>(o->stream, kind, n, o->A.as<double>(), n, nullptr, o->vec, o->hvec, o->sw, &est));
   else
-    GBS_TRY(inv_l1_estimate_device<float>(o->stream, kind, n, o->A.as<float>(), n, nullptr, o->vec, o->hvec, &est));
+    GBS_TRY(inv_l1_estimate_device<float>(o->stream, kind, n, o->A.as<float>(), n, nullptr, o->vec, o->hvec, o->sw, &est));
   *rcond = rcond_from_estimate(n, o->l1, est, single);
   return GBS_SUCCESS;
 }
@@ -272,7 +274,7 @@ extern "C" void* gbs_llt_device_matrix(gbs_llt* o, int64_t* ld)
 extern "C" int gbs_llt_synchronize(gbs_llt* o)
 {
   if (!o) return GBS_INVALID_ARGUMENT;
-  return sync(o->stream);
+  return solve_status(o->stream, o->sw);
 }
 
 // =================================================================== LU object
@@ -283,6 +285,7 @@ struct gbs_lu {
   int64_t n = 0;
   DevBuf A, tr, st, scratch, vec, rhs, norm;
   HostBuf hvec;
+  SolveWork sw;
   double l1 = 0;
   bool initialized = false;
   int64_t first_zero = -1;
@@ -401,8 +404,8 @@ static int lu_solve_inplace(gbs_lu* o, int nrhs, void* dX, int64_t ldx, int tran
   const int n = (int)o->n;
   if (o->dtype == GBS_F64)
     return lu_solve_device<double>(o->stream, n, nrhs, o->A.as<double>(), n, o->tr.as<int>(), (double*)dX, ldx,
-                                   transpose);
-  return lu_solve_device<float>(o->stream, n, nrhs, o->A.as<float>(), n, o->tr.as<int>(), (float*)dX, ldx, transpose);
+                                   transpose, o->sw);
+  return lu_solve_device<float>(o->stream, n, nrhs, o->A.as<float>(), n, o->tr.as<int>(), (float*)dX, ldx, transpose, o->sw);
 }
 
 extern "C" int gbs_lu_solve(gbs_lu* o, int64_t nrhs, const void* b, int64_t ldb, void* x, int64_t ldx, int transpose)
@@ -415,6 +418,7 @@ extern "C" int gbs_lu_solve(gbs_lu* o, int64_t nrhs, const void* b, int64_t ldb,
   GBS_TRY(o->rhs.reserve(es * (size_t)n * nrhs));
   GBS_TRY(upload_matrix(o->stream, b, ldb, o->rhs.p, n, n, nrhs, es));
   GBS_TRY(lu_solve_inplace(o, (int)nrhs, o->rhs.p, n, transpose));
+  GBS_TRY(solve_status(o->stream, o->sw));
   GBS_TRY(download_matrix(o->stream, o->rhs.p, n, x, ldx, n, nrhs, es));
   return sync(o->stream);
 }
@@ -445,10 +449,10 @@ extern "C" int gbs_lu_rcond(gbs_lu* o, double* rcond)
   double est = 0;
   if (o->dtype == GBS_F64)
     GBS_TRY(inv_l1_estimate_device<double>(o->stream, 0, n, o->A.as<double>(), n, o->tr.as<int>(), o->vec, o->hvec,
-                                           &est));
+                                           o->sw, &est));
   else
     GBS_TRY(inv_l1_estimate_device<float>(o->stream, 0, n, o->A.as<float>(), n, o->tr.as<int>(), o->vec, o->hvec,
-                                          &est));
+                                          o->sw, &est));
   *rcond = rcond_from_estimate(n, o->l1, est, single);
   return GBS_SUCCESS;
 }
@@ -525,7 +529,7 @@ extern "C" void* gbs_lu_device_matrix(gbs_lu* o, int64_t* ld)
 extern "C" int gbs_lu_synchronize(gbs_lu* o)
 {
   if (!o) return GBS_INVALID_ARGUMENT;
-  return sync(o->stream);
+  return solve_status(o->stream, o->sw);
 }
 
 // =================================================================== plug-in level
@@ -668,7 +672,8 @@ static int getrs_impl(const char* trans, const int* n, const int* nrhs, const T*
   GBS_TRY(upload_matrix(s, a, *lda, w.a.p, N, N, N, sizeof(T)));
   GBS_TRY(upload_matrix(s, b, *ldb, w.b.p, N, N, R, sizeof(T)));
   GBS_CUDA_TRY(cudaMemcpyAsync(w.piv.p, tr.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
-  GBS_TRY(lu_solve_device<T>(s, N, R, w.a.as<T>(), N, w.piv.as<int>(), w.b.as<T>(), N, op));
+  GBS_TRY(lu_solve_device<T>(s, N, R, w.a.as<T>(), N, w.piv.as<int>(), w.b.as<T>(), N, op, w.sw));
+  GBS_TRY(solve_status(s, w.sw));
   GBS_TRY(download_matrix(s, w.b.p, N, b, *ldb, N, R, sizeof(T)));
   return sync(s);
 }
@@ -739,7 +744,8 @@ static int potrs_impl(const char* uplo, const int* n, const int* nrhs, const T* 
   GBS_TRY(w.b.reserve(sizeof(T) * (size_t)N * R));
   GBS_TRY(upload_matrix(s, a, *lda, w.a.p, N, N, N, sizeof(T)));
   GBS_TRY(upload_matrix(s, b, *ldb, w.b.p, N, N, R, sizeof(T)));
-  GBS_TRY(llt_solve_device<T>(s, N, R, w.a.as<T>(), N, up, w.b.as<T>(), N));
+  GBS_TRY(llt_solve_device<T>(s, N, R, w.a.as<T>(), N, up, w.b.as<T>(), N, w.sw));
+  GBS_TRY(solve_status(s, w.sw));
   GBS_TRY(download_matrix(s, w.b.p, N, b, *ldb, N, R, sizeof(T)));
   return sync(s);
 }

@@ -195,6 +195,127 @@ static int gemm_sub(cudaStream_t s, int phase, int M, int N, int K, const T* A, 
   return GBS_SUCCESS;
 }
 
+template <typename T>
+int gemm_sub_device(cudaStream_t s, int phase, int M, int N, int K, const T* A, int64_t a_rs, int64_t a_cs, const T* B,
+                    int64_t b_rs, int64_t b_cs, T* C, int64_t ldc)
+{
+  return gemm_sub<T>(s, phase, M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, 0, nullptr);
+}
+
+// B(kb x ncols) <- L^{-1} B for a unit-lower L of kb <= 128 rows with many
+// columns: 32-row blocks solved one column per thread, SIMT updates between.
+template <typename T>
+int trsm_lunit_wide(cudaStream_t s, int kb, int ncols, const T* L, int64_t ldl, T* B, int64_t ldb)
+{
+  for (int b0 = 0; b0 < kb; b0 += kPanelNB) {
+    const int bb = std::min(kPanelNB, kb - b0);
+    {
+      PhaseScope ps(s, PH_TRSM_LU, (double)bb * bb * ncols, sizeof(T) * 2.0 * bb * ncols);
+      trsm_lunit_kernel<T, kPanelNB><<<ceil_div(ncols, 128), 128, 0, s>>>(L + b0 * ldl + b0, ldl, bb, B + b0, ldb,
+                                                                         ncols);
+      GBS_CUDA_TRY(cudaGetLastError());
+    }
+    const int rest = kb - b0 - bb;
+    if (rest > 0)
+      GBS_TRY(gemm_sub<T>(s, PH_TRSM_LU, rest, ncols, bb, L + b0 * ldl + b0 + bb, 1, ldl, B + b0, 1, ldb,
+                          B + b0 + bb, ldb, 0, nullptr));
+  }
+  return GBS_SUCCESS;
+}
+
+// Row interchanges tr[i0..i1) (applied in order) on the columns [c0,c1) and
+// [c2,c3), as ONE gather: each CTA replays the swaps on a row map in shared
+// memory, then every column reads its affected rows once (independent loads)
+// and writes them to their final places.
+// map[0] = cnt; map[1..1+cnt) = touched rows; map[257..257+cnt) = source row
+// now at each.  One warp replays the interchanges in order, finding rows with
+// a ballot over the list.
+__global__ void laswp_map_kernel(const int* __restrict__ tr, int i0, int i1, int* __restrict__ map)
+{
+  __shared__ int rows[256], src[256];
+  const int lane = threadIdx.x;
+  int cnt = 0;
+  for (int i = i0; i < i1; ++i) {
+    const int r1 = i, r2 = tr[i];
+    if (r1 == r2) continue;          // no interchange for this row
+    int u1 = -1, u2 = -1;
+    for (int b = 0; b < cnt; b += 32) {
+      const int u = b + lane;
+      const bool in = u < cnt;
+      const unsigned m1 = __ballot_sync(0xffffffffu, in && rows[u] == r1);
+      const unsigned m2 = __ballot_sync(0xffffffffu, in && rows[u] == r2);
+      if (m1 && u1 < 0) u1 = b + __ffs(m1) - 1;
+      if (m2 && u2 < 0) u2 = b + __ffs(m2) - 1;
+    }
+    if (u1 < 0) { u1 = cnt; if (lane == 0) { rows[cnt] = r1; src[cnt] = r1; } ++cnt; }
+    if (u2 < 0) { u2 = cnt; if (lane == 0) { rows[cnt] = r2; src[cnt] = r2; } ++cnt; }
+    __syncwarp();
+    if (lane == 0) { const int t = src[u1]; src[u1] = src[u2]; src[u2] = t; }
+    __syncwarp();
+  }
+  for (int u = lane; u < cnt; u += 32) {
+    map[1 + u] = rows[u];
+    map[257 + u] = src[u];
+  }
+  if (lane == 0) map[0] = cnt;
+}
+
+// Applies the row map to the columns [c0,c1) and [c2,c3): one warp per column
+// reads every affected row once (independent loads), then writes them back
+// to their final rows.
+template <typename T>
+__global__ void laswp_gather_kernel(T* __restrict__ a, int64_t lda, const int* __restrict__ map, int c0, int c1,
+                                    int c2, int c3)
+{
+  __shared__ int rows[256], src[256];
+  const int cnt = map[0];
+  for (int u = threadIdx.x; u < cnt; u += blockDim.x) {
+    rows[u] = map[1 + u];
+    src[u] = map[257 + u];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int n1 = c1 - c0, ntot = n1 + (c3 - c2);
+  for (int t = wid; t < ntot; t += nw) {
+    const int col = t < n1 ? c0 + t : c2 + (t - n1);
+    T* ac = a + (int64_t)col * lda;
+    T v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int u = q * 32 + lane;
+      if (u < cnt) v[q] = ac[src[u]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int u = q * 32 + lane;
+      if (u < cnt) ac[rows[u]] = v[q];
+    }
+    __syncwarp();
+  }
+}
+
+template <typename T>
+int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0, int i1, int c0, int c1, int c2,
+                        int c3, DevBuf& map)
+{
+  const int nc = (c1 - c0) + (c3 - c2);
+  if (nc <= 0 || i1 <= i0) return GBS_SUCCESS;
+  if (i1 - i0 > 128) {
+    gbs_set_last_message("laswp_gather: at most 128 interchanges per call");
+    return GBS_INVALID_ARGUMENT;
+  }
+  GBS_TRY(map.reserve(sizeof(int) * 520));
+  PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * (i1 - i0));
+  laswp_map_kernel<<<1, 32, 0, s>>>(tr, i0, i1, map.as<int>());
+  count_launch();
+  const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
+  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map.as<int>(), c0, c1, c2, c3);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
 // ------------------------------------------------------------------ LU
 template <typename T>
 int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, int i0, int i1, int reverse)
@@ -315,61 +436,68 @@ int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceSta
 // ------------------------------------------------------------------ solves
 template <typename T>
 int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
-                     T* B, int64_t ldb)
+                     T* B, int64_t ldb, SolveWork& w)
 {
   if (n <= 0 || nrhs <= 0) return GBS_SUCCESS;
-  constexpr int NBK = 32;
+  // FP64: 32-row blocks keep the per-block DFMA work on the critical path
+  // short; FP32: 64-row blocks.
+  constexpr int NB = sizeof(T) == 8 ? 32 : 64;
+  constexpr int RC = 16;
   const int64_t rs = trans ? ld : 1, cs = trans ? 1 : ld;   // op(Tri)(i,j) = tri[i*rs + j*cs]
   const int forward = (lower != 0) != (trans != 0);
-  const int nblk = ceil_div(n, NBK);
-  for (int bb = 0; bb < nblk; ++bb) {
-    const int b = forward ? bb : nblk - 1 - bb;
-    const int j0 = b * NBK, jb = std::min(NBK, n - j0);
-    const T* diag = tri + j0 * rs + j0 * cs;
-    {
-    PhaseScope ps(s, PH_TRI_SOLVE, (double)jb * jb * nrhs, sizeof(T) * ((double)jb * jb + 2.0 * jb * nrhs));
-    trsv_block_kernel<T, NBK><<<ceil_div(nrhs, 128), 128, 0, s>>>(diag, rs, cs, jb, forward, unit, B + j0, ldb, nrhs);
+  const int nblk = ceil_div(n, NB);
+  GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
+  const int grid = std::min(nblk, 2 * device_sm_count());
+  for (int c0 = 0; c0 < nrhs; c0 += RC) {
+    const int nc = std::min(RC, nrhs - c0);
+    GBS_CUDA_TRY(cudaMemsetAsync(w.flags.p, 0, sizeof(int) * (size_t)(nblk + 2), s));
+    PhaseScope ps(s, PH_TRI_SOLVE, (double)n * n * nc, sizeof(T) * (0.5 * (double)n * n + 2.0 * n * nc));
+    trsm_persistent_kernel<T, NB, RC><<<grid, RC * 32, 0, s>>>(n, nc, tri, rs, cs, forward, unit,
+                                                                B + (int64_t)c0 * ldb, ldb, w.flags.as<int>());
     GBS_CUDA_TRY(cudaGetLastError());
-    }
-    if (forward) {
-      const int r0 = j0 + jb, mr = n - r0;
-      if (mr > 0)
-        GBS_TRY(gemm_sub<T>(s, PH_TRI_SOLVE, mr, nrhs, jb, tri + r0 * rs + j0 * cs, rs, cs, B + j0, 1, ldb, B + r0, ldb, 0,
-                            nullptr));
-    } else {
-      const int mr = j0;
-      if (mr > 0)
-        GBS_TRY(gemm_sub<T>(s, PH_TRI_SOLVE, mr, nrhs, jb, tri + j0 * cs, rs, cs, B + j0, 1, ldb, B, ldb, 0, nullptr));
-    }
+  }
+  return GBS_SUCCESS;
+}
+
+int solve_status(cudaStream_t s, SolveWork& w)
+{
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  if (!w.flags.p) return GBS_SUCCESS;
+  int h[2] = {0, 0};
+  GBS_CUDA_TRY(cudaMemcpy(h, w.flags.p, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[1]) {
+    gbs_set_last_message("a triangular-solve wait timed out");
+    return GBS_TIMEOUT;
   }
   return GBS_SUCCESS;
 }
 
 template <typename T>
 int lu_solve_device(cudaStream_t s, int n, int nrhs, const T* dLU, int64_t ld, const int* dTr, T* B, int64_t ldb,
-                    int transpose)
+                    int transpose, SolveWork& w)
 {
   if (!transpose) {
     GBS_TRY(laswp_device<T>(s, B, ldb, nrhs, dTr, 0, n, 0));
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 0, 1, B, ldb));
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 0, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 0, 1, B, ldb, w));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 0, 0, B, ldb, w));
   } else {
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 1, 0, B, ldb));
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 1, 1, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 0, 1, 0, B, ldb, w));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dLU, ld, 1, 1, 1, B, ldb, w));
     GBS_TRY(laswp_device<T>(s, B, ldb, nrhs, dTr, 0, n, 1));
   }
   return GBS_SUCCESS;
 }
 
 template <typename T>
-int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb)
+int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb,
+                     SolveWork& w)
 {
   if (!upper) {
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 0, 0, B, ldb));
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 1, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 0, 0, B, ldb, w));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 1, 1, 0, B, ldb, w));
   } else {
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 1, 0, B, ldb));
-    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 0, 0, B, ldb));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 1, 0, B, ldb, w));
+    GBS_TRY(tri_solve_device<T>(s, n, nrhs, dL, ld, 0, 0, 0, B, ldb, w));
   }
   return GBS_SUCCESS;
 }
@@ -407,15 +535,17 @@ int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int s
 // ConditionEstimator.h:56-142.  The control flow (sign vectors, argmax, bound
 // comparisons) runs on the host on n-vectors read back after each solve.
 template <typename T>
-static int dec_solve(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr, T* v, int adjoint)
+static int dec_solve(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr, T* v, int adjoint,
+                     SolveWork& w)
 {
-  if (kind == 0) return lu_solve_device<T>(s, n, 1, dF, ld, dTr, v, n, adjoint);
-  return llt_solve_device<T>(s, n, 1, dF, ld, kind == 2, v, n);
+  if (kind == 0) GBS_TRY(lu_solve_device<T>(s, n, 1, dF, ld, dTr, v, n, adjoint, w));
+  else GBS_TRY(llt_solve_device<T>(s, n, 1, dF, ld, kind == 2, v, n, w));
+  return solve_status(s, w);
 }
 
 template <typename T>
 int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr, DevBuf& vec,
-                           HostBuf& hvec, double* est)
+                           HostBuf& hvec, SolveWork& w, double* est)
 {
   if (n == 0) { *est = 0; return GBS_SUCCESS; }
   GBS_TRY(vec.reserve(sizeof(T) * (size_t)n));
@@ -440,7 +570,7 @@ int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t
   };
   for (int i = 0; i < n; ++i) hv[i] = T(1) / T(n);
   GBS_TRY(upload());
-  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0, w));
   GBS_TRY(download());
   T lower_bound = l1();
   if (n == 1) { *est = (double)lower_bound; return GBS_SUCCESS; }
@@ -451,7 +581,7 @@ int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t
     if (k > 0 && memcmp(sgn, old_sgn, sizeof(T) * n) == 0) break;
     for (int i = 0; i < n; ++i) hv[i] = sgn[i];
     GBS_TRY(upload());
-    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 1));
+    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 1, w));
     GBS_TRY(download());
     vmax = 0;
     T best = hv[0] < 0 ? -hv[0] : hv[0];
@@ -463,7 +593,7 @@ int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t
     for (int i = 0; i < n; ++i) hv[i] = T(0);
     hv[vmax] = T(1);
     GBS_TRY(upload());
-    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+    GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0, w));
     GBS_TRY(download());
     lower_bound = l1();
     if (lower_bound <= old_lower_bound) break;
@@ -477,7 +607,7 @@ int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t
     alt = -alt;
   }
   GBS_TRY(upload());
-  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0));
+  GBS_TRY(dec_solve<T>(s, kind, n, dF, ld, dTr, dv, 0, w));
   GBS_TRY(download());
   T alternate = (T(2) * l1()) / (T(3) * T(n));
   *est = (double)(lower_bound > alternate ? lower_bound : alternate);
@@ -503,14 +633,20 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
 #define GBS_INSTANTIATE(T)                                                                                      \
   template int getrf_device<T>(cudaStream_t, int, int, T*, int64_t, int*, DeviceStatus*, DevBuf&);               \
   template int potrf_device<T>(cudaStream_t, int, T*, int64_t, int, DeviceStatus*, DevBuf&);                     \
-  template int tri_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, int, int, T*, int64_t);       \
+  template int tri_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, int, int, T*, int64_t,       \
+                                   SolveWork&);                                                              \
   template int laswp_device<T>(cudaStream_t, T*, int64_t, int, const int*, int, int, int);                       \
-  template int lu_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, T*, int64_t, int);      \
-  template int llt_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, T*, int64_t);                 \
+  template int lu_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, T*, int64_t, int,       \
+                                  SolveWork&);                                                               \
+  template int llt_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, T*, int64_t, SolveWork&);     \
   template int l1_norm_device<T>(cudaStream_t, const T*, int64_t, int, int, int, int, double*, double*);         \
   template int inv_l1_estimate_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, DevBuf&, HostBuf&, \
-                                         double*);                                                               \
-  template int copy_matrix_device<T>(cudaStream_t, const T*, int64_t, T*, int64_t, int, int);
+                                         SolveWork&, double*);                                                               \
+  template int copy_matrix_device<T>(cudaStream_t, const T*, int64_t, T*, int64_t, int, int);                   \
+  template int gemm_sub_device<T>(cudaStream_t, int, int, int, int, const T*, int64_t, int64_t, const T*, int64_t, \
+                                  int64_t, T*, int64_t);                                                       \
+  template int trsm_lunit_wide<T>(cudaStream_t, int, int, const T*, int64_t, T*, int64_t);                     \
+  template int laswp_gather_device<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int, int, int, DevBuf&);
 
 GBS_INSTANTIATE(double)
 GBS_INSTANTIATE(float)

@@ -40,6 +40,12 @@ struct HostBuf {
   HostBuf& operator=(const HostBuf&) = delete;
 };
 
+// Device workspace of the persistent triangular solve: ticket counter,
+// timeout flag and one ready flag per block row; one per stream of use.
+struct SolveWork {
+  DevBuf flags;
+};
+
 // Per-call workspace for the stateless (plug-in / LAPACK) entry points: a
 // stream plus buffers, taken from a process-wide pool so concurrent host
 // threads never share one.
@@ -47,6 +53,7 @@ struct Workspace {
   cudaStream_t stream = nullptr;
   DevBuf a, piv, status, scratch, b, vec;
   HostBuf hvec;
+  SolveWork sw;
 };
 struct WorkspaceLease {
   Workspace* ws = nullptr;
@@ -78,7 +85,10 @@ int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceSta
 // holds the factor; trans: solve with its transpose; unit: unit diagonal.
 template <typename T>
 int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
-                     T* B, int64_t ldb);
+                     T* B, int64_t ldb, SolveWork& w);
+
+// Waits for the stream and reports GBS_TIMEOUT if a solve's wait expired.
+int solve_status(cudaStream_t s, SolveWork& w);
 
 template <typename T>
 int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, int i0, int i1, int reverse);
@@ -86,10 +96,11 @@ int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, i
 // A x = b with PA = LU (transpose: A^T x = b), in place on B.
 template <typename T>
 int lu_solve_device(cudaStream_t s, int n, int nrhs, const T* dLU, int64_t ld, const int* dTr, T* B, int64_t ldb,
-                    int transpose);
+                    int transpose, SolveWork& w);
 
 template <typename T>
-int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb);
+int llt_solve_device(cudaStream_t s, int n, int nrhs, const T* dL, int64_t ld, int upper, T* B, int64_t ldb,
+                     SolveWork& w);
 
 template <typename T>
 int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int sym, int upper, double* d_out,
@@ -99,11 +110,26 @@ int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int s
 // 1 = LLT lower, 2 = LLT upper.  `vec` holds 2n scalars of device scratch.
 template <typename T>
 int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr,
-                           DevBuf& vec, HostBuf& hvec, double* est);
+                           DevBuf& vec, HostBuf& hvec, SolveWork& w, double* est);
 
 double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool single);
 
 template <typename T>
 int copy_matrix_device(cudaStream_t s, const T* a, int64_t lda, T* b, int64_t ldb, int m, int n);
+
+// C -= op(A) op(B) on the SIMT cores (strided operands, see gemm_sub_kernel).
+template <typename T>
+int gemm_sub_device(cudaStream_t s, int phase, int M, int N, int K, const T* A, int64_t a_rs, int64_t a_cs, const T* B,
+                    int64_t b_rs, int64_t b_cs, T* C, int64_t ldc);
+
+// B(kb x ncols) <- L^{-1} B, L unit lower with kb <= 128 rows and many columns.
+template <typename T>
+int trsm_lunit_wide(cudaStream_t s, int kb, int ncols, const T* L, int64_t ldl, T* B, int64_t ldb);
+
+// Row interchanges tr[i0..i1) (in order, at most 128) on columns [c0,c1) and
+// [c2,c3) as one gather per column; `map` is a small device scratch.
+template <typename T>
+int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0, int i1, int c0, int c1, int c2,
+                        int c3, DevBuf& map);
 
 }  // namespace gbs

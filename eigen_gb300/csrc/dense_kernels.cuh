@@ -10,8 +10,8 @@
 //                        SYRK (PartialPivLU.h:492, LLT.h:357)
 //   potrf_diag_kernel    left-looking Cholesky of one diagonal block (LLT.h:305-328)
 //   trsm_rlt_kernel      A21 <- A21 L11^{-T} (LLT.h:356)
-//   trsv_block_kernel    one diagonal block of a triangular solve (LLT.h:499-505,
-//                        PartialPivLU.h:224-271)
+//   trsm_persistent_kernel  whole triangular solve in one launch (LLT.h:499-505,
+//                        PartialPivLU.h:224-271, TriangularSolverMatrix.h)
 //   norm kernels         ||A||_1 (PartialPivLU.h:522, LLT.h:434-445)
 #pragma once
 
@@ -409,49 +409,135 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
   }
 }
 
-// --------------------------------------------------------------------- TRSV block
-// Solves one nb x nb diagonal block (nb <= NB) of op(Tri) X = B for all nrhs
-// columns, one thread per column.  op(Tri)(i,j) = tri[i*rs + j*cs].  forward:
-// lower-triangular op (rows top to bottom); else upper (bottom to top).
-template <typename T, int NB>
-__global__ void __launch_bounds__(128)
-trsv_block_kernel(const T* __restrict__ tri, int64_t rs, int64_t cs, int nb, int forward, int unit,
-                  T* __restrict__ B, int64_t ldb, int nrhs)
+// --------------------------------------------------------------------- persistent TRSM
+// op(Tri) X = B for up to RC right-hand sides in ONE launch.  Block rows of NB
+// are handed out in solve order by a ticket counter; block i waits (bounded)
+// on the ready flag of every earlier block j, subtracts op(Tri)(i,j) x_j, then
+// solves its diagonal block with one warp per right-hand side (rows spread
+// over lanes, shuffles carry x_r), writes x_i and raises its flag.  A CTA
+// only takes a ticket while running and only waits on lower tickets, so the
+// lowest unfinished block always progresses.  work: [0] ticket counter,
+// [1] timeout flag, [2..] one ready flag per block; zeroed before launch.
+template <typename T, int NB, int RC>
+__global__ void __launch_bounds__(RC * 32)
+trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, int64_t cs, int forward, int unit,
+                       T* B, int64_t ldb, int* work)
 {
+  constexpr int PER = NB / 32;
+  const int nblk = (n + NB - 1) / NB;
+  int* counter = work;
+  int* err = work + 1;
+  int* flags = work + 2;
   __shared__ T sT[NB][NB + 1];
-  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
-    int i = e % NB, j = e / NB;
-    sT[i][j] = (i < nb && j < nb) ? tri[(int64_t)i * rs + (int64_t)j * cs] : T(0);
-  }
-  __syncthreads();
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= nrhs) return;
-  T* b = B + (int64_t)col * ldb;
-  T x[NB];
-#pragma unroll
-  for (int i = 0; i < NB; ++i) x[i] = i < nb ? b[i] : T(0);
-  if (forward) {
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-      if (j < nb) {
-        if (!unit) x[j] = x[j] / sT[j][j];
-#pragma unroll
-        for (int i = j + 1; i < NB; ++i) x[i] = fma(-sT[i][j], x[j], x[i]);
-      }
+  __shared__ T sY[NB][RC];
+  __shared__ T sX[NB][RC];
+  __shared__ int s_t, s_ok;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const bool unit_rows_fast = (rs == 1);
+  for (;;) {
+    if (tid == 0) s_t = atomicAdd(counter, 1);
+    __syncthreads();
+    const int t = s_t;
+    if (t >= nblk) break;
+    const int bi = forward ? t : nblk - 1 - t;
+    const int i0 = bi * NB, ni = min(NB, n - i0);
+    for (int e = tid; e < NB * RC; e += nthr) {
+      const int r = e % NB, c = e / NB;
+      sY[r][c] = (r < ni && c < nrhs) ? B[(int64_t)c * ldb + i0 + r] : T(0);
     }
-  } else {
-#pragma unroll
-    for (int jj = NB - 1; jj >= 0; --jj) {
-      if (jj < nb) {
-        if (!unit) x[jj] = x[jj] / sT[jj][jj];
-#pragma unroll
-        for (int i = 0; i < jj; ++i) x[i] = fma(-sT[i][jj], x[jj], x[i]);
+    for (int tt = 0; tt < t; ++tt) {
+      const int bj = forward ? tt : nblk - 1 - tt;
+      const int j0 = bj * NB, nj = min(NB, n - j0);
+      if (tid == 0) {
+        int ok = 1;
+        if (ld_acquire_u32((const unsigned int*)&flags[bj]) == 0u) {
+          const uint64_t t0 = globaltimer_ns();
+          unsigned int spins = 0;
+          while (ld_acquire_u32((const unsigned int*)&flags[bj]) == 0u) {
+            if ((++spins & 63u) == 0 &&
+                (ld_volatile_i32(err) || globaltimer_ns() - t0 > kSpinDeadlineNs)) {
+              atomicExch(err, 1);
+              ok = 0;
+              break;
+            }
+            __nanosleep(32);
+          }
+        }
+        s_ok = ok;
       }
+      __syncthreads();
+      if (!s_ok) return;
+      for (int e = tid; e < NB * RC; e += nthr) {
+        const int r = e % NB, c = e / NB;
+        sX[r][c] = (r < nj && c < nrhs) ? __ldcg(&B[(int64_t)c * ldb + j0 + r]) : T(0);
+      }
+      for (int e = tid; e < NB * NB; e += nthr) {
+        int r, c;
+        if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
+        sT[r][c] = (r < ni && c < nj) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(j0 + c) * cs] : T(0);
+      }
+      __syncthreads();
+      for (int e = tid; e < NB * RC; e += nthr) {
+        const int r = e % NB, c = e / NB;
+        T acc = T(0);
+#pragma unroll 8
+        for (int k = 0; k < NB; ++k) acc = fma(sT[r][k], sX[k][c], acc);
+        sY[r][c] -= acc;
+      }
+      __syncthreads();
     }
-  }
+    for (int e = tid; e < NB * NB; e += nthr) {
+      int r, c;
+      if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
+      sT[r][c] = (r < ni && c < ni) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(i0 + c) * cs] : T(0);
+    }
+    __syncthreads();
+    if (warp < nrhs) {
+      T yl[PER];
 #pragma unroll
-  for (int i = 0; i < NB; ++i)
-    if (i < nb) b[i] = x[i];
+      for (int p = 0; p < PER; ++p) yl[p] = sY[lane + 32 * p][warp];
+      if (forward) {
+#pragma unroll
+        for (int r = 0; r < NB; ++r) {
+          if (r < ni) {
+            T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
+            if (!unit) xr = xr / sT[r][r];
+#pragma unroll
+            for (int p = 0; p < PER; ++p) {
+              const int row = lane + 32 * p;
+              if (row > r && row < ni) yl[p] = fma(-sT[row][r], xr, yl[p]);
+            }
+            if (lane == r % 32) yl[r / 32] = xr;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = NB - 1; r >= 0; --r) {
+          if (r < ni) {
+            T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
+            if (!unit) xr = xr / sT[r][r];
+#pragma unroll
+            for (int p = 0; p < PER; ++p) {
+              const int row = lane + 32 * p;
+              if (row < r) yl[p] = fma(-sT[row][r], xr, yl[p]);
+            }
+            if (lane == r % 32) yl[r / 32] = xr;
+          }
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < PER; ++p) sY[lane + 32 * p][warp] = yl[p];
+    }
+    __syncthreads();
+    for (int e = tid; e < NB * RC; e += nthr) {
+      const int r = e % NB, c = e / NB;
+      if (r < ni && c < nrhs) B[(int64_t)c * ldb + i0 + r] = sY[r][c];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(&flags[bi], 1);
+  }
 }
 
 // --------------------------------------------------------------------- norms

@@ -204,6 +204,38 @@ typedef enum gbs_tc_kind {
 int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, int64_t lda, const float* d_b, int64_t ldb,
                     float* d_c, int64_t ldc, int lower, void* stream);
 
+/* ------------------------------------------------------------------ mixed precision
+ * A x = B for a general FP64 matrix, factored in a low precision on the tensor
+ * cores and refined in FP64 until the normwise backward error
+ * max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
+ * The reference has no such path; it extends PartialPivLU::solve
+ * (PartialPivLU.h:224-244) the way LAPACK's dsgesv extends dgesv.  When the
+ * refinement stops improving (or needs more than max_iter steps) the plain
+ * FP64 factorization (identical pivots to the reference) decides the result,
+ * so the bound is met whenever the FP64 path meets it. */
+typedef enum gbs_tier {
+  GBS_TIER_FP64 = 0,     /* plain FP64 (no refinement) */
+  GBS_TIER_TF32X3 = 1,   /* FP32-accurate factors: 3xTF32 tensor-core updates */
+  GBS_TIER_TF32 = 2,     /* TF32 tensor-core updates */
+  GBS_TIER_BF16 = 3,     /* BF16 tensor-core updates */
+  GBS_TIER_FP16 = 4      /* FP16 tensor-core updates */
+} gbs_tier;
+
+typedef struct gbs_refine_info {
+  int tier_used;          /* gbs_tier that produced X (GBS_TIER_FP64 after a fallback) */
+  int iterations;         /* refinement steps taken by the low-precision tier */
+  int fell_back;          /* 1 when the FP64 factorization produced X */
+  int singular;           /* 1 when the FP64 factorization met an exactly-zero pivot */
+  double backward_error;  /* normwise backward error of X, computed in FP64 */
+} gbs_refine_info;
+
+/* Device buffers, stream-ordered on `stream` (NULL: the library's own); returns after X is final. */
+int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
+                           int ldx, int tier, double tol, int max_iter, gbs_refine_info* info, void* stream);
+/* Host buffers (copied in and out inside the call). */
+int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx, int tier,
+                    double tol, int max_iter, gbs_refine_info* info);
+
 /* ------------------------------------------------------------------ tracing
  * The reference has no runtime tracing (bench/BenchTimer.h times whole calls
  * from the host).  Here every kernel launch is counted, and when profiling is

@@ -1,0 +1,81 @@
+"""Mixed-precision factor + FP64 refinement (gbs_dgesv_mixed*) through the C ABI.
+
+Bar: normwise backward error <= 1e-13 for every tier (recomputed here with the
+CPU oracle in extended precision, not taken from the library's report), with
+the FP64 fallback taking over whenever refinement stalls.  The 3xTF32 tier
+(FP32-accurate factors) must converge without fallback on well-conditioned
+systems; the solution is also compared with the plain FP64 path.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from eigen_gb300 import PartialPivLU, solve_mixed
+
+pytestmark = pytest.mark.gpu
+BAR = 1e-13
+
+
+@pytest.mark.parametrize("tier", ["tf32x3", "tf32", "bf16", "fp16", "fp64"])
+@pytest.mark.parametrize("n", [100, 517, 2048])
+def test_mixed_reaches_the_backward_error_bar(tier, n):
+    a = O.gauss(100 + n, n, n)
+    b = O.gauss(200 + n, n, 3)
+    x, info = solve_mixed(a, b, tier=tier)
+    be = O.backward_error(a, x, b)
+    assert be <= BAR, (be, info)
+    assert info["backward_error"] <= BAR
+    if tier == "tf32x3":
+        assert not info["fell_back"] and info["iterations"] <= 10, info
+    x64 = PartialPivLU(a).solve(b)
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-9
+
+
+def test_mixed_many_rhs_groups():
+    n = 700
+    a = O.gauss(7, n, n)
+    b = O.gauss(8, n, 37)            # three refinement groups of <= 16 columns
+    x, info = solve_mixed(a, b, tier="tf32x3")
+    assert O.backward_error(a, x, b) <= BAR
+
+
+def test_ill_conditioned_falls_back_and_still_meets_the_bar():
+    n = 300
+    u, _ = np.linalg.qr(O.gauss(1, n, n))
+    v, _ = np.linalg.qr(O.gauss(2, n, n))
+    s = np.logspace(0, -13, n)
+    a = np.asfortranarray((u * s) @ v.T)
+    b = O.gauss(3, n, 2)
+    x, info = solve_mixed(a, b, tier="bf16")
+    assert info["fell_back"] and info["tier_used"] == "fp64"
+    assert O.backward_error(a, x, b) <= BAR
+
+
+def test_unreachable_tolerance_falls_back():
+    n = 256
+    a = O.gauss(11, n, n)
+    b = O.gauss(12, n, 1)
+    x, info = solve_mixed(a, b, tier="tf32x3", tol=0.0, max_iter=4)
+    assert info["fell_back"]
+    assert O.backward_error(a, x, b) <= BAR
+
+
+def test_singular_reports_it():
+    n = 64
+    a = O.gauss(13, n, n)
+    a[:, 10] = 0.0
+    b = O.gauss(14, n, 1)
+    _, info = solve_mixed(a, b, tier="tf32x3")
+    assert info["fell_back"] and info["singular"]
+
+
+def test_mixed_device_buffers():
+    torch = pytest.importorskip("torch")
+    n = 1500
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g).t()
+    B = torch.randn(4, n, dtype=torch.float64, device="cuda", generator=g).t()
+    X, info = solve_mixed(A, B, tier="tf32x3")
+    a = np.asfortranarray(A.cpu().numpy())
+    assert O.backward_error(a, X.cpu().numpy(), B.cpu().numpy()) <= BAR
+    assert not info["fell_back"]
