@@ -92,6 +92,15 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_dgesv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int,
                                        c_vp, c_vp]),
     "gbs_dgesv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int, c_vp]),
+    # batched
+    "gbs_batched_create": (c_int, [C.POINTER(c_vp), c_int, c_i64, c_vp, c_vp, c_int]),
+    "gbs_batched_destroy": (c_int, [c_vp]),
+    "gbs_batched_matrix_elements": (c_i64, [c_vp]),
+    "gbs_batched_rhs_elements": (c_i64, [c_vp]),
+    "gbs_batched_offsets": (c_int, [c_vp, c_vp, c_vp]),
+    "gbs_batched_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "gbs_batched_autotune": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
+    "gbs_batched_config": (c_int, [c_vp, c_ip, c_ip]),
     # tracing
     "gbs_kernel_launch_count": (C.c_uint64, []),
     "gbs_profile_enable": (c_int, [c_int]),

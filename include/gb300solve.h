@@ -236,6 +236,40 @@ int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const do
 int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx, int tier,
                     double tol, int max_iter, gbs_refine_info* info);
 
+/* ------------------------------------------------------------------ batched
+ * Many small, uneven systems, one right-hand side each: LLT + solve for SPD
+ * matrices (kind 0) and PartialPivLU + solve for general ones (kind 1), n in
+ * [1, 64].  The reference has no batch API; each item gives the results of
+ * LLT<MatrixX?>(A).solve(b) (LLT.h:305-328, 477-505) or
+ * PartialPivLU<MatrixX?>(A).solve(b) (PartialPivLU.h:365-409, 224-244) with
+ * the reference's pivot sequence and failing column.
+ *
+ * A plan fixes sizes and kinds; the caller's buffers hold the matrices back to
+ * back (column-major, ld = n, item i at the element offset
+ * sum_{j<i} n_j^2) and the right-hand sides back to back (offset
+ * sum_{j<i} n_j); gbs_batched_offsets returns both offset lists.  Solving
+ * overwrites the matrices with their factors (LLT: lower triangle; LU: L\U),
+ * the right-hand sides with the solutions, writes info[i] (-1 = success,
+ * else the failing column (LLT) or first exactly-zero pivot (LU)) and, for LU
+ * items, the 0-based transpositions at the item's right-hand-side offset of
+ * d_piv.  With use_graph != 0 the launch is a CUDA graph replayed per call
+ * (re-captured when the buffer pointers change). */
+typedef struct gbs_batched gbs_batched;
+int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, const int* sizes, const int* kinds,
+                       int use_graph);
+int gbs_batched_destroy(gbs_batched* plan);
+int64_t gbs_batched_matrix_elements(const gbs_batched* plan);
+int64_t gbs_batched_rhs_elements(const gbs_batched* plan);
+int gbs_batched_offsets(const gbs_batched* plan, int64_t* a_offsets, int64_t* b_offsets);
+int gbs_batched_solve(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, void* stream);
+/* Times each candidate CTA shape (warps per CTA) per size bucket on the given
+ * buffers (they are factored repeatedly: pass scratch copies), keeps the
+ * fastest and, if persist != 0, appends it to the autotune cache
+ * ($GBS_AUTOTUNE_CACHE, default ~/.gb300solve_autotune.jsonl), keyed by
+ * (GPU, bucket, dtype). */
+int gbs_batched_autotune(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, int persist);
+int gbs_batched_config(const gbs_batched* plan, int* warps_small, int* warps_large);
+
 /* ------------------------------------------------------------------ tracing
  * The reference has no runtime tracing (bench/BenchTimer.h times whole calls
  * from the host).  Here every kernel launch is counted, and when profiling is

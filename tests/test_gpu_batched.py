@@ -1,0 +1,100 @@
+"""Batched small-system solves (gbs_batched_*) against the CPU oracle, item by
+item: identical pivots and failing columns (bit-exact integer results),
+factors within 1e-12 (FP64) / 2e-5 (FP32) relative, solutions with backward
+error at the precision floor.  Sizes and mixes follow the batched workload
+(SPD n in [3, 24] with G G^T + 0.1 I, general n in [4, 64] iid N(0,1)),
+including non-SPD and singular items."""
+import numpy as np
+import pytest
+
+import oracle as O
+from eigen_gb300.batched import BatchedSolver
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(count_spd, count_gen, seed, bad=True):
+    rng = np.random.default_rng(seed)
+    sizes, kinds, mats, rhs = [], [], [], []
+    for i in range(count_spd):
+        n = int(rng.integers(3, 25))
+        g = O.gauss(seed * 100000 + i, n, n)
+        a = np.asfortranarray(g @ g.T + 0.1 * np.eye(n))
+        if bad and i % 97 == 5:
+            a[n // 2, n // 2] = -1.0          # not SPD: fails at column n // 2 (or earlier)
+        sizes.append(n); kinds.append(0); mats.append(a); rhs.append(O.gauss(seed * 7 + i, n, 1)[:, 0])
+    for i in range(count_gen):
+        n = int(rng.integers(4, 65))
+        a = O.gauss(seed * 200000 + i, n, n)
+        if bad and i % 53 == 7:
+            a[:, n // 3] = 0.0                # exactly singular
+        sizes.append(n); kinds.append(1); mats.append(a); rhs.append(O.gauss(seed * 11 + i, n, 1)[:, 0])
+    return sizes, kinds, mats, rhs
+
+
+def run_batch(dtype, sizes, kinds, mats, rhs, use_graph=True, repeat=1):
+    torch = pytest.importorskip("torch")
+    bs = BatchedSolver(sizes, kinds, dtype=dtype, use_graph=use_graph)
+    a, b = bs.pack(mats, rhs)
+    for _ in range(repeat):
+        d_a = torch.from_numpy(a.copy()).cuda()
+        d_b = torch.from_numpy(b.copy()).cuda()
+        d_info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+        d_piv = torch.zeros(max(bs.b_elems, 1), dtype=torch.int32, device="cuda")
+        bs.solve(d_a, d_b, d_info, d_piv)
+        torch.cuda.synchronize()
+    return bs, d_a.cpu().numpy(), d_b.cpu().numpy(), d_info.cpu().numpy(), d_piv.cpu().numpy()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_batched_matches_oracle_item_by_item(dtype):
+    sizes, kinds, mats, rhs = make_batch(600, 300, seed=3)
+    bs, fa, fb, info, piv = run_batch(dtype, sizes, kinds, mats, rhs, repeat=2)
+    ftol = 1e-12 if dtype == np.float64 else 2e-5
+    for i, (n, k) in enumerate(zip(sizes, kinds)):
+        a = np.asfortranarray(mats[i].astype(dtype))
+        f, x = bs.unpack(fa, fb, i)
+        if k == 0:
+            fo, io = O.llt(a)
+            assert info[i] == io, (i, info[i], io)
+            assert np.array_equal(np.triu(f, 1), np.triu(a, 1))
+            assert np.linalg.norm(np.tril(f) - np.tril(fo)) <= ftol * np.linalg.norm(np.tril(fo)) * 10
+            if io < 0:
+                xo = O.llt_solve(fo, rhs[i].astype(dtype))
+                assert np.linalg.norm(x - xo) <= 1e3 * ftol * np.linalg.norm(xo)
+        else:
+            fo, tro, _, fz = O.lu(a)
+            assert info[i] == fz, (i, info[i], fz)
+            tr = piv[bs.b_off[i]:bs.b_off[i] + n]
+            assert np.array_equal(tr, tro), (i, tr, tro)
+            assert np.linalg.norm(f - fo) <= ftol * np.linalg.norm(fo) * 10
+            if fz < 0 and dtype == np.float64:
+                assert O.backward_error(mats[i], x.reshape(-1, 1), rhs[i].reshape(-1, 1)) < 1e-14
+
+
+def test_batched_without_graph_equals_with_graph():
+    sizes, kinds, mats, rhs = make_batch(100, 50, seed=9, bad=False)
+    _, a1, b1, i1, p1 = run_batch(np.float64, sizes, kinds, mats, rhs, use_graph=True)
+    _, a2, b2, i2, p2 = run_batch(np.float64, sizes, kinds, mats, rhs, use_graph=False)
+    assert np.array_equal(i1, i2) and np.array_equal(p1, p2)
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+
+
+def test_batched_autotune_keeps_results():
+    torch = pytest.importorskip("torch")
+    sizes, kinds, mats, rhs = make_batch(400, 200, seed=12, bad=False)
+    bs = BatchedSolver(sizes, kinds, dtype=np.float64)
+    a, b = bs.pack(mats, rhs)
+    mk = lambda: (torch.from_numpy(a.copy()).cuda(), torch.from_numpy(b.copy()).cuda(),
+                  torch.zeros(len(sizes), dtype=torch.int32, device="cuda"),
+                  torch.zeros(bs.b_elems, dtype=torch.int32, device="cuda"))
+    cfg = bs.autotune(*mk(), persist=False)
+    assert cfg["warps_per_cta_n<=32"] in (1, 2, 4, 8) and cfg["warps_per_cta_n<=64"] in (1, 2, 4, 8)
+    d_a, d_b, d_info, d_piv = mk()
+    bs.solve(d_a, d_b, d_info, d_piv)
+    torch.cuda.synchronize()
+    assert (d_info.cpu().numpy() == -1).all()
+    x = d_b.cpu().numpy()
+    for i in range(0, len(sizes), 37):
+        _, xi = bs.unpack(d_a.cpu().numpy(), x, i)
+        assert O.backward_error(mats[i], xi.reshape(-1, 1), rhs[i].reshape(-1, 1)) < 1e-14
