@@ -251,7 +251,7 @@ def run_ours(args):
 
     import eigen_gb300 as gb
     from eigen_gb300 import _lib
-    from eigen_gb300.mixed import RefineInfo, TIERS
+    from eigen_gb300.mixed import RefineInfo, TIERS, options
     world, rank, local = dist_setup(args)
     L = gb.lib()
     n, nrhs = args.n, args.nrhs
@@ -261,13 +261,14 @@ def run_ours(args):
     B = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=g).t()
     X = torch.empty(nrhs, n, dtype=torch.float64, device="cuda").t()
     tier = TIERS[args.path]
+    opt = options(args.path, tol=BE_BAR)
     info = RefineInfo()
     lu = gb.PartialPivLU(dtype=np.float64)
     L.gbs_lu_set_stream(lu._h, C.c_void_p(stream.cuda_stream))
 
     def step_mixed():
         _lib.check(L.gbs_dgesv_mixed_device(n, nrhs, C.c_void_p(A.data_ptr()), n, C.c_void_p(B.data_ptr()), n,
-                                            C.c_void_p(X.data_ptr()), n, tier, BE_BAR, 30, C.byref(info),
+                                            C.c_void_p(X.data_ptr()), n, C.byref(opt), C.byref(info),
                                             C.c_void_p(stream.cuda_stream)), "gbs_dgesv_mixed_device")
 
     def step_plain():
@@ -305,8 +306,7 @@ def run_ours(args):
     be = backward_error_gpu(A, X, B)
     ok = be <= BE_BAR
     value = world * args.steps / dt_max if ok else 0.0
-    refine = {"tier_used": {v: k for k, v in TIERS.items()}[info.tier_used], "iterations": info.iterations,
-              "fell_back": bool(info.fell_back), "reported_backward_error": info.backward_error}
+    refine = info.as_dict()
 
     plain = None
     if args.path != "fp64" and args.plain_steps > 0:
@@ -360,7 +360,7 @@ def run_ours(args):
                 _lib.check(L.gbs_lu_compute(h, n, pa, n), "compute")
                 _lib.check(L.gbs_lu_solve(h, nrhs, pb, n, px, n, 0), "solve")
             else:
-                _lib.check(L.gbs_dgesv_mixed(n, nrhs, pa, n, pb, n, px, n, tier, BE_BAR, 30, C.byref(einfo)),
+                _lib.check(L.gbs_dgesv_mixed(n, nrhs, pa, n, pb, n, px, n, C.byref(opt), C.byref(einfo)),
                            "gbs_dgesv_mixed")
 
         for _ in range(max(1, args.warmup)):

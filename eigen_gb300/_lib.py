@@ -89,9 +89,11 @@ PROTOTYPES: dict[str, tuple] = {
     # tensor cores
     "gbs_tc_gemm_sub": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_int, c_vp]),
     # mixed precision
-    "gbs_dgesv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int,
-                                       c_vp, c_vp]),
-    "gbs_dgesv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, C.c_double, c_int, c_vp]),
+    "gbs_refine_options_default": (None, [c_vp]),
+    "gbs_dgesv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),
+    "gbs_dgesv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp]),
+    "gbs_dposv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),
+    "gbs_dposv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp]),
     # batched
     "gbs_batched_create": (c_int, [C.POINTER(c_vp), c_int, c_i64, c_vp, c_vp, c_int]),
     "gbs_batched_destroy": (c_int, [c_vp]),

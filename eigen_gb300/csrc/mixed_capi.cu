@@ -1,5 +1,5 @@
-// C-ABI of the low-precision tiers: the standalone tensor-core update and
-// (below) the mixed-precision factor + iterative-refinement solvers.
+// C-ABI of the low-precision tiers: the standalone tensor-core update and the
+// mixed-precision factor + FP64 refinement solvers (gbs_d{ge,po}sv_mixed*).
 #include <algorithm>
 
 #include "dense_driver.cuh"
@@ -7,76 +7,6 @@
 #include "tc_gemm.cuh"
 
 using namespace gbs;
-
-static void fill_info(gbs_refine_info* info, const MixedResult& r)
-{
-  if (!info) return;
-  info->tier_used = r.tier;
-  info->iterations = r.iterations;
-  info->fell_back = r.fell_back;
-  info->singular = r.singular;
-  info->backward_error = r.backward_error;
-}
-
-static int check_mixed_args(int n, int nrhs, int lda, int ldb, int ldx, int tier, int max_iter)
-{
-  if (n < 0 || nrhs < 0 || lda < std::max(1, n) || ldb < std::max(1, n) || ldx < std::max(1, n) ||
-      tier < GBS_TIER_FP64 || tier > GBS_TIER_FP16 || max_iter < 0) {
-    gbs_set_last_message("gbs_dgesv_mixed: invalid argument");
-    return GBS_INVALID_ARGUMENT;
-  }
-  return GBS_SUCCESS;
-}
-
-extern "C" int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb,
-                                      double* d_x, int ldx, int tier, double tol, int max_iter, gbs_refine_info* info,
-                                      void* stream)
-{
-  GBS_TRY(check_mixed_args(n, nrhs, lda, ldb, ldx, tier, max_iter));
-  GBS_TRY(ensure_device());
-  MixedOptions opt;
-  opt.tier = tier;
-  opt.tol = tol;
-  opt.max_iter = max_iter;
-  MixedResult r;
-  WorkspaceLease lease;
-  if (lease.status != GBS_SUCCESS) return lease.status;
-  cudaStream_t s = stream ? (cudaStream_t)stream : lease.ws->stream;
-  GBS_TRY(mixed_lu_solve(s, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, opt, &r));
-  fill_info(info, r);
-  return GBS_SUCCESS;
-}
-
-extern "C" int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
-                               int tier, double tol, int max_iter, gbs_refine_info* info)
-{
-  GBS_TRY(check_mixed_args(n, nrhs, lda, ldb, ldx, tier, max_iter));
-  if (n == 0 || nrhs == 0) return GBS_SUCCESS;
-  WorkspaceLease lease;
-  if (lease.status != GBS_SUCCESS) return lease.status;
-  Workspace& w = *lease.ws;
-  cudaStream_t s = w.stream;
-  GBS_TRY(w.a.reserve(sizeof(double) * (size_t)n * n));
-  GBS_TRY(w.b.reserve(sizeof(double) * (size_t)n * nrhs * 2));
-  double* dA = w.a.as<double>();
-  double* dB = w.b.as<double>();
-  double* dX = dB + (size_t)n * nrhs;
-  GBS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
-                                 cudaMemcpyHostToDevice, s));
-  GBS_CUDA_TRY(cudaMemcpy2DAsync(dB, sizeof(double) * n, b, sizeof(double) * ldb, sizeof(double) * n, nrhs,
-                                 cudaMemcpyHostToDevice, s));
-  MixedOptions opt;
-  opt.tier = tier;
-  opt.tol = tol;
-  opt.max_iter = max_iter;
-  MixedResult r;
-  GBS_TRY(mixed_lu_solve(s, n, nrhs, dA, n, dB, n, dX, n, opt, &r));
-  GBS_CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * ldx, dX, sizeof(double) * n, sizeof(double) * n, nrhs,
-                                 cudaMemcpyDeviceToHost, s));
-  GBS_CUDA_TRY(cudaStreamSynchronize(s));
-  fill_info(info, r);
-  return GBS_SUCCESS;
-}
 
 extern "C" int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, int64_t lda, const float* d_b,
                                int64_t ldb, float* d_c, int64_t ldc, int lower, void* stream)
@@ -94,4 +24,135 @@ extern "C" int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, 
   GBS_TRY(tc_gemm_sub(s, kind, m, n, k, d_a, 1, lda, d_b, 1, ldb, d_c, ldc, lower, w.status.as<DeviceStatus>(), tws));
   DeviceStatus h;
   return read_status(w.status.as<DeviceStatus>(), &h, s);
+}
+
+extern "C" void gbs_refine_options_default(gbs_refine_options* o)
+{
+  if (!o) return;
+  MixedOptions d;
+  o->tier = d.tier;
+  o->refine = d.refine;
+  o->tol = d.tol;
+  o->max_iter = d.max_iter;
+  o->gmres_restart = d.gmres_restart;
+  o->gmres_tol = d.gmres_tol;
+  o->shift_factor = d.shift_factor;
+}
+
+static int to_options(const gbs_refine_options* o, MixedOptions* m)
+{
+  MixedOptions d;
+  if (o) {
+    d.tier = o->tier;
+    d.refine = o->refine;
+    d.tol = o->tol;
+    d.max_iter = o->max_iter;
+    d.gmres_restart = o->gmres_restart;
+    d.gmres_tol = o->gmres_tol;
+    d.shift_factor = o->shift_factor;
+  }
+  if (d.tier < GBS_TIER_FP64 || d.tier > GBS_TIER_FP16 || d.refine < GBS_REFINE_AUTO || d.refine > GBS_REFINE_GMRES ||
+      d.max_iter < 0 || d.gmres_restart < 1 || d.gmres_restart > 200 || !(d.tol >= 0) || !(d.shift_factor >= 0)) {
+    gbs_set_last_message("invalid gbs_refine_options");
+    return GBS_INVALID_ARGUMENT;
+  }
+  *m = d;
+  return GBS_SUCCESS;
+}
+
+static void fill_info(gbs_refine_info* info, const MixedResult& r)
+{
+  if (!info) return;
+  info->tier_used = r.tier;
+  info->solver = r.solver;
+  info->iterations = r.iterations;
+  info->inner_iterations = r.inner_iterations;
+  info->fell_back = r.fell_back;
+  info->singular = r.singular;
+  info->backward_error = r.backward_error;
+  info->shift = r.shift;
+}
+
+static int check_dims(int n, int nrhs, int lda, int ldb, int ldx)
+{
+  if (n < 0 || nrhs < 0 || lda < std::max(1, n) || ldb < std::max(1, n) || ldx < std::max(1, n)) {
+    gbs_set_last_message("mixed solver: invalid size or leading dimension");
+    return GBS_INVALID_ARGUMENT;
+  }
+  return GBS_SUCCESS;
+}
+
+typedef int (*MixedFn)(cudaStream_t, int, int, const double*, int64_t, const double*, int64_t, double*, int64_t,
+                       const MixedOptions&, MixedResult*);
+
+static int run_device(MixedFn fn, int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
+                      int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream)
+{
+  GBS_TRY(check_dims(n, nrhs, lda, ldb, ldx));
+  MixedOptions o;
+  GBS_TRY(to_options(opt, &o));
+  GBS_TRY(ensure_device());
+  WorkspaceLease lease;
+  if (lease.status != GBS_SUCCESS) return lease.status;
+  cudaStream_t s = stream ? (cudaStream_t)stream : lease.ws->stream;
+  MixedResult r;
+  const int rc = fn(s, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, o, &r);
+  fill_info(info, r);
+  return rc;
+}
+
+static int run_host(MixedFn fn, int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
+                    const gbs_refine_options* opt, gbs_refine_info* info)
+{
+  GBS_TRY(check_dims(n, nrhs, lda, ldb, ldx));
+  MixedOptions o;
+  GBS_TRY(to_options(opt, &o));
+  if (n == 0 || nrhs == 0) return GBS_SUCCESS;
+  WorkspaceLease lease;
+  if (lease.status != GBS_SUCCESS) return lease.status;
+  Workspace& w = *lease.ws;
+  cudaStream_t s = w.stream;
+  GBS_TRY(w.a.reserve(sizeof(double) * (size_t)n * n));
+  GBS_TRY(w.b.reserve(sizeof(double) * (size_t)n * nrhs * 2));
+  double* dA = w.a.as<double>();
+  double* dB = w.b.as<double>();
+  double* dX = dB + (size_t)n * nrhs;
+  GBS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
+                                 cudaMemcpyHostToDevice, s));
+  GBS_CUDA_TRY(cudaMemcpy2DAsync(dB, sizeof(double) * n, b, sizeof(double) * ldb, sizeof(double) * n, nrhs,
+                                 cudaMemcpyHostToDevice, s));
+  MixedResult r;
+  const int rc = fn(s, n, nrhs, dA, n, dB, n, dX, n, o, &r);
+  fill_info(info, r);
+  if (rc != GBS_SUCCESS) return rc;
+  GBS_CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * ldx, dX, sizeof(double) * n, sizeof(double) * n, nrhs,
+                                 cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb,
+                                      double* d_x, int ldx, const gbs_refine_options* opt, gbs_refine_info* info,
+                                      void* stream)
+{
+  return run_device(mixed_lu_solve, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, opt, info, stream);
+}
+
+extern "C" int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
+                               const gbs_refine_options* opt, gbs_refine_info* info)
+{
+  return run_host(mixed_lu_solve, n, nrhs, a, lda, b, ldb, x, ldx, opt, info);
+}
+
+extern "C" int gbs_dposv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb,
+                                      double* d_x, int ldx, const gbs_refine_options* opt, gbs_refine_info* info,
+                                      void* stream)
+{
+  return run_device(mixed_llt_solve, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, opt, info, stream);
+}
+
+extern "C" int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
+                               const gbs_refine_options* opt, gbs_refine_info* info)
+{
+  return run_host(mixed_llt_solve, n, nrhs, a, lda, b, ldb, x, ldx, opt, info);
 }

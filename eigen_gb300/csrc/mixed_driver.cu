@@ -1,18 +1,22 @@
-// Mixed-precision LU + FP64 iterative refinement (the LAPACK dsgesv idea,
-// with the factorization's trailing updates on the tcgen05 tensor cores).
+// Mixed-precision factorizations + FP64 refinement (the LAPACK dsgesv /
+// dsposv idea, with the trailing updates on the tcgen05 tensor cores).
 //
-//   1. A32 = fp32(A)                                     (HBM-bound cast)
-//   2. P A32 = L U: 128-column outer panels; each panel is factored by the
-//      cooperative register kernel (32 columns at a time) with its inner
-//      updates and the outer trailing update A22 -= A21 A12 on tensor cores
-//      in the tier's precision (BF16 / FP16 / TF32 / 3xTF32)
-//   3. x = U^-1 L^-1 P b in FP32 (persistent triangular solves)
-//   4. repeat: r = b - A x in FP64 (split-K DFMA, deterministic reduction);
-//      stop when max_j ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf)
-//      <= tol; d = LU^-1 (r / s) in FP32 with s = ||r_j||_inf per column;
-//      x += s d in FP64
-//   5. refinement that stops decreasing (or runs out of iterations) falls
-//      back to the plain FP64 factorization, which then decides the result.
+// Factorizations (FP32 working storage, tensor-core updates in the tier's
+// precision: BF16 / FP16 / TF32 / 3xTF32):
+//   mixed_getrf  P A = L U: 128-column outer panels, each factored 32 columns
+//                at a time by the cooperative register kernel; inner and outer
+//                trailing updates A22 -= A21 A12 on tensor cores
+//   mixed_potrf  D A D + sigma I = L L^T, D = diag(A)^-1/2 (unit diagonal, so
+//                FP16 cannot overflow), the reference's block size; diagonal
+//                blocks and TRSM on FP32 cores, SYRK on tensor cores
+// Refinement (FP64 residuals against the original matrix):
+//   classic IR   x += M^-1 r until the normwise backward error
+//                max_j ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol
+//   GMRES-IR     each correction solves M^-1 A d = M^-1 r with GMRES
+//                (CGS2 orthogonalisation, FP64), preconditioner applied in
+//                FP32 (Carson & Higham, SIAM J. Sci. Comput. 40(2), 2018)
+// A refinement whose backward error stops halving, or a low-precision
+// factorization that breaks down, falls back to the plain FP64 factorization.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -29,10 +33,10 @@ namespace gbs {
 static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 // ------------------------------------------------------------------ kernels
-// R = B - A X, FP64.  Grid (row blocks of 128, K splits); each thread owns one
-// row and RC right-hand sides; X's K-chunk is staged in shared memory.
-// Partial sums go to part[split][col][row]; residual_reduce adds them in
-// split order (deterministic).
+// Y = A X (B == null) or R = B - A X, FP64.  Grid (row blocks of 128, K
+// splits); a thread owns one row and up to 16 right-hand sides; the K-chunk
+// of X is staged in shared memory.  Partial sums per split are added in split
+// order by residual_reduce (deterministic).
 constexpr int kResRows = 128, kResRC = 16, kResKC = 64;
 
 __global__ void __launch_bounds__(kResRows)
@@ -68,23 +72,57 @@ residual_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t l
   }
 }
 
+// Symmetric A stored in the lower triangle: the same product with
+// A(i,k) = A(k,i) read from the lower part (k > i).
+__global__ void __launch_bounds__(kResRows)
+symv_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t lda, const double* __restrict__ X,
+                    int64_t ldx, int kspan, double* __restrict__ part)
+{
+  __shared__ double sx[kResKC][kResRC];
+  const int row = blockIdx.x * kResRows + threadIdx.x;
+  const int split = blockIdx.y;
+  const int k0 = split * kspan, k1 = min(n, k0 + kspan);
+  double acc[kResRC];
+#pragma unroll
+  for (int c = 0; c < kResRC; ++c) acc[c] = 0.0;
+  for (int kc = k0; kc < k1; kc += kResKC) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kResKC * kResRC; e += kResRows) {
+      const int kk = e % kResKC, c = e / kResKC;
+      sx[kk][c] = (kc + kk < k1 && c < nrhs) ? X[(int64_t)c * ldx + kc + kk] : 0.0;
+    }
+    __syncthreads();
+    if (row < n) {
+      const int kend = min(kResKC, k1 - kc);
+      for (int kk = 0; kk < kend; ++kk) {
+        const int col = kc + kk;
+        const double a = col <= row ? A[(int64_t)col * lda + row] : A[(int64_t)row * lda + col];
+#pragma unroll
+        for (int c = 0; c < kResRC; ++c) acc[c] = fma(a, sx[kk][c], acc[c]);
+      }
+    }
+  }
+  if (row < n) {
+    for (int c = 0; c < nrhs; ++c) part[((int64_t)split * nrhs + c) * n + row] = acc[c];
+  }
+}
+
 __global__ void residual_reduce_kernel(int n, int nrhs, int splits, const double* __restrict__ part,
-                                       const double* __restrict__ B, int64_t ldb, double* __restrict__ R)
+                                       const double* __restrict__ B, int64_t ldb, double* __restrict__ R, int64_t ldr)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * nrhs) return;
   const int row = (int)(t % n), c = (int)(t / n);
   double s = 0.0;
   for (int k = 0; k < splits; ++k) s += part[((int64_t)k * nrhs + c) * n + row];
-  R[(int64_t)c * n + row] = B[(int64_t)c * ldb + row] - s;
+  R[(int64_t)c * ldr + row] = B ? B[(int64_t)c * ldb + row] - s : s;
 }
 
-// out[c] = max_i |V(i, c)| for the three matrices (R, X, B) of one refinement
-// step, stored as out[0..nrhs) = R, [nrhs..2nrhs) = X, [2nrhs..3nrhs) = B.
+// out[which*nrhs + c] = max_i |V(i, c)| for V = R, X, B (which = 0, 1, 2)
 __global__ void col_absmax3_kernel(int n, int nrhs, const double* R, int64_t ldr, const double* X, int64_t ldx,
                                    const double* B, int64_t ldb, double* out)
 {
-  const int which = blockIdx.y;   // 0 = R, 1 = X, 2 = B
+  const int which = blockIdx.y;
   const int c = blockIdx.x;
   const double* V = which == 0 ? R : which == 1 ? X : B;
   const int64_t ld = which == 0 ? ldr : which == 1 ? ldx : ldb;
@@ -104,13 +142,18 @@ __global__ void col_absmax3_kernel(int n, int nrhs, const double* R, int64_t ldr
   }
 }
 
-// ||A||_inf = max_i sum_j |a_ij| : one thread per row, coalesced over rows.
-__global__ void row_abs_sum_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restrict__ rows)
+// ||A||_inf rows: general (sym = 0) or symmetric with the lower triangle stored
+__global__ void row_abs_sum_kernel(int n, const double* __restrict__ A, int64_t lda, int sym, double* __restrict__ rows)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double s = 0.0;
-  for (int j = 0; j < n; ++j) s += fabs(A[(int64_t)j * lda + i]);
+  if (!sym) {
+    for (int j = 0; j < n; ++j) s += fabs(A[(int64_t)j * lda + i]);
+  } else {
+    for (int j = 0; j <= i; ++j) s += fabs(A[(int64_t)j * lda + i]);
+    for (int j = i + 1; j < n; ++j) s += fabs(A[(int64_t)i * lda + j]);
+  }
   rows[i] = s;
 }
 
@@ -125,7 +168,7 @@ __global__ void scale_to_f32_kernel(int n, int nrhs, const double* __restrict__ 
   W[t] = (float)(R[(int64_t)c * ldr + row] / s);
 }
 
-// X += s_c * W32 (FP64); init != 0: X = s_c * W32
+// X = init ? s_c W : X + s_c W   (FP64)
 __global__ void update_from_f32_kernel(int n, int nrhs, const float* __restrict__ W, const double* __restrict__ scale,
                                        double* __restrict__ X, int64_t ldx, int init)
 {
@@ -138,14 +181,82 @@ __global__ void update_from_f32_kernel(int n, int nrhs, const float* __restrict_
   *xp = init ? d : *xp + d;
 }
 
+// W32 (packed n x nrhs) *= d (FP32 diagonal scaling of the LLT tier)
+__global__ void diag_scale_f32_kernel(int n, int nrhs, const float* __restrict__ d, float* __restrict__ W)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * nrhs) return;
+  W[t] *= d[t % n];
+}
+
+// As32(i,j) = fp32(d_i a_ij d_j) (+ sigma on the diagonal), lower triangle;
+// d_i = 1 / sqrt(a_ii).  Also writes d in FP32.
+__global__ void scale_spd_kernel(int n, const double* __restrict__ A, int64_t lda, double sigma,
+                                 float* __restrict__ As, float* __restrict__ d32)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * n) return;
+  const int i = (int)(t % n), j = (int)(t / n);
+  if (i < j) return;
+  const double di = 1.0 / sqrt(A[(int64_t)i * lda + i]);
+  const double dj = 1.0 / sqrt(A[(int64_t)j * lda + j]);
+  double v = di * A[(int64_t)j * lda + i] * dj;
+  if (i == j) {
+    v += sigma;
+    d32[i] = (float)di;
+  }
+  As[(int64_t)j * n + i] = (float)v;
+}
+
+// ---- GMRES helpers; the Krylov basis is stored as slabs V_i (n x nrhs, ld n)
+// out[i*nrhs + c] = <V_i(:,c), W(:,c)>, i < k
+__global__ void gmres_dots_kernel(int n, int nrhs, const double* __restrict__ V, const double* __restrict__ W,
+                                  double* __restrict__ out)
+{
+  const int i = blockIdx.x, c = blockIdx.y;
+  const double* v = V + (int64_t)i * n * nrhs + (int64_t)c * n;
+  const double* w = W + (int64_t)c * n;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) s = fma(v[t], w[t], s);
+  s = warp_sum(s);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+    s = warp_sum(s);
+    if (threadIdx.x == 0) out[i * nrhs + c] = s;
+  }
+}
+
+// W(:,c) += sign * sum_{i<k} coef[i*nrhs + c] V_i(:,c)   (W with leading dimension ldw)
+__global__ void gmres_combine_kernel(int n, int nrhs, int k, const double* __restrict__ V,
+                                     const double* __restrict__ coef, double sign, double* __restrict__ W, int64_t ldw)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * nrhs) return;
+  const int row = (int)(t % n), c = (int)(t / n);
+  double s = 0.0;
+  for (int i = 0; i < k; ++i) s = fma(coef[i * nrhs + c], V[(int64_t)i * n * nrhs + (int64_t)c * n + row], s);
+  W[(int64_t)c * ldw + row] += sign * s;
+}
+
+// V_out(:,c) = W(:,c) * inv[c]
+__global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W, const double* __restrict__ inv,
+                                   double* __restrict__ Vout)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * nrhs) return;
+  Vout[t] = W[t] * inv[t / n];
+}
+
 // ------------------------------------------------------------------ workspace pool
 struct MixedWork {
   cudaStream_t stream = nullptr;
-  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, x64, map;
+  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, z, v, w, coef;
   SolveWork sw;
   TcWorkspace tc;
   HostBuf hstats;
-  Workspace plain;
 };
 
 static std::mutex g_mpool_mu;
@@ -165,14 +276,7 @@ struct MixedLease {
         g_mpool.pop_back();
       }
     }
-    if (!w) {
-      w = new MixedWork();
-      if (cudaStreamCreateWithFlags(&w->stream, cudaStreamDefault) != cudaSuccess) {
-        delete w;
-        w = nullptr;
-        status = GBS_CUDA_ERROR;
-      }
-    }
+    if (!w) w = new MixedWork();
   }
   ~MixedLease()
   {
@@ -182,15 +286,20 @@ struct MixedLease {
   }
 };
 
-// ------------------------------------------------------------------ factorization
+static int tc_kind(int tier)
+{
+  return tier == GBS_TIER_BF16 ? TC_BF16 : tier == GBS_TIER_FP16 ? TC_FP16 : tier == GBS_TIER_TF32 ? TC_TF32 : TC_TF32X3;
+}
+
+// ------------------------------------------------------------------ factorizations
 constexpr int kMixedNB = 128;
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
                 TcWorkspace& tcw, SolveWork& sw, DevBuf& map)
 {
+  (void)sw;
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
-    // ---- panel [k:n, k:k+kb]
     for (int j = k; j < k + kb; j += kPanelNB) {
       const int jb = std::min(kPanelNB, k + kb - j);
       float* Ajj = A + (int64_t)j * lda + j;
@@ -209,7 +318,6 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
           GBS_TRY(tc_gemm_sub(s, kind, rows, rest, jb, Ajj + jb, 1, lda, A12, 1, lda, A12 + jb, lda, 0, st, tcw));
       }
     }
-    // ---- interchanges outside the panel, TRSM of A12, trailing update
     GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, k, k + kb, 0, k, k + kb, n, map));
     const int nr = n - k - kb;
     if (nr > 0) {
@@ -222,40 +330,351 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
   return GBS_SUCCESS;
 }
 
-// ------------------------------------------------------------------ refinement
-static int residual(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* X, int64_t ldx,
-                    const double* B, int64_t ldb, double* R, MixedWork& w)
+// Cholesky of the lower triangle of As (FP32, ld = lda) with the reference's
+// block size; diagonal blocks and TRSM on FP32 cores, SYRK on tensor cores.
+int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st, int kind, TcWorkspace& tcw)
 {
+  static bool attr = false;
+  const int max_bs = 128;
+  if (!attr) {
+    GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(float) * max_bs * (max_bs + 1))));
+    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64))));
+    attr = true;
+  }
+  int bs = n < 32 ? n : std::min(std::max((n / 8 / 16) * 16, 8), max_bs);
+  for (int k = 0; k < n; k += bs) {
+    const int b = std::min(bs, n - k);
+    const int rs = n - k - b;
+    float* Akk = As + (int64_t)k * lda + k;
+    {
+      PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
+      potrf_diag_kernel<float><<<1, 256, sizeof(float) * b * (b + 1), s>>>(Akk, lda, b, k, st);
+      GBS_CUDA_TRY(cudaGetLastError());
+    }
+    if (rs > 0) {
+      float* A21 = Akk + b;
+      {
+        PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, 8.0 * rs * b);
+        trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64), s>>>(Akk, lda, b, A21,
+                                                                                                   lda, rs, st);
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
+      GBS_TRY(tc_gemm_sub(s, kind, rs, rs, b, A21, 1, lda, A21, lda, 1, A21 + (int64_t)b * lda, lda, 1, st, tcw));
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ refinement engine
+struct Problem {
+  int n, nrhs;
+  const double* A;
+  int64_t lda;
+  int sym;            // 1: A symmetric, lower triangle stored
+  const double* B;
+  int64_t ldb;
+  double* X;
+  int64_t ldx;
+};
+
+// Applies M^-1 to W32 (packed n x nrhs, FP32) in place.
+struct Precond {
+  int kind;           // 0 = LU (A32, tr), 1 = scaled LLT (As32 lower, d32)
+  int n;
+  float* F;
+  const int* tr;
+  const float* d;
+};
+
+static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, SolveWork& sw)
+{
+  if (M.kind == 0) return lu_solve_device<float>(s, M.n, nrhs, M.F, M.n, M.tr, W, M.n, 0, sw);
+  const int64_t tot = (int64_t)M.n * nrhs;
+  count_launch();
+  diag_scale_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(M.n, nrhs, M.d, W);
+  GBS_TRY(llt_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, W, M.n, sw));
+  count_launch();
+  diag_scale_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(M.n, nrhs, M.d, W);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+// Y = A X (B == null) or Y = B - A X, FP64 (Y with leading dimension ldy)
+static int apply_a(cudaStream_t s, const Problem& P, const double* X, int64_t ldx, const double* B, int64_t ldb, double* Y,
+                   int64_t ldy, int nrhs, MixedWork& w)
+{
+  const int n = P.n;
   const int splits = std::max(1, std::min(32, cdiv((int64_t)device_sm_count() * 4, cdiv(n, kResRows))));
   const int kspan = cdiv(cdiv(n, splits), kResKC) * kResKC;
   const int used = cdiv(n, kspan);
   GBS_TRY(w.part.reserve(sizeof(double) * (size_t)used * n * nrhs));
   {
     PhaseScope ps(s, PH_RESIDUAL, 2.0 * n * (double)n * nrhs, 8.0 * ((double)n * n + 2.0 * n * nrhs));
-    residual_partial_kernel<<<dim3(cdiv(n, kResRows), used), kResRows, 0, s>>>(n, nrhs, A, lda, X, ldx, kspan,
-                                                                               w.part.as<double>());
+    if (P.sym)
+      symv_partial_kernel<<<dim3(cdiv(n, kResRows), used), kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan,
+                                                                             w.part.as<double>());
+    else
+      residual_partial_kernel<<<dim3(cdiv(n, kResRows), used), kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan,
+                                                                                 w.part.as<double>());
     GBS_CUDA_TRY(cudaGetLastError());
   }
   count_launch();
-  residual_reduce_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, used, w.part.as<double>(), B, ldb, R);
+  residual_reduce_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, used, w.part.as<double>(), B, ldb, Y,
+                                                                      ldy);
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }
 
-static double host_backward_error(int nrhs, const double* st, double anorm, double* worst_out)
+// max_j backward error of the current X (computes R = B - A X into w.r)
+static int backward_error(cudaStream_t s, const Problem& P, double anorm, MixedWork& w, double* be)
 {
+  const int n = P.n, nrhs = P.nrhs;
+  double* R = w.r.as<double>();
+  GBS_TRY(apply_a(s, P, P.X, P.ldx, P.B, P.ldb, R, n, nrhs, w));
+  count_launch();
+  col_absmax3_kernel<<<dim3(nrhs, 3), 256, 0, s>>>(n, nrhs, R, n, P.X, P.ldx, P.B, P.ldb, w.stats.as<double>());
+  GBS_CUDA_TRY(cudaGetLastError());
+  double* h = (double*)w.hstats.p;
+  GBS_CUDA_TRY(cudaMemcpyAsync(h, w.stats.p, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, s));
+  GBS_TRY(solve_status(s, w.sw));
   double worst = 0.0;
   for (int c = 0; c < nrhs; ++c) {
-    const double rn = st[c], xn = st[nrhs + c], bn = st[2 * nrhs + c];
-    const double den = anorm * xn + bn;
-    double e = den > 0 ? rn / den : rn;
+    const double den = anorm * h[nrhs + c] + h[2 * nrhs + c];
+    double e = den > 0 ? h[c] / den : h[c];
     if (e != e) e = INFINITY;
     worst = std::max(worst, e);
   }
-  if (worst_out) *worst_out = worst;
-  return worst;
+  *be = worst;
+  return GBS_SUCCESS;
 }
 
+// D64 (n x nrhs, ld n) = M^-1 Y64 via FP32 with per-column scaling
+static int precond_f64(cudaStream_t s, const Precond& M, const double* Y, double* D, int nrhs, MixedWork& w)
+{
+  const int n = M.n;
+  const int64_t tot = (int64_t)n * nrhs;
+  double* sc = w.stats.as<double>() + 3 * nrhs;
+  count_launch();
+  col_absmax3_kernel<<<dim3(nrhs, 1), 256, 0, s>>>(n, nrhs, Y, n, Y, n, Y, n, sc);
+  count_launch();
+  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, Y, n, sc, w.w32.as<float>());
+  GBS_CUDA_TRY(cudaGetLastError());
+  GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
+  count_launch();
+  update_from_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.w32.as<float>(), sc, D, n, 1);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+// One GMRES-IR correction: X += d with (M^-1 A) d ~= M^-1 r (r = w.r).
+static int gmres_correction(cudaStream_t s, const Problem& P, const Precond& M, int mmax, double tau, MixedWork& w,
+                            int* inner_its)
+{
+  const int n = P.n, nrhs = P.nrhs;
+  const int64_t slab = (int64_t)n * nrhs;
+  GBS_TRY(w.v.reserve(sizeof(double) * (size_t)slab * (mmax + 1)));
+  GBS_TRY(w.z.reserve(sizeof(double) * (size_t)slab));
+  GBS_TRY(w.coef.reserve(sizeof(double) * (size_t)(mmax + 2) * nrhs * 2));
+  double* V = w.v.as<double>();
+  double* Z = w.z.as<double>();
+  double* coef = w.coef.as<double>();
+  std::vector<double> hcoef((size_t)(mmax + 2) * nrhs);
+  // z0 = M^-1 r ; beta = ||z0|| ; V_0 = z0 / beta
+  GBS_TRY(precond_f64(s, M, w.r.as<double>(), Z, nrhs, w));
+  count_launch();
+  gmres_dots_kernel<<<dim3(1, nrhs), 256, 0, s>>>(n, nrhs, Z, Z, coef);
+  GBS_CUDA_TRY(cudaMemcpyAsync(hcoef.data(), coef, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<double> beta(nrhs), inv(nrhs);
+  for (int c = 0; c < nrhs; ++c) {
+    beta[c] = std::sqrt(hcoef[c]);
+    inv[c] = beta[c] > 0 ? 1.0 / beta[c] : 0.0;
+  }
+  GBS_CUDA_TRY(cudaMemcpyAsync(coef, inv.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+  count_launch();
+  gmres_scale_kernel<<<cdiv(slab, 256), 256, 0, s>>>(n, nrhs, Z, coef, V);
+  // Hessenberg + Givens per column
+  std::vector<double> H((size_t)(mmax + 1) * mmax * nrhs, 0.0), cs((size_t)mmax * nrhs), sn((size_t)mmax * nrhs),
+      g((size_t)(mmax + 1) * nrhs, 0.0);
+  auto Hc = [&](int i, int j, int c) -> double& { return H[((size_t)c * (mmax + 1) + i) * mmax + j]; };
+  for (int c = 0; c < nrhs; ++c) g[(size_t)c * (mmax + 1)] = beta[c];
+  std::vector<char> done(nrhs, 0);
+  for (int c = 0; c < nrhs; ++c) done[c] = beta[c] == 0.0;
+  int m = 0;
+  for (int j = 0; j < mmax; ++j) {
+    double* Vj = V + (int64_t)j * slab;
+    double* Vn = V + (int64_t)(j + 1) * slab;
+    // w = M^-1 A V_j  (into Vn as scratch)
+    GBS_TRY(apply_a(s, P, Vj, n, nullptr, 0, Vn, n, nrhs, w));
+    GBS_TRY(precond_f64(s, M, Vn, Z, nrhs, w));
+    // CGS2: h = V^T z ; z -= V h ; twice
+    std::vector<double> hsum((size_t)(j + 1) * nrhs, 0.0);
+    for (int pass = 0; pass < 2; ++pass) {
+      count_launch();
+      gmres_dots_kernel<<<dim3(j + 1, nrhs), 256, 0, s>>>(n, nrhs, V, Z, coef);
+      count_launch();
+      gmres_combine_kernel<<<cdiv(slab, 256), 256, 0, s>>>(n, nrhs, j + 1, V, coef, -1.0, Z, n);
+      GBS_CUDA_TRY(cudaMemcpyAsync(hcoef.data(), coef, sizeof(double) * (j + 1) * nrhs, cudaMemcpyDeviceToHost, s));
+      GBS_CUDA_TRY(cudaStreamSynchronize(s));
+      for (size_t q = 0; q < hsum.size(); ++q) hsum[q] += hcoef[q];
+    }
+    count_launch();
+    gmres_dots_kernel<<<dim3(1, nrhs), 256, 0, s>>>(n, nrhs, Z, Z, coef);
+    GBS_CUDA_TRY(cudaMemcpyAsync(hcoef.data(), coef, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    GBS_CUDA_TRY(cudaStreamSynchronize(s));
+    bool all_done = true;
+    for (int c = 0; c < nrhs; ++c) {
+      const double hn = std::sqrt(std::max(hcoef[c], 0.0));
+      for (int i = 0; i <= j; ++i) Hc(i, j, c) = hsum[(size_t)i * nrhs + c];
+      Hc(j + 1, j, c) = hn;
+      inv[c] = hn > 0 ? 1.0 / hn : 0.0;
+      // apply previous rotations, then a new one
+      for (int i = 0; i < j; ++i) {
+        const double a = Hc(i, j, c), b = Hc(i + 1, j, c);
+        const double C = cs[(size_t)c * mmax + i], S = sn[(size_t)c * mmax + i];
+        Hc(i, j, c) = C * a + S * b;
+        Hc(i + 1, j, c) = -S * a + C * b;
+      }
+      const double a = Hc(j, j, c), b = Hc(j + 1, j, c);
+      const double r = std::hypot(a, b);
+      const double C = r > 0 ? a / r : 1.0, S = r > 0 ? b / r : 0.0;
+      cs[(size_t)c * mmax + j] = C;
+      sn[(size_t)c * mmax + j] = S;
+      Hc(j, j, c) = r;
+      Hc(j + 1, j, c) = 0.0;
+      double& gj = g[(size_t)c * (mmax + 1) + j];
+      double& gj1 = g[(size_t)c * (mmax + 1) + j + 1];
+      gj1 = -S * gj;
+      gj = C * gj;
+      if (done[c] || beta[c] == 0.0 || std::fabs(gj1) <= tau * beta[c] || hn == 0.0) done[c] = 1;
+      all_done = all_done && done[c];
+    }
+    GBS_CUDA_TRY(cudaMemcpyAsync(coef, inv.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+    count_launch();
+    gmres_scale_kernel<<<cdiv(slab, 256), 256, 0, s>>>(n, nrhs, Z, coef, Vn);
+    m = j + 1;
+    if (all_done) break;
+  }
+  // y = R^-1 g (per column), X += V y
+  std::vector<double> y((size_t)m * nrhs, 0.0);
+  for (int c = 0; c < nrhs; ++c) {
+    if (beta[c] == 0.0) continue;
+    for (int i = m - 1; i >= 0; --i) {
+      double acc = g[(size_t)c * (mmax + 1) + i];
+      for (int k = i + 1; k < m; ++k) acc -= Hc(i, k, c) * y[(size_t)k * nrhs + c];
+      const double d = Hc(i, i, c);
+      y[(size_t)i * nrhs + c] = d != 0 ? acc / d : 0.0;
+    }
+  }
+  GBS_CUDA_TRY(cudaMemcpyAsync(coef, y.data(), sizeof(double) * m * nrhs, cudaMemcpyHostToDevice, s));
+  count_launch();
+  gmres_combine_kernel<<<cdiv(slab, 256), 256, 0, s>>>(n, nrhs, m, V, coef, 1.0, P.X, P.ldx);
+  GBS_CUDA_TRY(cudaGetLastError());
+  *inner_its += m;
+  return GBS_SUCCESS;
+}
+
+// Refines P.X (already holding x0) to the backward-error bound.  Returns
+// converged through *ok.
+static int refine(cudaStream_t s, const Problem& P, const Precond& M, bool use_gmres, const MixedOptions& opt,
+                  double anorm, MixedWork& w, MixedResult& out, bool* ok)
+{
+  const int n = P.n, nrhs = P.nrhs;
+  *ok = false;
+  double prev = INFINITY;
+  int stalls = 0;
+  for (int it = 0; it <= opt.max_iter; ++it) {
+    double be = 0;
+    GBS_TRY(backward_error(s, P, anorm, w, &be));
+    out.backward_error = be;
+    out.iterations = it;
+    if (be <= opt.tol) { *ok = true; return GBS_SUCCESS; }
+    if (!(be < 0.5 * prev)) { if (++stalls >= 2) return GBS_SUCCESS; } else stalls = 0;
+    prev = std::min(prev, be);
+    if (it == opt.max_iter) break;
+    if (use_gmres) {
+      GBS_TRY(gmres_correction(s, P, M, opt.gmres_restart, opt.gmres_tol, w, &out.inner_iterations));
+    } else {
+      double* sc = w.stats.as<double>();
+      const int64_t tot = (int64_t)n * nrhs;
+      count_launch();
+      scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.r.as<double>(), n, sc, w.w32.as<float>());
+      GBS_CUDA_TRY(cudaGetLastError());
+      GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
+      count_launch();
+      update_from_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.w32.as<float>(), sc, P.X, P.ldx, 0);
+      GBS_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+static int reserve_common(MixedWork& w, int n, int nrhs)
+{
+  GBS_TRY(w.st.reserve(sizeof(DeviceStatus)));
+  GBS_TRY(w.r.reserve(sizeof(double) * (size_t)n * nrhs));
+  GBS_TRY(w.w32.reserve(sizeof(float) * (size_t)n * nrhs));
+  GBS_TRY(w.stats.reserve(sizeof(double) * (4 * nrhs + 4)));
+  GBS_TRY(w.rows.reserve(sizeof(double) * (size_t)n));
+  GBS_TRY(w.hstats.reserve(sizeof(double) * (4 * nrhs + 4)));
+  return GBS_SUCCESS;
+}
+
+static int inf_norm(cudaStream_t s, const Problem& P, MixedWork& w, double* anorm)
+{
+  count_launch();
+  row_abs_sum_kernel<<<cdiv(P.n, 256), 256, 0, s>>>(P.n, P.A, P.lda, P.sym, w.rows.as<double>());
+  GBS_CUDA_TRY(cudaGetLastError());
+  std::vector<double> h((size_t)P.n);
+  GBS_CUDA_TRY(cudaMemcpyAsync(h.data(), w.rows.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  double a = 0;
+  for (double v : h) a = std::max(a, v);
+  *anorm = a;
+  return GBS_SUCCESS;
+}
+
+// x0 = M^-1 b
+static int initial_solve(cudaStream_t s, const Problem& P, const Precond& M, MixedWork& w)
+{
+  const int n = P.n, nrhs = P.nrhs;
+  const int64_t tot = (int64_t)n * nrhs;
+  double* sc = w.stats.as<double>();
+  count_launch();
+  col_absmax3_kernel<<<dim3(nrhs, 1), 256, 0, s>>>(n, nrhs, P.B, P.ldb, P.B, P.ldb, P.B, P.ldb, sc);
+  count_launch();
+  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, P.B, P.ldb, sc, w.w32.as<float>());
+  GBS_CUDA_TRY(cudaGetLastError());
+  GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
+  count_launch();
+  update_from_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.w32.as<float>(), sc, P.X, P.ldx, 1);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+template <typename Fn>
+static int per_group(int nrhs, MixedResult* res, Fn fn)
+{
+  MixedResult worst;
+  bool first = true;
+  for (int c0 = 0; c0 < nrhs; c0 += kResRC) {
+    MixedResult r;
+    GBS_TRY(fn(c0, std::min(kResRC, nrhs - c0), &r));
+    if (first) { worst = r; first = false; continue; }
+    worst.iterations = std::max(worst.iterations, r.iterations);
+    worst.inner_iterations = std::max(worst.inner_iterations, r.inner_iterations);
+    worst.fell_back |= r.fell_back;
+    worst.singular |= r.singular;
+    worst.backward_error = std::max(worst.backward_error, r.backward_error);
+    if (r.fell_back) worst.tier = r.tier;
+  }
+  if (res) *res = worst;
+  return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ LU front end
 int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
                    double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
 {
@@ -265,106 +684,45 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
     if (res) *res = out;
     return GBS_SUCCESS;
   }
-  if (nrhs > kResRC) {
-    // refine independent 16-column groups
-    MixedResult worst;
-    for (int c0 = 0; c0 < nrhs; c0 += kResRC) {
-      MixedResult r;
-      const int nc = std::min(kResRC, nrhs - c0);
-      GBS_TRY(mixed_lu_solve(s, n, nc, A, lda, B + (int64_t)c0 * ldb, ldb, X + (int64_t)c0 * ldx, ldx, opt, &r));
-      worst.iterations = std::max(worst.iterations, r.iterations);
-      worst.fell_back |= r.fell_back;
-      worst.backward_error = std::max(worst.backward_error, r.backward_error);
-      worst.tier = r.tier;
-    }
-    if (res) *res = worst;
-    return GBS_SUCCESS;
-  }
+  if (nrhs > kResRC)
+    return per_group(nrhs, res, [&](int c0, int nc, MixedResult* r) {
+      return mixed_lu_solve(s, n, nc, A, lda, B + (int64_t)c0 * ldb, ldb, X + (int64_t)c0 * ldx, ldx, opt, r);
+    });
   MixedLease lease;
   if (lease.status != GBS_SUCCESS) return lease.status;
   MixedWork& w = *lease.w;
-  const size_t nn = (size_t)n * n;
-  GBS_TRY(w.a32.reserve(sizeof(float) * nn));
+  GBS_TRY(reserve_common(w, n, nrhs));
+  GBS_TRY(w.a32.reserve(sizeof(float) * (size_t)n * n));
   GBS_TRY(w.tr.reserve(sizeof(int) * (size_t)n));
-  GBS_TRY(w.st.reserve(sizeof(DeviceStatus)));
-  GBS_TRY(w.r.reserve(sizeof(double) * (size_t)n * nrhs));
-  GBS_TRY(w.w32.reserve(sizeof(float) * (size_t)n * nrhs));
-  GBS_TRY(w.stats.reserve(sizeof(double) * (3 * nrhs + 1)));
-  GBS_TRY(w.rows.reserve(sizeof(double) * (size_t)n));
-  GBS_TRY(w.hstats.reserve(sizeof(double) * (3 * nrhs + 1)));
   DeviceStatus* st = w.st.as<DeviceStatus>();
-  float* A32 = w.a32.as<float>();
-  double* R = w.r.as<double>();
-  float* W = w.w32.as<float>();
-  double* stats = w.stats.as<double>();
-  double* hst = (double*)w.hstats.p;
-
-  // ||A||_inf (once)
-  count_launch();
-  row_abs_sum_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, A, lda, w.rows.as<double>());
-  GBS_CUDA_TRY(cudaGetLastError());
-  std::vector<double> hrows((size_t)n);
-  GBS_CUDA_TRY(cudaMemcpyAsync(hrows.data(), w.rows.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-
-  GBS_TRY(reset_status(st, s));
+  Problem P{n, nrhs, A, lda, 0, B, ldb, X, ldx};
   double anorm = 0;
-  for (double v : hrows) anorm = std::max(anorm, v);
-
+  GBS_TRY(inf_norm(s, P, w, &anorm));
   bool converged = false;
   if (opt.tier != GBS_TIER_FP64) {
+    GBS_TRY(reset_status(st, s));
     {
-      PhaseScope ps(s, PH_COPY, 0.0, 12.0 * nn);
-      copy_matrix_kernel<double, float><<<std::min<int64_t>(cdiv(nn, 256), 65535 * 8), 256, 0, s>>>(A, lda, A32, n, n, n);
+      PhaseScope ps(s, PH_COPY, 0.0, 12.0 * (double)n * n);
+      copy_matrix_kernel<double, float><<<std::min<int64_t>(cdiv((int64_t)n * n, 256), 65535 * 8), 256, 0, s>>>(
+          A, lda, w.a32.as<float>(), n, n, n);
       GBS_CUDA_TRY(cudaGetLastError());
     }
-    const int kind = opt.tier == GBS_TIER_BF16 ? TC_BF16 : opt.tier == GBS_TIER_FP16 ? TC_FP16
-                   : opt.tier == GBS_TIER_TF32 ? TC_TF32 : TC_TF32X3;
-    GBS_TRY(mixed_getrf(s, n, A32, n, w.tr.as<int>(), st, w.scratch, kind, w.tc, w.sw, w.map));
+    GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.sw,
+                        w.map));
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {
-      // x0 = LU^-1 b in FP32, scaled per column
-      count_launch();
-      col_absmax3_kernel<<<dim3(nrhs, 3), 256, 0, s>>>(n, nrhs, B, ldb, B, ldb, B, ldb, stats);
-      count_launch();
-      scale_to_f32_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, B, ldb, stats, W);
-      GBS_CUDA_TRY(cudaGetLastError());
-      GBS_TRY(lu_solve_device<float>(s, n, nrhs, A32, n, w.tr.as<int>(), W, n, 0, w.sw));
-      count_launch();
-      update_from_f32_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, W, stats, X, ldx, 1);
-      GBS_CUDA_TRY(cudaGetLastError());
-      double prev = INFINITY;
-      int stalls = 0;
-      for (int it = 0; it <= opt.max_iter; ++it) {
-        GBS_TRY(residual(s, n, nrhs, A, lda, X, ldx, B, ldb, R, w));
-        count_launch();
-        col_absmax3_kernel<<<dim3(nrhs, 3), 256, 0, s>>>(n, nrhs, R, n, X, ldx, B, ldb, stats);
-        GBS_CUDA_TRY(cudaGetLastError());
-        GBS_CUDA_TRY(cudaMemcpyAsync(hst, stats, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, s));
-        GBS_TRY(solve_status(s, w.sw));
-        double be = host_backward_error(nrhs, hst, anorm, nullptr);
-        out.backward_error = be;
-        out.iterations = it;
-        if (be <= opt.tol) { converged = true; break; }
-        if (!(be < 0.5 * prev)) { if (++stalls >= 2) break; } else stalls = 0;
-        prev = std::min(prev, be);
-        if (it == opt.max_iter) break;
-        count_launch();
-        scale_to_f32_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, R, n, stats, W);
-        GBS_CUDA_TRY(cudaGetLastError());
-        GBS_TRY(lu_solve_device<float>(s, n, nrhs, A32, n, w.tr.as<int>(), W, n, 0, w.sw));
-        count_launch();
-        update_from_f32_kernel<<<cdiv((int64_t)n * nrhs, 256), 256, 0, s>>>(n, nrhs, W, stats, X, ldx, 0);
-        GBS_CUDA_TRY(cudaGetLastError());
-      }
+      Precond M{0, n, w.a32.as<float>(), w.tr.as<int>(), nullptr};
+      GBS_TRY(initial_solve(s, P, M, w));
+      const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
+      out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
+      GBS_TRY(refine(s, P, M, gm, opt, anorm, w, out, &converged));
     }
   }
   if (!converged) {
-    // plain FP64 factorization decides the result
     out.fell_back = opt.tier != GBS_TIER_FP64;
     out.tier = GBS_TIER_FP64;
-    GBS_TRY(w.a64.reserve(sizeof(double) * nn));
-    GBS_TRY(w.tr.reserve(sizeof(int) * (size_t)n));
+    GBS_TRY(w.a64.reserve(sizeof(double) * (size_t)n * n));
     GBS_TRY(copy_matrix_device<double>(s, A, lda, w.a64.as<double>(), n, n, n));
     GBS_TRY(reset_status(st, s));
     GBS_TRY(getrf_device<double>(s, n, n, w.a64.as<double>(), n, w.tr.as<int>(), st, w.scratch));
@@ -372,16 +730,89 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
     GBS_TRY(read_status(st, &h, s));
     GBS_TRY(copy_matrix_device<double>(s, B, ldb, X, ldx, n, nrhs));
     GBS_TRY(lu_solve_device<double>(s, n, nrhs, w.a64.as<double>(), n, w.tr.as<int>(), X, ldx, 0, w.sw));
-    GBS_TRY(residual(s, n, nrhs, A, lda, X, ldx, B, ldb, R, w));
-    count_launch();
-    col_absmax3_kernel<<<dim3(nrhs, 3), 256, 0, s>>>(n, nrhs, R, n, X, ldx, B, ldb, stats);
-    GBS_CUDA_TRY(cudaMemcpyAsync(hst, stats, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, s));
-    GBS_TRY(solve_status(s, w.sw));
-    out.backward_error = host_backward_error(nrhs, hst, anorm, nullptr);
+    GBS_TRY(backward_error(s, P, anorm, w, &out.backward_error));
     if (h.info >= 0) out.singular = 1;
   }
   if (res) *res = out;
   return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ LLT front end
+int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
+                    double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
+{
+  MixedResult out;
+  out.tier = opt.tier;
+  if (n <= 0 || nrhs <= 0) {
+    if (res) *res = out;
+    return GBS_SUCCESS;
+  }
+  if (nrhs > kResRC)
+    return per_group(nrhs, res, [&](int c0, int nc, MixedResult* r) {
+      return mixed_llt_solve(s, n, nc, A, lda, B + (int64_t)c0 * ldb, ldb, X + (int64_t)c0 * ldx, ldx, opt, r);
+    });
+  MixedLease lease;
+  if (lease.status != GBS_SUCCESS) return lease.status;
+  MixedWork& w = *lease.w;
+  GBS_TRY(reserve_common(w, n, nrhs));
+  GBS_TRY(w.a32.reserve(sizeof(float) * (size_t)n * n));
+  GBS_TRY(w.d32.reserve(sizeof(float) * (size_t)n));
+  DeviceStatus* st = w.st.as<DeviceStatus>();
+  Problem P{n, nrhs, A, lda, 1, B, ldb, X, ldx};
+  double anorm = 0;
+  GBS_TRY(inf_norm(s, P, w, &anorm));
+  bool converged = false;
+  int not_spd = 0;
+  if (opt.tier != GBS_TIER_FP64) {
+    // unit roundoff of the factorization's products: the shift that keeps the
+    // low-precision Cholesky of D A D positive (Higham & Pranesh) grows by 10
+    // on each breakdown, starting at 0 for the FP32-accurate tier
+    const double uf = opt.tier == GBS_TIER_BF16 ? 0x1p-8 : (opt.tier == GBS_TIER_TF32X3 ? 0x1p-24 : 0x1p-11);
+    double sigma = opt.tier == GBS_TIER_TF32X3 ? 0.0 : opt.shift_factor * uf;
+    for (int attempt = 0; attempt < 4 && !converged; ++attempt) {
+      GBS_TRY(reset_status(st, s));
+      {
+        PhaseScope ps(s, PH_COPY, 0.0, 12.0 * (double)n * n);
+        scale_spd_kernel<<<cdiv((int64_t)n * n, 256), 256, 0, s>>>(n, A, lda, sigma, w.a32.as<float>(),
+                                                                   w.d32.as<float>());
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
+      GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc));
+      DeviceStatus h;
+      GBS_TRY(read_status(st, &h, s));
+      out.shift = sigma;
+      if (h.info >= 0) {
+        sigma = sigma > 0 ? sigma * 10.0 : 8.0 * uf;
+        continue;
+      }
+      Precond M{1, n, w.a32.as<float>(), nullptr, w.d32.as<float>()};
+      GBS_TRY(initial_solve(s, P, M, w));
+      const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
+      out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
+      GBS_TRY(refine(s, P, M, gm, opt, anorm, w, out, &converged));
+      break;
+    }
+  }
+  if (!converged) {
+    out.fell_back = opt.tier != GBS_TIER_FP64;
+    out.tier = GBS_TIER_FP64;
+    GBS_TRY(w.a64.reserve(sizeof(double) * (size_t)n * n));
+    GBS_TRY(copy_matrix_device<double>(s, A, lda, w.a64.as<double>(), n, n, n));
+    GBS_TRY(reset_status(st, s));
+    GBS_TRY(potrf_device<double>(s, n, w.a64.as<double>(), n, 0, st, w.scratch));
+    DeviceStatus h;
+    GBS_TRY(read_status(st, &h, s));
+    if (h.info >= 0) {
+      not_spd = 1;
+    } else {
+      GBS_TRY(copy_matrix_device<double>(s, B, ldb, X, ldx, n, nrhs));
+      GBS_TRY(llt_solve_device<double>(s, n, nrhs, w.a64.as<double>(), n, 0, X, ldx, w.sw));
+      GBS_TRY(backward_error(s, P, anorm, w, &out.backward_error));
+    }
+  }
+  out.singular = not_spd;
+  if (res) *res = out;
+  return not_spd ? GBS_NUMERICAL_ISSUE : GBS_SUCCESS;
 }
 
 }  // namespace gbs

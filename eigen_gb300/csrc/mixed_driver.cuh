@@ -10,19 +10,28 @@ namespace gbs {
 
 struct MixedOptions {
   int tier = GBS_TIER_TF32X3;
-  double tol = 1e-13;     // normwise backward error to reach
-  int max_iter = 30;      // refinement steps before falling back to FP64
+  int refine = GBS_REFINE_AUTO;  // AUTO: classic for TF32X3, GMRES-IR otherwise
+  double tol = 1e-13;            // normwise backward error to reach
+  int max_iter = 30;             // outer refinement steps before the FP64 fallback
+  int gmres_restart = 40;        // Krylov vectors per GMRES-IR correction
+  double gmres_tol = 1e-10;      // relative preconditioned-residual target of one correction
+  double shift_factor = 4.0;     // LLT tiers: initial diagonal shift = shift_factor * u_factorization
 };
 
 struct MixedResult {
-  int tier = GBS_TIER_TF32X3;   // tier that produced the answer (GBS_TIER_FP64 after a fallback)
+  int tier = GBS_TIER_TF32X3;    // tier that produced the answer (GBS_TIER_FP64 after a fallback)
+  int solver = GBS_REFINE_CLASSIC;
   int iterations = 0;
+  int inner_iterations = 0;
   int fell_back = 0;
-  int singular = 0;             // the FP64 factorization met an exactly-zero pivot
+  int singular = 0;              // FP64 factorization met a zero pivot / non-SPD column
   double backward_error = 0.0;
+  double shift = 0.0;
 };
 
 int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
                    double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
+int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
+                    double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
 
 }  // namespace gbs

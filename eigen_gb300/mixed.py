@@ -1,10 +1,11 @@
-"""Mixed-precision solve with FP64 iterative refinement (gbs_dgesv_mixed*).
+"""Mixed-precision solves with FP64 refinement (gbs_dgesv_mixed*, gbs_dposv_mixed*).
 
-``solve_mixed(A, B, tier)`` factors A in a low precision on the tensor cores,
-refines in FP64 to a normwise backward error <= tol and falls back to the
-plain FP64 factorization (the reference's pivots) when refinement stalls.
-A and B are numpy arrays (host buffers) or column-major CUDA torch tensors
-(device buffers, ordered on torch's current stream).
+``solve_mixed(A, B, tier)`` (general A) and ``solve_spd_mixed(A, B, tier)``
+(SPD A, lower triangle read) factor in a low precision on the tensor cores,
+refine in FP64 (classic or GMRES-IR) to a normwise backward error <= tol and
+fall back to the plain FP64 factorization when refinement stalls.  A and B are
+numpy arrays (host buffers) or column-major CUDA torch tensors (device
+buffers, ordered on torch's current stream).
 """
 from __future__ import annotations
 
@@ -16,26 +17,43 @@ from . import _lib as L
 
 TIERS = {"fp64": 0, "tf32x3": 1, "tf32": 2, "bf16": 3, "fp16": 4}
 TIER_NAMES = {v: k for k, v in TIERS.items()}
+REFINE = {"auto": 0, "classic": 1, "gmres": 2}
+REFINE_NAMES = {v: k for k, v in REFINE.items()}
+
+
+class RefineOptions(C.Structure):
+    _fields_ = [("tier", C.c_int), ("refine", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
+                ("gmres_restart", C.c_int), ("gmres_tol", C.c_double), ("shift_factor", C.c_double)]
 
 
 class RefineInfo(C.Structure):
-    _fields_ = [("tier_used", C.c_int), ("iterations", C.c_int), ("fell_back", C.c_int), ("singular", C.c_int),
-                ("backward_error", C.c_double)]
+    _fields_ = [("tier_used", C.c_int), ("solver", C.c_int), ("iterations", C.c_int), ("inner_iterations", C.c_int),
+                ("fell_back", C.c_int), ("singular", C.c_int), ("backward_error", C.c_double),
+                ("shift", C.c_double)]
 
     def as_dict(self):
-        return {"tier_used": TIER_NAMES.get(self.tier_used, self.tier_used), "iterations": self.iterations,
-                "fell_back": bool(self.fell_back), "singular": bool(self.singular),
-                "backward_error": self.backward_error}
+        return {"tier_used": TIER_NAMES.get(self.tier_used, self.tier_used),
+                "solver": REFINE_NAMES.get(self.solver, self.solver), "iterations": self.iterations,
+                "inner_iterations": self.inner_iterations, "fell_back": bool(self.fell_back),
+                "singular": bool(self.singular), "backward_error": self.backward_error, "shift": self.shift}
 
 
-def _tier(t) -> int:
-    return TIERS[t] if isinstance(t, str) else int(t)
+def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=40, gmres_tol=1e-10,
+            shift_factor=4.0) -> RefineOptions:
+    o = RefineOptions()
+    L.lib().gbs_refine_options_default(C.byref(o))
+    o.tier = TIERS[tier] if isinstance(tier, str) else int(tier)
+    o.refine = REFINE[refine] if isinstance(refine, str) else int(refine)
+    o.tol, o.max_iter, o.gmres_restart, o.gmres_tol, o.shift_factor = tol, max_iter, gmres_restart, gmres_tol, \
+        shift_factor
+    return o
 
 
-def solve_mixed(A, B, tier="tf32x3", tol=1e-13, max_iter=30):
-    """Returns (X, info dict)."""
+def _solve(kind, A, B, opt, allow_not_spd=False):
     lib = L.lib()
     info = RefineInfo()
+    dev_fn = lib.gbs_dgesv_mixed_device if kind == "ge" else lib.gbs_dposv_mixed_device
+    host_fn = lib.gbs_dgesv_mixed if kind == "ge" else lib.gbs_dposv_mixed
     if hasattr(A, "is_cuda") and A.is_cuda:
         import torch
         n = A.shape[0]
@@ -43,22 +61,32 @@ def solve_mixed(A, B, tier="tf32x3", tol=1e-13, max_iter=30):
         Bm = B.reshape(-1, 1) if vec else B
         nrhs = Bm.shape[1]
         X = torch.empty((nrhs, n), dtype=torch.float64, device=A.device).t()
-        lda = max(A.stride(1), 1) if A.stride(0) == 1 else None
-        ldb = max(Bm.stride(1), n, 1) if Bm.stride(0) == 1 else None
-        if lda is None or ldb is None:
+        if A.stride(0) != 1 or Bm.stride(0) != 1:
             raise ValueError("device matrices must be column-major")
-        L.check(lib.gbs_dgesv_mixed_device(n, nrhs, C.c_void_p(A.data_ptr()), lda, C.c_void_p(Bm.data_ptr()), ldb,
-                                           C.c_void_p(X.data_ptr()), max(n, 1), _tier(tier), tol, max_iter,
-                                           C.byref(info), C.c_void_p(torch.cuda.current_stream().cuda_stream)),
-                "gbs_dgesv_mixed_device")
-        return (X.reshape(-1) if vec else X), info.as_dict()
-    a = np.asfortranarray(A, dtype=np.float64)
-    b = np.asarray(B, dtype=np.float64)
-    vec = b.ndim == 1
-    bm = np.asfortranarray(b.reshape(-1, 1) if vec else b)
-    n, nrhs = a.shape[0], bm.shape[1]
-    x = np.empty((n, nrhs), dtype=np.float64, order="F")
-    L.check(lib.gbs_dgesv_mixed(n, nrhs, a.ctypes.data_as(C.c_void_p), max(n, 1), bm.ctypes.data_as(C.c_void_p),
-                                max(n, 1), x.ctypes.data_as(C.c_void_p), max(n, 1), _tier(tier), tol, max_iter,
-                                C.byref(info)), "gbs_dgesv_mixed")
-    return (x.reshape(-1) if vec else x), info.as_dict()
+        rc = dev_fn(n, nrhs, C.c_void_p(A.data_ptr()), max(A.stride(1), n, 1), C.c_void_p(Bm.data_ptr()),
+                    max(Bm.stride(1), n, 1), C.c_void_p(X.data_ptr()), max(n, 1), C.byref(opt), C.byref(info),
+                    C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        out = X.reshape(-1) if vec else X
+    else:
+        a = np.asfortranarray(A, dtype=np.float64)
+        b = np.asarray(B, dtype=np.float64)
+        vec = b.ndim == 1
+        bm = np.asfortranarray(b.reshape(-1, 1) if vec else b)
+        n, nrhs = a.shape[0], bm.shape[1]
+        x = np.empty((n, nrhs), dtype=np.float64, order="F")
+        rc = host_fn(n, nrhs, a.ctypes.data_as(C.c_void_p), max(n, 1), bm.ctypes.data_as(C.c_void_p), max(n, 1),
+                     x.ctypes.data_as(C.c_void_p), max(n, 1), C.byref(opt), C.byref(info))
+        out = x.reshape(-1) if vec else x
+    if not (allow_not_spd and rc == L.GBS_NUMERICAL_ISSUE):
+        L.check(rc, f"gbs_d{kind}sv_mixed")
+    return out, info.as_dict()
+
+
+def solve_mixed(A, B, tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", **kw):
+    """General A: returns (X, info dict)."""
+    return _solve("ge", A, B, options(tier, tol, max_iter, refine, **kw))
+
+
+def solve_spd_mixed(A, B, tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", allow_not_spd=False, **kw):
+    """SPD A (lower triangle read): returns (X, info dict)."""
+    return _solve("po", A, B, options(tier, tol, max_iter, refine, **kw), allow_not_spd)

@@ -205,36 +205,64 @@ int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, int64_t lda
                     float* d_c, int64_t ldc, int lower, void* stream);
 
 /* ------------------------------------------------------------------ mixed precision
- * A x = B for a general FP64 matrix, factored in a low precision on the tensor
- * cores and refined in FP64 until the normwise backward error
+ * A x = B for an FP64 matrix, factored in a low precision on the tensor cores
+ * and refined in FP64 until the normwise backward error
  * max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
- * The reference has no such path; it extends PartialPivLU::solve
- * (PartialPivLU.h:224-244) the way LAPACK's dsgesv extends dgesv.  When the
- * refinement stops improving (or needs more than max_iter steps) the plain
- * FP64 factorization (identical pivots to the reference) decides the result,
- * so the bound is met whenever the FP64 path meets it. */
+ * The reference has no such path; these extend PartialPivLU::solve
+ * (PartialPivLU.h:224-244) and LLT::solve (LLT.h:477-505) the way LAPACK's
+ * dsgesv / dsposv extend dgesv / dposv.  Refinement is classic (x += M^-1 r)
+ * or GMRES-IR (each correction solves M^-1 A d = M^-1 r by GMRES in FP64 with
+ * the low-precision factors applied in FP32).  When the refinement stops
+ * improving, needs more than max_iter steps, or the low-precision
+ * factorization breaks down, the plain FP64 factorization (the reference's
+ * pivots / failing column) decides the result. */
 typedef enum gbs_tier {
   GBS_TIER_FP64 = 0,     /* plain FP64 (no refinement) */
   GBS_TIER_TF32X3 = 1,   /* FP32-accurate factors: 3xTF32 tensor-core updates */
   GBS_TIER_TF32 = 2,     /* TF32 tensor-core updates */
   GBS_TIER_BF16 = 3,     /* BF16 tensor-core updates */
-  GBS_TIER_FP16 = 4      /* FP16 tensor-core updates */
+  GBS_TIER_FP16 = 4      /* FP16 tensor-core updates (SPD: on the unit-diagonal scaled matrix) */
 } gbs_tier;
+
+typedef enum gbs_refine_mode { GBS_REFINE_AUTO = 0, GBS_REFINE_CLASSIC = 1, GBS_REFINE_GMRES = 2 } gbs_refine_mode;
+
+typedef struct gbs_refine_options {
+  int tier;               /* gbs_tier */
+  int refine;             /* gbs_refine_mode; AUTO = classic for TF32X3, GMRES-IR otherwise */
+  double tol;             /* backward-error target (default 1e-13) */
+  int max_iter;           /* outer refinement steps before the FP64 fallback (default 30) */
+  int gmres_restart;      /* Krylov vectors per GMRES-IR correction (default 40) */
+  double gmres_tol;       /* relative target of one GMRES correction (default 1e-10) */
+  double shift_factor;    /* SPD tiers: diagonal shift = shift_factor * u of the tier (default 4) */
+} gbs_refine_options;
 
 typedef struct gbs_refine_info {
   int tier_used;          /* gbs_tier that produced X (GBS_TIER_FP64 after a fallback) */
-  int iterations;         /* refinement steps taken by the low-precision tier */
+  int solver;             /* gbs_refine_mode used */
+  int iterations;         /* outer refinement steps */
+  int inner_iterations;   /* GMRES iterations, summed over outer steps */
   int fell_back;          /* 1 when the FP64 factorization produced X */
-  int singular;           /* 1 when the FP64 factorization met an exactly-zero pivot */
+  int singular;           /* 1 when the FP64 factorization met a zero pivot (LU) / non-SPD column (LLT) */
   double backward_error;  /* normwise backward error of X, computed in FP64 */
+  double shift;           /* SPD tiers: diagonal shift used for the factorization */
 } gbs_refine_info;
 
-/* Device buffers, stream-ordered on `stream` (NULL: the library's own); returns after X is final. */
+void gbs_refine_options_default(gbs_refine_options* opt);
+
+/* General A (PartialPivLU).  Device buffers, stream-ordered on `stream`
+ * (NULL: the library's own); returns when X is final.  opt NULL: defaults. */
 int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
-                           int ldx, int tier, double tol, int max_iter, gbs_refine_info* info, void* stream);
+                           int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
 /* Host buffers (copied in and out inside the call). */
-int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx, int tier,
-                    double tol, int max_iter, gbs_refine_info* info);
+int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
+                    const gbs_refine_options* opt, gbs_refine_info* info);
+/* SPD A, lower triangle read (LLT<MatrixXd, Lower>).  Returns
+ * GBS_NUMERICAL_ISSUE (info->singular = 1) when A is not positive definite in
+ * FP64 either. */
+int gbs_dposv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
+                           int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
+int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
+                    const gbs_refine_options* opt, gbs_refine_info* info);
 
 /* ------------------------------------------------------------------ batched
  * Many small, uneven systems, one right-hand side each: LLT + solve for SPD

@@ -69,6 +69,51 @@ def test_singular_reports_it():
     assert info["fell_back"] and info["singular"]
 
 
+def spd_with_condition(n, kappa, seed):
+    """A = Q diag(sigma) Q^T, Q Haar-orthogonal (QR of a seeded Gaussian with
+    the signs of diag(R) fixed), sigma log-spaced from 1 to kappa."""
+    q, r = np.linalg.qr(O.gauss(seed, n, n))
+    q = q * np.sign(np.diag(r))
+    s = np.logspace(0, np.log10(kappa), n)
+    a = (q * s) @ q.T
+    return np.asfortranarray((a + a.T) / 2)
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
+@pytest.mark.parametrize("tier", ["tf32x3", "tf32", "bf16", "fp16"])
+def test_spd_mixed_tiers_meet_the_bar(tier, kappa):
+    from eigen_gb300 import solve_spd_mixed
+    n = 640
+    a = spd_with_condition(n, kappa, seed=int(np.log10(kappa)) + 17)
+    b = O.gauss(23, n, 4)
+    x, info = solve_spd_mixed(np.tril(a), b, tier=tier)
+    be = O.backward_error(a, x, b)
+    assert be <= BAR, (be, info)
+    if kappa <= 1e6:
+        # the refinement itself converges (no FP64 fallback) for moderate kappa
+        assert not info["fell_back"], info
+
+
+def test_spd_not_positive_definite_is_reported():
+    from eigen_gb300 import solve_spd_mixed
+    n = 200
+    a = -O.spd(3, n)
+    b = O.gauss(4, n, 1)
+    _, info = solve_spd_mixed(a, b, tier="bf16", allow_not_spd=True)
+    assert info["singular"] and info["fell_back"]
+
+
+@pytest.mark.parametrize("tier", ["tf32", "bf16", "fp16"])
+def test_gmres_ir_lets_low_tiers_converge_on_general_matrices(tier):
+    n = 1024
+    a = O.gauss(31, n, n)
+    b = O.gauss(32, n, 2)
+    x, info = solve_mixed(a, b, tier=tier, refine="gmres")
+    assert info["solver"] == "gmres"
+    assert O.backward_error(a, x, b) <= BAR
+    assert not info["fell_back"], info
+
+
 def test_mixed_device_buffers():
     torch = pytest.importorskip("torch")
     n = 1500
