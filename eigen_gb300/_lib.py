@@ -103,6 +103,26 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_batched_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "gbs_batched_autotune": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
     "gbs_batched_config": (c_int, [c_vp, c_ip, c_ip]),
+    # medium batches + router
+    "gbs_mbatch_create": (c_int, [C.POINTER(c_vp), c_i64, c_vp]),
+    "gbs_mbatch_destroy": (c_int, [c_vp]),
+    "gbs_mbatch_matrix_elements": (c_i64, [c_vp]),
+    "gbs_mbatch_vector_elements": (c_i64, [c_vp]),
+    "gbs_mbatch_offsets": (c_int, [c_vp, c_vp, c_vp]),
+    "gbs_mbatch_lu_rcond": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "gbs_mbatch_ir": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_vp, c_vp]),
+    "gbs_mbatch_features": (c_int, [c_vp, c_vp, c_vp, c_vp]),
+    "gbs_router_feature_count": (c_int, []),
+    "gbs_mlp_create": (c_int, [C.POINTER(c_vp), c_int, c_int, C.c_uint64]),
+    "gbs_mlp_destroy": (c_int, [c_vp]),
+    "gbs_mlp_param_count": (c_int, [c_vp]),
+    "gbs_mlp_get_params": (c_int, [c_vp, c_vp]),
+    "gbs_mlp_set_params": (c_int, [c_vp, c_vp]),
+    "gbs_mlp_gradients": (c_int, [c_vp, c_vp, c_vp, c_int, c_vp, c_dp]),
+    "gbs_mlp_train_step": (c_int, [c_vp, c_vp, c_vp, c_int, C.c_float, c_dp]),
+    "gbs_mlp_fit": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, C.c_float, C.c_uint64, c_dp]),
+    "gbs_mlp_predict": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp]),
+    "gbs_router_route": (c_int, [c_vp, c_int, C.c_float, c_vp, c_vp]),
     # tracing
     "gbs_kernel_launch_count": (C.c_uint64, []),
     "gbs_profile_enable": (c_int, [c_int]),

@@ -1,0 +1,517 @@
+// Batches of medium general systems (n <= 512): one CTA per matrix, matrix in
+// global memory (L2-resident while its CTA works on it).
+//
+//   mbatch_lu_rcond   FP64 PartialPivLU (first max wins, PartialPivLU.h:365-409)
+//                     + ||A||_1 + Hager/Higham rcond (ConditionEstimator.h:56-169)
+//                     + solve of one right-hand side: the plain FP64 tier and the
+//                     label generator of the precision router
+//   mbatch_ir         FP32 LU of a working copy + FP64 iterative refinement to the
+//                     backward-error bound; flags the items that did not reach it
+//   mbatch_features   router features: size, diagonal and row-norm statistics and
+//                     four power-iteration estimates of ||A||_2 / ||A||_F
+// Every item is independent; a CTA loops over items (grid-stride).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "dense_driver.cuh"
+#include "gbs_common.cuh"
+#include "gbs_profile.cuh"
+
+namespace gbs {
+namespace {
+
+constexpr int kMB = 256;          // threads per CTA
+constexpr int kMaxN = 512;
+
+struct MItem {
+  int64_t a_off;   // element offset of the n x n column-major matrix (ld = n)
+  int64_t v_off;   // element offset of its n-vectors (rhs / solution / pivots)
+  int n;
+  int pad;
+};
+
+template <typename T>
+__device__ T block_sum(T v, T* red)
+{
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = T(0);
+  for (int i = 0; i < kMB / 32; ++i) s += red[i];
+  return s;
+}
+
+template <typename T>
+__device__ T block_max(T v, T* red)
+{
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = red[0];
+  for (int i = 1; i < kMB / 32; ++i) s = red[i] > s ? red[i] : s;
+  return s;
+}
+
+// first maximum of score over the CTA (lowest index on ties)
+template <typename T>
+__device__ void block_argmax(T& s, int& i, T* rv, int* ri)
+{
+  warp_argmax(s, i);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) { rv[warp] = s; ri[warp] = i; }
+  __syncthreads();
+  s = rv[0];
+  i = ri[0];
+  for (int w = 1; w < kMB / 32; ++w)
+    if (better(rv[w], ri[w], s, i)) { s = rv[w]; i = ri[w]; }
+}
+
+// In-place partial-pivoting LU of a (n x n, ld n); pivots (0-based) to piv.
+// Returns the first exactly-zero pivot or -1 (same for every thread).
+template <typename T>
+__device__ int cta_getrf(T* a, int n, int* piv, T* rv, int* ri)
+{
+  int first_zero = -1;
+  for (int k = 0; k < n; ++k) {
+    T s = T(-2);
+    int idx = 0x7fffffff;
+    for (int i = k + threadIdx.x; i < n; i += kMB) {
+      const T x = a[(int64_t)k * n + i];
+      const T sc = (i == k) ? ((x != x) ? T(INFINITY) : gbs_abs(x)) : pivot_score(x);
+      if (better(sc, i, s, idx)) { s = sc; idx = i; }
+    }
+    block_argmax(s, idx, rv, ri);
+    const int p = idx;
+    const T pv = a[(int64_t)k * n + p];
+    __syncthreads();
+    if (threadIdx.x == 0) piv[k] = p;
+    if (pv != T(0)) {
+      if (p != k)
+        for (int c = threadIdx.x; c < n; c += kMB) {
+          const T t = a[(int64_t)c * n + k];
+          a[(int64_t)c * n + k] = a[(int64_t)c * n + p];
+          a[(int64_t)c * n + p] = t;
+        }
+      __syncthreads();
+      const T d = a[(int64_t)k * n + k];
+      for (int i = k + 1 + threadIdx.x; i < n; i += kMB) a[(int64_t)k * n + i] /= d;
+    } else if (first_zero < 0) {
+      first_zero = k;
+    }
+    __syncthreads();
+    // rank-1 update: warps over columns, lanes over rows (coalesced)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int j = k + 1 + wid; j < n; j += kMB / 32) {
+      const T u = a[(int64_t)j * n + k];
+      T* cj = a + (int64_t)j * n;
+      const T* ck = a + (int64_t)k * n;
+      for (int i = k + 1 + lane; i < n; i += 32) cj[i] = fma(-ck[i], u, cj[i]);
+    }
+    __syncthreads();
+  }
+  return first_zero;
+}
+
+// x <- A^-1 x (trans = 0) or A^-T x (trans = 1) with PA = LU in a; x in shared memory
+template <typename T>
+__device__ void cta_lu_solve(const T* a, int n, const int* piv, T* x, int trans)
+{
+  if (!trans) {
+    if (threadIdx.x == 0)
+      for (int k = 0; k < n; ++k) {
+        const int p = piv[k];
+        if (p != k) { const T t = x[k]; x[k] = x[p]; x[p] = t; }
+      }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {            // unit lower, column-oriented
+      const T xj = x[j];
+      for (int i = j + 1 + threadIdx.x; i < n; i += kMB) x[i] = fma(-a[(int64_t)j * n + i], xj, x[i]);
+      __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {       // upper
+      if (threadIdx.x == 0) x[j] = x[j] / a[(int64_t)j * n + j];
+      __syncthreads();
+      const T xj = x[j];
+      for (int i = threadIdx.x; i < j; i += kMB) x[i] = fma(-a[(int64_t)j * n + i], xj, x[i]);
+      __syncthreads();
+    }
+  } else {
+    for (int j = 0; j < n; ++j) {            // U^T y = b: forward, row j of U^T = column j of U
+      if (threadIdx.x == 0) x[j] = x[j] / a[(int64_t)j * n + j];
+      __syncthreads();
+      const T xj = x[j];
+      for (int i = j + 1 + threadIdx.x; i < n; i += kMB) x[i] = fma(-a[(int64_t)i * n + j], xj, x[i]);
+      __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {       // L^T z = y: backward, unit
+      const T xj = x[j];
+      for (int i = threadIdx.x; i < j; i += kMB) x[i] = fma(-a[(int64_t)i * n + j], xj, x[i]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0)
+      for (int k = n - 1; k >= 0; --k) {
+        const int p = piv[k];
+        if (p != k) { const T t = x[k]; x[k] = x[p]; x[p] = t; }
+      }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kMB)
+mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __restrict__ A, int* __restrict__ piv,
+                       double* __restrict__ rhs, double* __restrict__ rcond, int* __restrict__ info)
+{
+  __shared__ double x[kMaxN], sgn[kMaxN], osgn[kMaxN];
+  __shared__ double rv[kMB / 32];
+  __shared__ int ri[kMB / 32];
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    const MItem m = items[it];
+    const int n = m.n;
+    double* a = A + m.a_off;
+    int* pv = piv + m.v_off;
+    // ||A||_1
+    double best = 0.0;
+    for (int c = threadIdx.x >> 5; c < n; c += kMB / 32) {
+      double s = 0.0;
+      for (int i = threadIdx.x & 31; i < n; i += 32) s += fabs(a[(int64_t)c * n + i]);
+      s = warp_sum(s);
+      best = s > best ? s : best;
+    }
+    const double anorm = block_max(best, rv);
+    const int fz = cta_getrf(a, n, pv, rv, ri);
+    if (threadIdx.x == 0) info[it] = fz;
+    // solve the right-hand side
+    if (rhs) {
+      for (int i = threadIdx.x; i < n; i += kMB) x[i] = rhs[m.v_off + i];
+      __syncthreads();
+      cta_lu_solve(a, n, pv, x, 0);
+      for (int i = threadIdx.x; i < n; i += kMB) rhs[m.v_off + i] = x[i];
+      __syncthreads();
+    }
+    // rcond (ConditionEstimator.h:56-169)
+    double rc;
+    if (n == 0) rc = 1.0;
+    else if (anorm == 0.0) rc = 0.0;
+    else if (n == 1) rc = 1.0;
+    else {
+      for (int i = threadIdx.x; i < n; i += kMB) x[i] = 1.0 / n;
+      __syncthreads();
+      cta_lu_solve(a, n, pv, x, 0);
+      double lb = block_sum([&] { double s = 0; for (int i = threadIdx.x; i < n; i += kMB) s += fabs(x[i]); return s; }(), rv);
+      double old_lb = lb;
+      int old_v = -1;
+      for (int k = 0; k < 4; ++k) {
+        int same = 1;
+        for (int i = threadIdx.x; i < n; i += kMB) {
+          const double sg = x[i] < 0 ? -1.0 : 1.0;
+          if (k > 0 && sg != osgn[i]) same = 0;
+          sgn[i] = sg;
+        }
+        same = __syncthreads_and(same);
+        if (k > 0 && same) break;
+        for (int i = threadIdx.x; i < n; i += kMB) x[i] = sgn[i];
+        __syncthreads();
+        cta_lu_solve(a, n, pv, x, 1);
+        double s = -1.0;
+        int vi = 0x7fffffff;
+        for (int i = threadIdx.x; i < n; i += kMB) {
+          const double t = fabs(x[i]);
+          if (better(t, i, s, vi)) { s = t; vi = i; }
+        }
+        block_argmax(s, vi, rv, ri);
+        if (vi == old_v) break;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += kMB) x[i] = i == vi ? 1.0 : 0.0;
+        __syncthreads();
+        cta_lu_solve(a, n, pv, x, 0);
+        lb = block_sum([&] { double t = 0; for (int i = threadIdx.x; i < n; i += kMB) t += fabs(x[i]); return t; }(), rv);
+        if (lb <= old_lb) break;
+        for (int i = threadIdx.x; i < n; i += kMB) osgn[i] = sgn[i];
+        old_v = vi;
+        old_lb = lb;
+        __syncthreads();
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += kMB) x[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (double)i / (double)(n - 1));
+      __syncthreads();
+      cta_lu_solve(a, n, pv, x, 0);
+      const double alt =
+          2.0 * block_sum([&] { double t = 0; for (int i = threadIdx.x; i < n; i += kMB) t += fabs(x[i]); return t; }(), rv) /
+          (3.0 * n);
+      const double est = lb > alt ? lb : alt;
+      rc = est == 0.0 ? 0.0 : (1.0 / est) / anorm;
+    }
+    if (threadIdx.x == 0) rcond[it] = rc;
+    __syncthreads();
+  }
+}
+
+// FP32 LU + FP64 refinement.  W: FP32 working copies (same layout as A).
+// status[it] = refinement steps taken (>= 0) when the backward error reached
+// tol, -1 when it did not (the caller re-solves those in FP64).
+__global__ void __launch_bounds__(kMB)
+mbatch_ir_kernel(const MItem* __restrict__ items, int count, const double* __restrict__ A, float* __restrict__ W,
+                 int* __restrict__ piv, const double* __restrict__ rhs, double* __restrict__ X, double tol, int max_iter,
+                 int* __restrict__ status)
+{
+  __shared__ double x[kMaxN], r[kMaxN];
+  __shared__ float d[kMaxN];
+  __shared__ float rv[kMB / 32];
+  __shared__ int ri[kMB / 32];
+  __shared__ double rvd[kMB / 32];
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    const MItem m = items[it];
+    const int n = m.n;
+    const double* a = A + m.a_off;
+    float* w = W + m.a_off;
+    int* pv = piv + m.v_off;
+    for (int e = threadIdx.x; e < n * n; e += kMB) w[e] = (float)a[e];
+    __syncthreads();
+    // ||A||_inf
+    double rmax = 0.0;
+    for (int i = threadIdx.x; i < n; i += kMB) {
+      double s = 0.0;
+      for (int j = 0; j < n; ++j) s += fabs(a[(int64_t)j * n + i]);
+      rmax = s > rmax ? s : rmax;
+    }
+    const double anorm = block_max(rmax, rvd);
+    const int fz = cta_getrf(w, n, pv, rv, ri);
+    int result = -1;
+    if (fz < 0) {
+      double bmax = 0.0;
+      for (int i = threadIdx.x; i < n; i += kMB) { x[i] = 0.0; r[i] = rhs[m.v_off + i]; bmax = fmax(bmax, fabs(r[i])); }
+      bmax = block_max(bmax, rvd);
+      for (int step = 0; step <= max_iter; ++step) {
+        // correction d = LU^-1 (r / s) in FP32, x += s d
+        double rm = 0.0;
+        for (int i = threadIdx.x; i < n; i += kMB) rm = fmax(rm, fabs(r[i]));
+        rm = block_max(rm, rvd);
+        const double sc = rm > 0 ? rm : 1.0;
+        for (int i = threadIdx.x; i < n; i += kMB) d[i] = (float)(r[i] / sc);
+        __syncthreads();
+        cta_lu_solve(w, n, pv, d, 0);
+        for (int i = threadIdx.x; i < n; i += kMB) x[i] += sc * (double)d[i];
+        __syncthreads();
+        // r = b - A x (FP64), backward error
+        double rn = 0.0, xn = 0.0;
+        for (int i = threadIdx.x; i < n; i += kMB) {
+          double s = rhs[m.v_off + i];
+          for (int j = 0; j < n; ++j) s = fma(-a[(int64_t)j * n + i], x[j], s);
+          r[i] = s;
+          rn = fmax(rn, fabs(s));
+          xn = fmax(xn, fabs(x[i]));
+        }
+        rn = block_max(rn, rvd);
+        xn = block_max(xn, rvd);
+        const double den = anorm * xn + bmax;
+        const double be = den > 0 ? rn / den : rn;
+        if (be <= tol) { result = step; break; }
+        if (!(be == be)) break;
+      }
+      for (int i = threadIdx.x; i < n; i += kMB) X[m.v_off + i] = x[i];
+    }
+    if (threadIdx.x == 0) status[it] = result;
+    __syncthreads();
+  }
+}
+
+// Router features (kFeat floats per matrix, scale invariant):
+//  0 log2(n)/9           1 ||diag||_2/||A||_F       2 min|a_ii|/mean|a_ii|   3 max|a_ii|/mean|a_ii|
+//  4 min row norm/mean   5 max row norm/mean        6 std row norm/mean
+//  7..10 power-iteration estimates rho_k = ||A^T A x_k||^(1/2) / ||A||_F, x_{k+1} = A^T A x_k / ||.||
+//  11..13 log of rho_{k+1}/rho_k (convergence rate of the power iteration)   14 1.0 (bias)  15 0
+constexpr int kFeat = 16;
+
+__global__ void __launch_bounds__(kMB)
+mbatch_features_kernel(const MItem* __restrict__ items, int count, const double* __restrict__ A, float* __restrict__ F)
+{
+  __shared__ float x[kMaxN], y[kMaxN];
+  __shared__ float rv[kMB / 32];
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    const MItem m = items[it];
+    const int n = m.n;
+    const double* a = A + m.a_off;
+    // FP32 arithmetic: the features are estimates, and FP64 here would cost more
+    // than the low-precision attempt the router is meant to save
+    float fro = 0.f, dsq = 0.f, dmin = INFINITY, dmax = 0.f, dsum = 0.f, rmin = INFINITY, rmax = 0.f, rsum = 0.f,
+          rsq = 0.f;
+    for (int i = threadIdx.x; i < n; i += kMB) {
+      float rs = 0.f;
+      for (int j = 0; j < n; ++j) { const float v = (float)a[(int64_t)j * n + i]; rs = fmaf(v, v, rs); }
+      const float dv = fabsf((float)a[(int64_t)i * n + i]);
+      fro += rs;
+      dsq += dv * dv;
+      dmin = fmin(dmin, dv); dmax = fmax(dmax, dv); dsum += dv;
+      const float rn = sqrtf(rs);
+      rmin = fmin(rmin, rn); rmax = fmax(rmax, rn); rsum += rn; rsq += rn * rn;
+    }
+    fro = block_sum(fro, rv);
+    dsq = block_sum(dsq, rv);
+    dsum = block_sum(dsum, rv);
+    rsum = block_sum(rsum, rv);
+    rsq = block_sum(rsq, rv);
+    dmax = block_max(dmax, rv);
+    rmax = block_max(rmax, rv);
+    dmin = -block_max(-dmin, rv);
+    rmin = -block_max(-rmin, rv);
+    const float fnorm = sqrtf(fro) > 0 ? sqrtf(fro) : 1.f;
+    const float dmean = dsum / n > 0 ? dsum / n : 1.f, rmean = rsum / n > 0 ? rsum / n : 1.f;
+    const float rstd = sqrtf(fmaxf(rsq / n - rmean * rmean, 0.f));
+    // power iteration on A^T A from a fixed start vector
+    for (int i = threadIdx.x; i < n; i += kMB) x[i] = rsqrtf((float)n) * ((i % 3) ? 1.f : -1.f);
+    __syncthreads();
+    float rho[4];
+    for (int k = 0; k < 4; ++k) {
+      for (int i = threadIdx.x; i < n; i += kMB) {
+        float s = 0.f;
+        for (int j = 0; j < n; ++j) s = fmaf((float)a[(int64_t)j * n + i], x[j], s);
+        y[i] = s;
+      }
+      __syncthreads();
+      float nn = 0.f;
+      for (int j = threadIdx.x; j < n; j += kMB) {
+        float s = 0.f;
+        for (int i = 0; i < n; ++i) s = fmaf((float)a[(int64_t)j * n + i], y[i], s);
+        x[j] = s;
+        nn = fmaf(s, s, nn);
+      }
+      nn = sqrtf(block_sum(nn, rv));
+      rho[k] = sqrtf(nn) / fnorm;
+      const float inv = nn > 0 ? 1.f / nn : 0.f;
+      for (int j = threadIdx.x; j < n; j += kMB) x[j] *= inv;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      float* f = F + (int64_t)it * kFeat;
+      f[0] = (float)(log2((double)n) / 9.0);
+      f[1] = (float)(sqrt(dsq) / fnorm);
+      f[2] = (float)(dmin / dmean);
+      f[3] = (float)(dmax / dmean);
+      f[4] = (float)(rmin / rmean);
+      f[5] = (float)(rmax / rmean);
+      f[6] = (float)(rstd / rmean);
+      for (int k = 0; k < 4; ++k) f[7 + k] = (float)rho[k];
+      for (int k = 0; k < 3; ++k) f[11 + k] = (rho[k] > 0 ? 10.f * logf(rho[k + 1] / rho[k]) : 0.f);
+      f[14] = 1.0f;
+      f[15] = 0.0f;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+struct gbs_mbatch {
+  int64_t count = 0;
+  std::vector<int> sizes;
+  std::vector<int64_t> a_off, v_off;
+  int64_t total_a = 0, total_v = 0;
+  DevBuf items;
+};
+
+static int mb_grid(int64_t count) { return (int)std::min<int64_t>(count, 8LL * device_sm_count()); }
+
+extern "C" int gbs_mbatch_create(gbs_mbatch** out, int64_t count, const int* sizes)
+{
+  if (!out || count < 0 || (count > 0 && !sizes)) return GBS_INVALID_ARGUMENT;
+  *out = nullptr;
+  GBS_TRY(ensure_device());
+  gbs_mbatch* p = new gbs_mbatch();
+  p->count = count;
+  p->sizes.assign(sizes, sizes + count);
+  p->a_off.resize((size_t)count);
+  p->v_off.resize((size_t)count);
+  std::vector<MItem> items((size_t)count);
+  int64_t ao = 0, vo = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const int n = sizes[i];
+    if (n < 1 || n > kMaxN) {
+      delete p;
+      gbs_set_last_message("gbs_mbatch_create: sizes must be in [1, 512]");
+      return GBS_INVALID_ARGUMENT;
+    }
+    items[(size_t)i] = MItem{ao, vo, n, 0};
+    p->a_off[(size_t)i] = ao;
+    p->v_off[(size_t)i] = vo;
+    ao += (int64_t)n * n;
+    vo += n;
+  }
+  p->total_a = ao;
+  p->total_v = vo;
+  int rc = p->items.reserve(sizeof(MItem) * (size_t)std::max<int64_t>(count, 1));
+  if (rc == GBS_SUCCESS && count > 0 &&
+      cudaMemcpy(p->items.p, items.data(), sizeof(MItem) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = GBS_CUDA_ERROR;
+  if (rc != GBS_SUCCESS) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_destroy(gbs_mbatch* p)
+{
+  delete p;
+  return GBS_SUCCESS;
+}
+
+extern "C" int64_t gbs_mbatch_matrix_elements(const gbs_mbatch* p) { return p ? p->total_a : 0; }
+extern "C" int64_t gbs_mbatch_vector_elements(const gbs_mbatch* p) { return p ? p->total_v : 0; }
+
+extern "C" int gbs_mbatch_offsets(const gbs_mbatch* p, int64_t* a_off, int64_t* v_off)
+{
+  if (!p) return GBS_INVALID_ARGUMENT;
+  if (a_off) std::copy(p->a_off.begin(), p->a_off.end(), a_off);
+  if (v_off) std::copy(p->v_off.begin(), p->v_off.end(), v_off);
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_lu_rcond(gbs_mbatch* p, double* d_a, int* d_piv, double* d_rhs, double* d_rcond, int* d_info,
+                                   void* stream)
+{
+  if (!p || (p->count > 0 && (!d_a || !d_piv || !d_rcond || !d_info))) return GBS_INVALID_ARGUMENT;
+  if (p->count == 0) return GBS_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+  mbatch_lu_rcond_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_piv, d_rhs,
+                                                          d_rcond, d_info);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const double* d_a, float* d_work, int* d_piv, const double* d_rhs,
+                             double* d_x, double tol, int max_iter, int* d_status, void* stream)
+{
+  if (!p || (p->count > 0 && (!d_a || !d_work || !d_piv || !d_rhs || !d_x || !d_status)) || max_iter < 0)
+    return GBS_INVALID_ARGUMENT;
+  if (p->count == 0) return GBS_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+  mbatch_ir_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_work, d_piv, d_rhs,
+                                                    d_x, tol, max_iter, d_status);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_features(gbs_mbatch* p, const double* d_a, float* d_feat, void* stream)
+{
+  if (!p || (p->count > 0 && (!d_a || !d_feat))) return GBS_INVALID_ARGUMENT;
+  if (p->count == 0) return GBS_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  PhaseScope ps(s, PH_ROUTER, 0.0, 0.0);
+  mbatch_features_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_feat);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_router_feature_count(void) { return kFeat; }

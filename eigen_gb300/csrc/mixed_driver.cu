@@ -34,25 +34,28 @@ static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 // ------------------------------------------------------------------ kernels
 // Y = A X (B == null) or R = B - A X, FP64.  Grid (row blocks of 128, K
-// splits); a thread owns one row and up to 16 right-hand sides; the K-chunk
-// of X is staged in shared memory.  Partial sums per split are added in split
-// order by residual_reduce (deterministic).
+// splits); a thread owns one row and RC right-hand sides (RC = 4, 8 or 16,
+// the smallest that covers nrhs, so no FMA is spent on absent columns); the
+// K-chunk of X is staged in shared memory.  A is read column by column,
+// coalesced over rows.  Partial sums per split are added in split order by
+// residual_reduce (deterministic).
 constexpr int kResRows = 128, kResRC = 16, kResKC = 64;
 
+template <int RC>
 __global__ void __launch_bounds__(kResRows)
-residual_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t lda, const double* __restrict__ X,
-                        int64_t ldx, int kspan, double* __restrict__ part)
+mv_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t lda, const double* __restrict__ X,
+                  int64_t ldx, int kspan, double* __restrict__ part)
 {
-  __shared__ double sx[kResKC][kResRC];
+  __shared__ double sx[kResKC][RC];
   const int row = blockIdx.x * kResRows + threadIdx.x;
   const int split = blockIdx.y;
   const int k0 = split * kspan, k1 = min(n, k0 + kspan);
-  double acc[kResRC];
+  double acc[RC];
 #pragma unroll
-  for (int c = 0; c < kResRC; ++c) acc[c] = 0.0;
+  for (int c = 0; c < RC; ++c) acc[c] = 0.0;
   for (int kc = k0; kc < k1; kc += kResKC) {
     __syncthreads();
-    for (int e = threadIdx.x; e < kResKC * kResRC; e += kResRows) {
+    for (int e = threadIdx.x; e < kResKC * RC; e += kResRows) {
       const int kk = e % kResKC, c = e / kResKC;
       sx[kk][c] = (kc + kk < k1 && c < nrhs) ? X[(int64_t)c * ldx + kc + kk] : 0.0;
     }
@@ -60,50 +63,41 @@ residual_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t l
     if (row < n) {
       const int kend = min(kResKC, k1 - kc);
       const double* ap = A + (int64_t)kc * lda + row;
+#pragma unroll 4
       for (int kk = 0; kk < kend; ++kk) {
         const double a = ap[(int64_t)kk * lda];
 #pragma unroll
-        for (int c = 0; c < kResRC; ++c) acc[c] = fma(a, sx[kk][c], acc[c]);
+        for (int c = 0; c < RC; ++c) acc[c] = fma(a, sx[kk][c], acc[c]);
       }
     }
   }
   if (row < n) {
-    for (int c = 0; c < nrhs; ++c) part[((int64_t)split * nrhs + c) * n + row] = acc[c];
+    for (int c = 0; c < nrhs && c < RC; ++c) part[((int64_t)split * nrhs + c) * n + row] = acc[c];
   }
 }
 
-// Symmetric A stored in the lower triangle: the same product with
-// A(i,k) = A(k,i) read from the lower part (k > i).
-__global__ void __launch_bounds__(kResRows)
-symv_partial_kernel(int n, int nrhs, const double* __restrict__ A, int64_t lda, const double* __restrict__ X,
-                    int64_t ldx, int kspan, double* __restrict__ part)
+// Full symmetric copy of the lower triangle: F(i,j) = A(max,min), by 32x32
+// tiles through shared memory so both the read and the write are coalesced.
+__global__ void symmetrize_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restrict__ F)
 {
-  __shared__ double sx[kResKC][kResRC];
-  const int row = blockIdx.x * kResRows + threadIdx.x;
-  const int split = blockIdx.y;
-  const int k0 = split * kspan, k1 = min(n, k0 + kspan);
-  double acc[kResRC];
-#pragma unroll
-  for (int c = 0; c < kResRC; ++c) acc[c] = 0.0;
-  for (int kc = k0; kc < k1; kc += kResKC) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < kResKC * kResRC; e += kResRows) {
-      const int kk = e % kResKC, c = e / kResKC;
-      sx[kk][c] = (kc + kk < k1 && c < nrhs) ? X[(int64_t)c * ldx + kc + kk] : 0.0;
+  __shared__ double t[32][33];
+  const int bi = blockIdx.x * 32, bj = blockIdx.y * 32;
+  if (bi < bj) {
+    // upper tile (bi, bj): transpose of the lower tile (bj, bi)
+    for (int y = threadIdx.y; y < 32; y += 8) {
+      const int r = bj + threadIdx.x, c = bi + y;
+      t[y][threadIdx.x] = (r < n && c < n) ? A[(int64_t)c * lda + r] : 0.0;
     }
     __syncthreads();
-    if (row < n) {
-      const int kend = min(kResKC, k1 - kc);
-      for (int kk = 0; kk < kend; ++kk) {
-        const int col = kc + kk;
-        const double a = col <= row ? A[(int64_t)col * lda + row] : A[(int64_t)row * lda + col];
-#pragma unroll
-        for (int c = 0; c < kResRC; ++c) acc[c] = fma(a, sx[kk][c], acc[c]);
-      }
+    for (int y = threadIdx.y; y < 32; y += 8) {
+      const int r = bi + threadIdx.x, c = bj + y;
+      if (r < n && c < n) F[(int64_t)c * n + r] = t[threadIdx.x][y];
     }
-  }
-  if (row < n) {
-    for (int c = 0; c < nrhs; ++c) part[((int64_t)split * nrhs + c) * n + row] = acc[c];
+  } else {
+    for (int y = threadIdx.y; y < 32; y += 8) {
+      const int r = bi + threadIdx.x, c = bj + y;
+      if (r < n && c < n) F[(int64_t)c * n + r] = r >= c ? A[(int64_t)c * lda + r] : A[(int64_t)r * lda + c];
+    }
   }
 }
 
@@ -191,20 +185,25 @@ __global__ void diag_scale_f32_kernel(int n, int nrhs, const float* __restrict__
 
 // As32(i,j) = fp32(d_i a_ij d_j) (+ sigma on the diagonal), lower triangle;
 // d_i = 1 / sqrt(a_ii).  Also writes d in FP32.
+__global__ void spd_diag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restrict__ d64,
+                                float* __restrict__ d32)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = 1.0 / sqrt(A[(int64_t)i * lda + i]);
+  d64[i] = d;
+  d32[i] = (float)d;
+}
+
 __global__ void scale_spd_kernel(int n, const double* __restrict__ A, int64_t lda, double sigma,
-                                 float* __restrict__ As, float* __restrict__ d32)
+                                 const double* __restrict__ d64, float* __restrict__ As)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * n) return;
   const int i = (int)(t % n), j = (int)(t / n);
   if (i < j) return;
-  const double di = 1.0 / sqrt(A[(int64_t)i * lda + i]);
-  const double dj = 1.0 / sqrt(A[(int64_t)j * lda + j]);
-  double v = di * A[(int64_t)j * lda + i] * dj;
-  if (i == j) {
-    v += sigma;
-    d32[i] = (float)di;
-  }
+  double v = d64[i] * A[(int64_t)j * lda + i] * d64[j];
+  if (i == j) v += sigma;
   As[(int64_t)j * n + i] = (float)v;
 }
 
@@ -253,7 +252,7 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
 // ------------------------------------------------------------------ workspace pool
 struct MixedWork {
   cudaStream_t stream = nullptr;
-  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, z, v, w, coef;
+  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef;
   SolveWork sw;
   TcWorkspace tc;
   HostBuf hstats;
@@ -412,12 +411,10 @@ static int apply_a(cudaStream_t s, const Problem& P, const double* X, int64_t ld
   GBS_TRY(w.part.reserve(sizeof(double) * (size_t)used * n * nrhs));
   {
     PhaseScope ps(s, PH_RESIDUAL, 2.0 * n * (double)n * nrhs, 8.0 * ((double)n * n + 2.0 * n * nrhs));
-    if (P.sym)
-      symv_partial_kernel<<<dim3(cdiv(n, kResRows), used), kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan,
-                                                                             w.part.as<double>());
-    else
-      residual_partial_kernel<<<dim3(cdiv(n, kResRows), used), kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan,
-                                                                                 w.part.as<double>());
+    const dim3 grid(cdiv(n, kResRows), used);
+    if (nrhs <= 4) mv_partial_kernel<4><<<grid, kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan, w.part.as<double>());
+    else if (nrhs <= 8) mv_partial_kernel<8><<<grid, kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan, w.part.as<double>());
+    else mv_partial_kernel<16><<<grid, kResRows, 0, s>>>(n, nrhs, P.A, P.lda, X, ldx, kspan, w.part.as<double>());
     GBS_CUDA_TRY(cudaGetLastError());
   }
   count_launch();
@@ -757,8 +754,18 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
   GBS_TRY(reserve_common(w, n, nrhs));
   GBS_TRY(w.a32.reserve(sizeof(float) * (size_t)n * n));
   GBS_TRY(w.d32.reserve(sizeof(float) * (size_t)n));
+  GBS_TRY(w.d64.reserve(sizeof(double) * (size_t)n));
+  GBS_TRY(w.afull.reserve(sizeof(double) * (size_t)n * n));
   DeviceStatus* st = w.st.as<DeviceStatus>();
-  Problem P{n, nrhs, A, lda, 1, B, ldb, X, ldx};
+  // the residuals read a full symmetric copy (coalesced, general kernel)
+  {
+    PhaseScope ps(s, PH_COPY, 0.0, 16.0 * (double)n * n);
+    symmetrize_kernel<<<dim3(cdiv(n, 32), cdiv(n, 32)), dim3(32, 8), 0, s>>>(n, A, lda, w.afull.as<double>());
+    spd_diag_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, A, lda, w.d64.as<double>(), w.d32.as<float>());
+    GBS_CUDA_TRY(cudaGetLastError());
+    count_launch();
+  }
+  Problem P{n, nrhs, w.afull.as<double>(), n, 0, B, ldb, X, ldx};
   double anorm = 0;
   GBS_TRY(inf_norm(s, P, w, &anorm));
   bool converged = false;
@@ -773,8 +780,8 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
       GBS_TRY(reset_status(st, s));
       {
         PhaseScope ps(s, PH_COPY, 0.0, 12.0 * (double)n * n);
-        scale_spd_kernel<<<cdiv((int64_t)n * n, 256), 256, 0, s>>>(n, A, lda, sigma, w.a32.as<float>(),
-                                                                   w.d32.as<float>());
+        scale_spd_kernel<<<cdiv((int64_t)n * n, 256), 256, 0, s>>>(n, A, lda, sigma, w.d64.as<double>(),
+                                                                   w.a32.as<float>());
         GBS_CUDA_TRY(cudaGetLastError());
       }
       GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc));

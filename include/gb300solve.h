@@ -298,6 +298,53 @@ int gbs_batched_solve(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int*
 int gbs_batched_autotune(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, int persist);
 int gbs_batched_config(const gbs_batched* plan, int* warps_small, int* warps_large);
 
+/* ------------------------------------------------------------------ medium batches + precision router
+ * Batches of general systems with n in [1, 512], one CTA per matrix, packed
+ * back to back like gbs_batched (matrix i at sum_{j<i} n_j^2, vectors at
+ * sum_{j<i} n_j).  No counterpart in the reference, which factors one matrix
+ * per PartialPivLU object; each item reproduces PartialPivLU (pivots:
+ * PartialPivLU.h:365-409), its solve and rcond() (ConditionEstimator.h:56-169).
+ *   gbs_mbatch_lu_rcond  FP64 LU in place, 0-based pivots, solve of d_rhs in
+ *                        place (may be NULL), rcond per item, info = first zero
+ *                        pivot or -1
+ *   gbs_mbatch_ir        FP32 LU of a working copy (d_work: matrix-sized FP32
+ *                        scratch) + FP64 refinement of x to backward error
+ *                        <= tol; status = refinement steps, or -1 when the bound
+ *                        was not reached (solve those items in FP64)
+ *   gbs_mbatch_features  gbs_router_feature_count() floats per item: size,
+ *                        diagonal and row-norm statistics, four power-iteration
+ *                        estimates of ||A||_2 / ||A||_F and their ratios
+ * The router network is a 3-layer MLP (in -> 64 -> 64 -> 1, ReLU) trained on
+ * the GPU by its own kernels (Adam on the mean squared error of the predicted
+ * log10 condition number against rcond-derived labels); gbs_router_route maps
+ * predictions to tiers: 1 = FP32 + refinement, 0 = FP64. */
+typedef struct gbs_mbatch gbs_mbatch;
+int gbs_mbatch_create(gbs_mbatch** out, int64_t count, const int* sizes);
+int gbs_mbatch_destroy(gbs_mbatch* plan);
+int64_t gbs_mbatch_matrix_elements(const gbs_mbatch* plan);
+int64_t gbs_mbatch_vector_elements(const gbs_mbatch* plan);
+int gbs_mbatch_offsets(const gbs_mbatch* plan, int64_t* a_offsets, int64_t* v_offsets);
+int gbs_mbatch_lu_rcond(gbs_mbatch* plan, double* d_a, int* d_piv, double* d_rhs, double* d_rcond, int* d_info,
+                        void* stream);
+int gbs_mbatch_ir(gbs_mbatch* plan, const double* d_a, float* d_work, int* d_piv, const double* d_rhs, double* d_x,
+                  double tol, int max_iter, int* d_status, void* stream);
+int gbs_mbatch_features(gbs_mbatch* plan, const double* d_a, float* d_features, void* stream);
+int gbs_router_feature_count(void);
+
+typedef struct gbs_mlp gbs_mlp;
+int gbs_mlp_create(gbs_mlp** out, int in_dim, int width, uint64_t seed);   /* width must be 64, in_dim <= 16 */
+int gbs_mlp_destroy(gbs_mlp* mlp);
+int gbs_mlp_param_count(const gbs_mlp* mlp);
+int gbs_mlp_get_params(const gbs_mlp* mlp, float* host_params);
+int gbs_mlp_set_params(gbs_mlp* mlp, const float* host_params);           /* also resets Adam state */
+/* Gradient of mean((y - t)^2) over `count` samples (device X: count x in_dim row-major, T: count). */
+int gbs_mlp_gradients(gbs_mlp* mlp, const float* d_x, const float* d_t, int count, float* host_grad, double* loss);
+int gbs_mlp_train_step(gbs_mlp* mlp, const float* d_x, const float* d_t, int count, float lr, double* loss);
+int gbs_mlp_fit(gbs_mlp* mlp, const float* d_x, const float* d_t, int count, int epochs, int batch, float lr,
+                uint64_t seed, double* final_loss);
+int gbs_mlp_predict(const gbs_mlp* mlp, const float* d_x, int count, float* d_y, void* stream);
+int gbs_router_route(const float* d_pred, int count, float threshold, int* d_tier, void* stream);
+
 /* ------------------------------------------------------------------ tracing
  * The reference has no runtime tracing (bench/BenchTimer.h times whole calls
  * from the host).  Here every kernel launch is counted, and when profiling is
