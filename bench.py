@@ -66,6 +66,11 @@ def args_parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
                    help="factor one seeded n x n system on the chosen path and exit (small ncu captures)")
+    p.add_argument("--config", default="lu8192", choices=["lu8192", "llt16384", "batched", "router", "mbatch"],
+                   help="lu8192 is the headline workload; the others are the LLT kappa sweep, the batched "
+                        "small systems and the learned router")
+    p.add_argument("--train-labels", type=int, default=200000, help="router: training systems (rcond labels)")
+    p.add_argument("--count", type=int, default=20000, help="mbatch: systems of the router workload (n 32..512)")
     return p.parse_args()
 
 
@@ -425,10 +430,251 @@ def factor_once(args):
     return 0 if ok else 1
 
 
+def _event_time(fn, reps=1):
+    import torch
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    out = None
+    for _ in range(reps):
+        out = fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return out, e0.elapsed_time(e1) / 1e3 / reps
+
+
+def run_llt16384(args):
+    """LLT n = 16384, A = Q diag(sigma) Q^T (Haar Q, sigma log-spaced 1..kappa),
+    4 right-hand sides, kappa in {1e2, 1e6, 1e10}: every tier's solves/s at
+    backward error <= 1e-13 and its forward error against the FP64 solution."""
+    import numpy as np
+    import torch
+
+    import eigen_gb300 as gb
+    n, nrhs = 16384 if args.n == 8192 else args.n, 4
+    g = torch.Generator(device="cuda").manual_seed(7)
+    G = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    Q, Rq = torch.linalg.qr(G)
+    Q = Q * torch.sign(torch.diagonal(Rq))
+    del G, Rq
+    B = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=g).t()
+    flops = n ** 3 / 3.0 + 2.0 * n * n * nrhs
+    per_kappa = {}
+    best = None
+    for kappa in (1e2, 1e6, 1e10):
+        s = torch.logspace(0, float(np.log10(kappa)), n, dtype=torch.float64, device="cuda")
+        A = (Q * s) @ Q.t()
+        A = ((A + A.t()) / 2).contiguous().t()
+        x64, _ = gb.solve_spd_mixed(A, B, tier="fp64")
+        rows = {}
+        for tier in ("fp64", "tf32x3", "fp16", "bf16"):
+            gb.solve_spd_mixed(A, B, tier=tier)
+            (X, info), dt = _event_time(lambda: gb.solve_spd_mixed(A, B, tier=tier))
+            be = backward_error_gpu(A, X, B)
+            fe = float(((X - x64).abs().amax(0) / x64.abs().amax(0)).max().item())
+            rows[tier] = {"solves_per_s": 1.0 / dt if be <= BE_BAR else 0.0, "ms": 1e3 * dt,
+                          "tflops": flops / dt / 1e12, "backward_error": be, "forward_error_vs_fp64": fe,
+                          "refine": info}
+        fastest = max(rows, key=lambda t: rows[t]["solves_per_s"])
+        per_kappa[f"{kappa:.0e}"] = {"tiers": rows, "fastest": fastest,
+                                     "speedup_vs_fp64": rows[fastest]["solves_per_s"] / rows["fp64"]["solves_per_s"]}
+        if kappa == 1e2:
+            best = rows[fastest]
+        del A
+    line = {"metric": METRIC, "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": best["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: A = Q diag(sigma) Q^T, Q Haar (QR of seeded Gaussian), B iid N(0,1)",
+            "config": {"workload": f"LLT<MatrixXd> n={n}, {nrhs} RHS, kappa sweep (value: kappa=1e2, fastest tier)",
+                       "n": n, "nrhs": nrhs}, "per_kappa": per_kappa}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batched(args):
+    """100,000 SPD systems n ~ U{3..24} (G G^T + 0.1 I) and 20,000 general n ~
+    U{4..64} (iid N(0,1)), one RHS each, FP64 and FP32: one graph launch per
+    batch; per-matrix plain GPU (sampled) and the CPU oracle beside it."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    import eigen_gb300 as gb
+    from eigen_gb300.batched import BatchedSolver
+    rng = np.random.default_rng(0)
+    sizes = np.concatenate([rng.integers(3, 25, 100000), rng.integers(4, 65, 20000)]).astype(np.int32)
+    kinds = np.concatenate([np.zeros(100000), np.ones(20000)]).astype(np.int32)
+    out = {}
+    for dtype, tdt, name in ((np.float64, torch.float64, "f64"), (np.float32, torch.float32, "f32")):
+        bs = BatchedSolver(sizes, kinds, dtype=dtype)
+        g = torch.Generator(device="cuda").manual_seed(1)
+        ah = np.empty(bs.a_elems, dtype=np.float64)
+        for i, n in enumerate(sizes):
+            m = rng.standard_normal((n, n))
+            if kinds[i] == 0:
+                m = m @ m.T + 0.1 * np.eye(n)
+            ah[bs.a_off[i]:bs.a_off[i] + n * n] = m.reshape(-1, order="F")
+        A0 = torch.from_numpy(ah).to(tdt).cuda()
+        B0 = torch.randn(bs.b_elems, dtype=tdt, device="cuda", generator=g)
+        A, B = A0.clone(), B0.clone()
+        info = torch.empty(len(sizes), dtype=torch.int32, device="cuda")
+        piv = torch.empty(bs.b_elems, dtype=torch.int32, device="cuda")
+        cfg = bs.autotune(A.clone(), B.clone(), info, piv)
+        times = []
+        for _ in range(args.warmup + args.steps):
+            A.copy_(A0); B.copy_(B0)
+            _, dt = _event_time(lambda: bs.solve(A, B, info, piv))
+            times.append(dt)
+        dt = min(times[args.warmup:])
+        failures = int((info >= 0).sum().item())
+        # per-matrix plain GPU path on a sample of 200 items
+        idx = rng.choice(len(sizes), 200, replace=False)
+        t0 = time.perf_counter()
+        for i in idx:
+            n = int(sizes[i])
+            m = ah[bs.a_off[i]:bs.a_off[i] + n * n].reshape((n, n), order="F").astype(dtype)
+            bvec = B0[bs.b_off[i]:bs.b_off[i] + n].cpu().numpy()
+            (gb.LLT(m, dtype=dtype) if kinds[i] == 0 else gb.PartialPivLU(m, dtype=dtype)).solve(bvec)
+        per_matrix = 200 / (time.perf_counter() - t0)
+        # CPU oracle
+        a_np = ah.astype(dtype)
+        b_np = B0.cpu().numpy().copy()
+        lib = O.port()
+        sfx = "d" if dtype == np.float64 else "s"
+        t0 = time.perf_counter()
+        getattr(lib, f"oracle_batched_llt_solve_{sfx}")(
+            100000, np.ascontiguousarray(sizes[:100000]), np.ascontiguousarray(bs.a_off[:100000]),
+            a_np.ctypes.data_as(C.c_void_p), np.ascontiguousarray(bs.b_off[:100000]), b_np.ctypes.data_as(C.c_void_p),
+            np.zeros(100000, dtype=np.int32))
+        getattr(lib, f"oracle_batched_lu_solve_{sfx}")(
+            20000, np.ascontiguousarray(sizes[100000:]), np.ascontiguousarray(bs.a_off[100000:120000]),
+            a_np.ctypes.data_as(C.c_void_p), np.ascontiguousarray(bs.b_off[100000:120000]),
+            b_np.ctypes.data_as(C.c_void_p), np.zeros(bs.b_elems, dtype=np.int32), np.zeros(20000, dtype=np.int32))
+        cpu = len(sizes) / (time.perf_counter() - t0)
+        flops = float(np.sum(np.where(kinds == 0, sizes ** 3 / 3 + 2 * sizes ** 2, 2 * sizes ** 3 / 3 + 2 * sizes ** 2)))
+        byts = float(np.sum(2 * sizes.astype(np.float64) ** 2 + 3 * sizes)) * np.dtype(dtype).itemsize
+        out[name] = {"solves_per_s": len(sizes) / dt, "ms": 1e3 * dt, "tflops": flops / dt / 1e12,
+                     "hbm_gbs": byts / dt / 1e9, "failures": failures, "autotuned": cfg,
+                     "per_matrix_plain_gpu_solves_per_s": per_matrix, "cpu_oracle_solves_per_s": cpu,
+                     "cpu_cores": O.num_threads()}
+    line = {"metric": METRIC, "value": out["f64"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["f64"]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: SPD G G^T + 0.1 I (n 3..24), general iid N(0,1) (n 4..64), seeded",
+            "config": {"workload": "batched: 100,000 LLT + 20,000 PartialPivLU, 1 RHS each, one CUDA-graph launch",
+                       "count": int(len(sizes))}, "batched": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_router(args):
+    """20,000 general systems n ~ U{32..512}, A = U diag(s) V^T, log10 kappa ~
+    U[1, 12]; the router (trained on rcond labels the method produces) against
+    always-FP64 and try-FP32-then-FP64, all at backward error <= 1e-13."""
+    import numpy as np
+    import torch
+
+    from eigen_gb300 import router as R
+    ntrain = args.train_labels
+    feats, labs = [], []
+    t_gen = t_lab = t_feat = 0.0
+    chunk = 20000
+    for c0 in range(0, ntrain, chunk):
+        (mb, A, _, _), dt = R.timed(lambda: R.generate(min(chunk, ntrain - c0), seed=1000 + c0, nmin=32, nmax=512))
+        t_gen += dt
+        y, dt = R.timed(lambda: R.labels(mb, A))
+        labs.append(y)
+        t_lab += dt
+        f, dt = R.timed(lambda: R.features(mb, A))
+        feats.append(f)
+        t_feat += dt
+        del A, mb
+    Ftr = torch.cat(feats).contiguous()
+    Ytr = torch.cat(labs).contiguous()
+    r = R.Router(seed=1)
+    (loss, t_fit) = R.timed(lambda: r.fit(Ftr, Ytr, epochs=12, batch=2048, lr=2e-3))
+    mt, At, Bt, logk = R.generate(20000, seed=7, nmin=32, nmax=512)
+    from eigen_gb300 import _lib
+    Lb = _lib.lib()
+    # always FP64 (the batched FP64 kernel; the plain GPU FP64 path per matrix is sampled below)
+    R.solve_fp64(mt, At, Bt)
+    X64, t64 = R.timed(lambda: R.solve_fp64(mt, At, Bt))
+    # try the FP32 tier on everything, FP64 for the failures
+    (Xtry, st_try), t_try = R.timed(lambda: R.solve_with_fallback(mt, At, Bt, np.arange(mt.count)))
+    # kernel phases of both (separate, profiled runs)
+    Lb.gbs_profile_reset()
+    Lb.gbs_profile_enable(1)
+    R.solve_fp64(mt, At, Bt)
+    torch.cuda.synchronize()
+    ph64 = collect_phases(Lb, 1)
+    R.solve_fp32_ir(mt, At, Bt)
+    torch.cuda.synchronize()
+    ph32 = collect_phases(Lb, 1)
+    Lb.gbs_profile_enable(0)
+    # routed: features + network + tier choice on the GPU, then the same fallback rule
+    (Xr, st_r), t_r = R.timed(lambda: R.route_and_solve(r, mt, At, Bt))
+    _, t_features = R.timed(lambda: R.features(mt, At))
+    import eigen_gb300 as gb
+    psample = np.random.default_rng(1).choice(mt.count, 100, replace=False)
+    t0 = time.perf_counter()
+    for i in psample:
+        gb.PartialPivLU(mt.matrix(At, i).contiguous().t()).solve(mt.vector(Bt, i).reshape(-1, 1).contiguous())
+    torch.cuda.synchronize()
+    per_matrix = len(psample) / (time.perf_counter() - t0)
+    sample = np.random.default_rng(0).choice(mt.count, 500, replace=False)
+    def worst(X):
+        errs = np.array([float(((mt.vector(Bt, i) - mt.matrix(At, i) @ mt.vector(X, i)).abs().max() /
+                                (mt.matrix(At, i).abs().sum(1).max() * mt.vector(X, i).abs().max() +
+                                 mt.vector(Bt, i).abs().max())).item()) for i in sample])
+        return float(errs.max())
+    pred = r.predict(R.features(mt, At))
+    ytest = R.labels(mt, At)
+    res = {"always_fp64": {"solves_per_s": mt.count / t64, "s": t64, "worst_backward_error_sample": worst(X64)},
+           "try_fp32_then_fp64": {"solves_per_s": mt.count / t_try, "s": t_try, **st_try,
+                                  "worst_backward_error_sample": worst(Xtry)},
+           "router": {"solves_per_s": mt.count / t_r, "s": t_r, **st_r, "worst_backward_error_sample": worst(Xr)},
+           "per_matrix_plain_gpu_fp64": {"solves_per_s": per_matrix, "sample": len(psample)},
+           "phases_ms": {"fp64_all": {k: v["ms"] for k, v in ph64.items()},
+                         "fp32_ir_all": {k: v["ms"] for k, v in ph32.items()}},
+           "features_s": t_features,
+           "network": {"train_systems": int(ntrain), "generate_s": t_gen, "labels_s": t_lab, "features_s": t_feat,
+                       "fit_s": t_fit,
+                       "final_train_mse_scaled": loss,
+                       "test_median_abs_err_log10_kappa": float((pred - ytest).abs().median().item()),
+                       "threshold_log10_kappa": r.threshold}}
+    line = {"metric": METRIC, "value": res["router"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1,
+            "warmup": 0, "ms_per_step": 1e3 * t_r, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic: A = U diag(s) V^T, Haar U, V, log10 kappa ~ U[1,12], seeded",
+            "config": {"workload": "router: 20,000 PartialPivLU systems n 32..512, 1 RHS", "count": 20000},
+            "router": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_mbatch(args):
+    """The router workload's medium batch (n ~ U{32..512}, log10 kappa ~
+    U[1, 12]) through each tier once: FP64 LU + solve, FP32 LU + FP64
+    refinement (small counts keep an ncu capture short)."""
+    import torch
+
+    from eigen_gb300 import router as R
+    mt, At, Bt, _ = R.generate(args.count, seed=7, nmin=32, nmax=512)
+    _, t64 = R.timed(lambda: R.solve_fp64(mt, At, Bt))
+    (_, st), t32 = R.timed(lambda: R.solve_fp32_ir(mt, At, Bt))
+    conv = int((st >= 0).sum().item())
+    print(json.dumps({"config": "mbatch", "count": args.count, "fp64_s": t64, "fp32_ir_s": t32,
+                      "fp32_converged": conv}), flush=True)
+    return 0
+
+
 def main():
     args = args_parse()
     if args.factor_once:
         return factor_once(args)
+    if args.impl == "ours" and args.config != "lu8192":
+        return {"llt16384": run_llt16384, "batched": run_batched, "router": run_router,
+                "mbatch": run_mbatch}[args.config](args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -109,9 +109,9 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_mbatch_matrix_elements": (c_i64, [c_vp]),
     "gbs_mbatch_vector_elements": (c_i64, [c_vp]),
     "gbs_mbatch_offsets": (c_int, [c_vp, c_vp, c_vp]),
-    "gbs_mbatch_lu_rcond": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
-    "gbs_mbatch_ir": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_vp, c_vp]),
-    "gbs_mbatch_features": (c_int, [c_vp, c_vp, c_vp, c_vp]),
+    "gbs_mbatch_lu_rcond": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "gbs_mbatch_ir": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_vp, c_vp]),
+    "gbs_mbatch_features": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "gbs_router_feature_count": (c_int, []),
     "gbs_mlp_create": (c_int, [C.POINTER(c_vp), c_int, c_int, C.c_uint64]),
     "gbs_mlp_destroy": (c_int, [c_vp]),

@@ -468,7 +468,7 @@ extern "C" int gbs_batched_solve(gbs_batched* p, void* d_a, void* d_b, int* d_in
 {
   if (!p || (p->count > 0 && (!d_a || !d_b || !d_info || !d_piv))) return GBS_INVALID_ARGUMENT;
   if (p->count == 0) return GBS_SUCCESS;
-  cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
+  cudaStream_t s = (cudaStream_t)stream;     // NULL: the legacy default stream
   if (!p->use_graph) return enqueue(p, s, d_a, d_b, d_info, d_piv);
   if (p->exec && (p->g_a != d_a || p->g_b != d_b || p->g_info != d_info || p->g_piv != d_piv)) {
     cudaGraphExecDestroy(p->exec);

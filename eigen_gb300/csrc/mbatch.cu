@@ -17,6 +17,7 @@
 #include "dense_driver.cuh"
 #include "gbs_common.cuh"
 #include "gbs_profile.cuh"
+#include "mbatch_lu.cuh"
 
 namespace gbs {
 namespace {
@@ -72,53 +73,11 @@ __device__ void block_argmax(T& s, int& i, T* rv, int* ri)
     if (better(rv[w], ri[w], s, i)) { s = rv[w]; i = ri[w]; }
 }
 
-// In-place partial-pivoting LU of a (n x n, ld n); pivots (0-based) to piv.
-// Returns the first exactly-zero pivot or -1 (same for every thread).
-template <typename T>
-__device__ int cta_getrf(T* a, int n, int* piv, T* rv, int* ri)
-{
-  int first_zero = -1;
-  for (int k = 0; k < n; ++k) {
-    T s = T(-2);
-    int idx = 0x7fffffff;
-    for (int i = k + threadIdx.x; i < n; i += kMB) {
-      const T x = a[(int64_t)k * n + i];
-      const T sc = (i == k) ? ((x != x) ? T(INFINITY) : gbs_abs(x)) : pivot_score(x);
-      if (better(sc, i, s, idx)) { s = sc; idx = i; }
-    }
-    block_argmax(s, idx, rv, ri);
-    const int p = idx;
-    const T pv = a[(int64_t)k * n + p];
-    __syncthreads();
-    if (threadIdx.x == 0) piv[k] = p;
-    if (pv != T(0)) {
-      if (p != k)
-        for (int c = threadIdx.x; c < n; c += kMB) {
-          const T t = a[(int64_t)c * n + k];
-          a[(int64_t)c * n + k] = a[(int64_t)c * n + p];
-          a[(int64_t)c * n + p] = t;
-        }
-      __syncthreads();
-      const T d = a[(int64_t)k * n + k];
-      for (int i = k + 1 + threadIdx.x; i < n; i += kMB) a[(int64_t)k * n + i] /= d;
-    } else if (first_zero < 0) {
-      first_zero = k;
-    }
-    __syncthreads();
-    // rank-1 update: warps over columns, lanes over rows (coalesced)
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int j = k + 1 + wid; j < n; j += kMB / 32) {
-      const T u = a[(int64_t)j * n + k];
-      T* cj = a + (int64_t)j * n;
-      const T* ck = a + (int64_t)k * n;
-      for (int i = k + 1 + lane; i < n; i += 32) cj[i] = fma(-ck[i], u, cj[i]);
-    }
-    __syncthreads();
-  }
-  return first_zero;
-}
+constexpr int kNB64 = 16;        // panel width of the FP64 LU
+constexpr int kNB32 = 32;        // panel width of the FP32 LU
 
-// x <- A^-1 x (trans = 0) or A^-T x (trans = 1) with PA = LU in a; x in shared memory
+// x <- A^-1 x (trans = 0) or A^-T x (trans = 1) with PA = LU in a; x in shared
+// memory; one barrier per column (the rcond estimator's transposed solves)
 template <typename T>
 __device__ void cta_lu_solve(const T* a, int n, const int* piv, T* x, int trans)
 {
@@ -163,37 +122,129 @@ __device__ void cta_lu_solve(const T* a, int n, const int* piv, T* x, int trans)
   }
 }
 
-__global__ void __launch_bounds__(kMB)
-mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __restrict__ A, int* __restrict__ piv,
-                       double* __restrict__ rhs, double* __restrict__ rcond, int* __restrict__ info)
+// Factor kernels: one CTA per item, the blocked LU's shared memory (two CTAs
+// per SM).  The FP64 one records ||A||_1 (needed by rcond) in anorm1 before the
+// matrix is overwritten; the FP32 one converts its FP64 item into the working
+// copy first.  info[it] = first exactly-zero pivot or -1.
+__global__ void __launch_bounds__(kMB, 2)
+mbatch_getrf64_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                      double* __restrict__ A, int* __restrict__ piv, double* __restrict__ anorm1,
+                      int* __restrict__ info)
+{
+  __shared__ double rv[kMB / 32];
+  extern __shared__ __align__(16) char dsm[];
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;      // ignore out-of-range indices (uniform over the CTA)
+    const MItem m = items[it];
+    const int n = m.n;
+    double* a = A + m.a_off;
+    if (anorm1) {
+      double best = 0.0;
+      for (int c = threadIdx.x >> 5; c < n; c += kMB / 32) {
+        double s = 0.0;
+#pragma unroll 4
+        for (int i = threadIdx.x & 31; i < n; i += 32) s += fabs(a[(int64_t)c * n + i]);
+        s = warp_sum(s);
+        best = s > best ? s : best;
+      }
+      best = block_max(best, rv);
+      if (threadIdx.x == 0) anorm1[it] = best;
+    }
+    const int fz = mb::cta_blocked_getrf<double, kNB64>(a, n, piv + m.v_off, dsm);
+    if (threadIdx.x == 0) info[it] = fz;
+  }
+}
+
+__global__ void __launch_bounds__(kMB, 2)
+mbatch_getrf32_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                      const double* __restrict__ A, float* __restrict__ W, int* __restrict__ piv,
+                      int* __restrict__ info)
+{
+  extern __shared__ __align__(16) char dsm[];
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;
+    const MItem m = items[it];
+    const int n = m.n;
+    const double* a = A + m.a_off;
+    float* w = W + m.a_off;
+    const int nn = n * n;
+#pragma unroll 4
+    for (int e = threadIdx.x; e < nn; e += kMB) w[e] = (float)a[e];
+    __syncthreads();
+    const int fz = mb::cta_blocked_getrf<float, kNB32>(w, n, piv + m.v_off, dsm);
+    if (threadIdx.x == 0) info[it] = fz;
+  }
+}
+
+// b - A x for the CTA's rows (FP64); 16 columns of loads issued together per
+// row.  Returns the thread's max |r_i| and max |x_i|.
+__device__ __forceinline__ void cta_residual(const double* __restrict__ a, int n, const double* __restrict__ b,
+                                             const double* x, double* r, double& rn, double& xn)
+{
+  for (int i = threadIdx.x; i < n; i += kMB) {
+    double s[4] = {b[i], 0.0, 0.0, 0.0};
+    for (int j0 = 0; j0 < n; j0 += 16) {
+      double v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = j0 + q < n ? a[(int64_t)(j0 + q) * n + i] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (j0 + q < n) s[q & 3] = fma(-v[q], x[j0 + q], s[q & 3]);
+    }
+    const double t = (s[0] + s[1]) + (s[2] + s[3]);
+    r[i] = t;
+    rn = fmax(rn, fabs(t));
+    xn = fmax(xn, fabs(x[i]));
+  }
+}
+
+// max_i sum_j |a(i, j)| over the CTA's rows, 16 loads issued together
+__device__ __forceinline__ double cta_row_abs_max(const double* __restrict__ a, int n)
+{
+  double best = 0.0;
+  for (int i = threadIdx.x; i < n; i += kMB) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int j0 = 0; j0 < n; j0 += 16) {
+      double v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = j0 + q < n ? a[(int64_t)(j0 + q) * n + i] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) s[q & 3] += fabs(v[q]);
+    }
+    best = fmax(best, (s[0] + s[1]) + (s[2] + s[3]));
+  }
+  return best;
+}
+
+// Solve + rcond of items factored by mbatch_getrf64_kernel (no dynamic shared
+// memory: several CTAs per SM hide the triangular solves' latency).
+// rcond: ConditionEstimator.h:56-169 (Hager / Higham), ||A||_1 from anorm1.
+__global__ void __launch_bounds__(kMB, 3)
+mbatch_solve_rcond_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                          const double* __restrict__ A, const int* __restrict__ piv, double* __restrict__ rhs,
+                          double* __restrict__ rcond)
 {
   __shared__ double x[kMaxN], sgn[kMaxN], osgn[kMaxN];
   __shared__ double rv[kMB / 32];
   __shared__ int ri[kMB / 32];
-  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;
     const MItem m = items[it];
     const int n = m.n;
-    double* a = A + m.a_off;
-    int* pv = piv + m.v_off;
-    // ||A||_1
-    double best = 0.0;
-    for (int c = threadIdx.x >> 5; c < n; c += kMB / 32) {
-      double s = 0.0;
-      for (int i = threadIdx.x & 31; i < n; i += 32) s += fabs(a[(int64_t)c * n + i]);
-      s = warp_sum(s);
-      best = s > best ? s : best;
-    }
-    const double anorm = block_max(best, rv);
-    const int fz = cta_getrf(a, n, pv, rv, ri);
-    if (threadIdx.x == 0) info[it] = fz;
-    // solve the right-hand side
+    const double* a = A + m.a_off;
+    const int* pv = piv + m.v_off;
     if (rhs) {
       for (int i = threadIdx.x; i < n; i += kMB) x[i] = rhs[m.v_off + i];
       __syncthreads();
-      cta_lu_solve(a, n, pv, x, 0);
+      mb::cta_lu_solve_blocked(a, n, pv, x);
       for (int i = threadIdx.x; i < n; i += kMB) rhs[m.v_off + i] = x[i];
       __syncthreads();
     }
+    if (!rcond) continue;        // uniform over the CTA
+    const double anorm = rcond[it];
     // rcond (ConditionEstimator.h:56-169)
     double rc;
     if (n == 0) rc = 1.0;
@@ -202,7 +253,7 @@ mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __res
     else {
       for (int i = threadIdx.x; i < n; i += kMB) x[i] = 1.0 / n;
       __syncthreads();
-      cta_lu_solve(a, n, pv, x, 0);
+      mb::cta_lu_solve_blocked(a, n, pv, x);
       double lb = block_sum([&] { double s = 0; for (int i = threadIdx.x; i < n; i += kMB) s += fabs(x[i]); return s; }(), rv);
       double old_lb = lb;
       int old_v = -1;
@@ -229,7 +280,7 @@ mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __res
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += kMB) x[i] = i == vi ? 1.0 : 0.0;
         __syncthreads();
-        cta_lu_solve(a, n, pv, x, 0);
+        mb::cta_lu_solve_blocked(a, n, pv, x);
         lb = block_sum([&] { double t = 0; for (int i = threadIdx.x; i < n; i += kMB) t += fabs(x[i]); return t; }(), rv);
         if (lb <= old_lb) break;
         for (int i = threadIdx.x; i < n; i += kMB) osgn[i] = sgn[i];
@@ -240,7 +291,7 @@ mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __res
       __syncthreads();
       for (int i = threadIdx.x; i < n; i += kMB) x[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (double)i / (double)(n - 1));
       __syncthreads();
-      cta_lu_solve(a, n, pv, x, 0);
+      mb::cta_lu_solve_blocked(a, n, pv, x);
       const double alt =
           2.0 * block_sum([&] { double t = 0; for (int i = threadIdx.x; i < n; i += kMB) t += fabs(x[i]); return t; }(), rv) /
           (3.0 * n);
@@ -252,40 +303,35 @@ mbatch_lu_rcond_kernel(const MItem* __restrict__ items, int count, double* __res
   }
 }
 
-// FP32 LU + FP64 refinement.  W: FP32 working copies (same layout as A).
-// status[it] = refinement steps taken (>= 0) when the backward error reached
-// tol, -1 when it did not (the caller re-solves those in FP64).
-__global__ void __launch_bounds__(kMB)
-mbatch_ir_kernel(const MItem* __restrict__ items, int count, const double* __restrict__ A, float* __restrict__ W,
-                 int* __restrict__ piv, const double* __restrict__ rhs, double* __restrict__ X, double tol, int max_iter,
+// FP64 refinement of items factored in FP32 by mbatch_getrf32_kernel.
+// status[it] on entry: the factor kernel's info (-1: no zero pivot); on exit:
+// refinement steps taken (>= 0) when the backward error reached tol, -1 when it
+// did not (the caller re-solves those in FP64).  X is written only on success.
+__global__ void __launch_bounds__(kMB, 4)
+mbatch_ir_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                 const double* __restrict__ A, const float* __restrict__ W, const int* __restrict__ piv,
+                 const double* __restrict__ rhs, double* __restrict__ X, double tol, int max_iter,
                  int* __restrict__ status)
 {
   __shared__ double x[kMaxN], r[kMaxN];
   __shared__ float d[kMaxN];
-  __shared__ float rv[kMB / 32];
-  __shared__ int ri[kMB / 32];
   __shared__ double rvd[kMB / 32];
-  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;
     const MItem m = items[it];
     const int n = m.n;
     const double* a = A + m.a_off;
-    float* w = W + m.a_off;
-    int* pv = piv + m.v_off;
-    for (int e = threadIdx.x; e < n * n; e += kMB) w[e] = (float)a[e];
+    const float* w = W + m.a_off;
+    const int* pv = piv + m.v_off;
+    const double* b = rhs + m.v_off;
+    const int fz = status[it];
     __syncthreads();
-    // ||A||_inf
-    double rmax = 0.0;
-    for (int i = threadIdx.x; i < n; i += kMB) {
-      double s = 0.0;
-      for (int j = 0; j < n; ++j) s += fabs(a[(int64_t)j * n + i]);
-      rmax = s > rmax ? s : rmax;
-    }
-    const double anorm = block_max(rmax, rvd);
-    const int fz = cta_getrf(w, n, pv, rv, ri);
     int result = -1;
     if (fz < 0) {
+      const double anorm = block_max(cta_row_abs_max(a, n), rvd);      // ||A||_inf
       double bmax = 0.0;
-      for (int i = threadIdx.x; i < n; i += kMB) { x[i] = 0.0; r[i] = rhs[m.v_off + i]; bmax = fmax(bmax, fabs(r[i])); }
+      for (int i = threadIdx.x; i < n; i += kMB) { x[i] = 0.0; r[i] = b[i]; bmax = fmax(bmax, fabs(r[i])); }
       bmax = block_max(bmax, rvd);
       for (int step = 0; step <= max_iter; ++step) {
         // correction d = LU^-1 (r / s) in FP32, x += s d
@@ -295,18 +341,12 @@ mbatch_ir_kernel(const MItem* __restrict__ items, int count, const double* __res
         const double sc = rm > 0 ? rm : 1.0;
         for (int i = threadIdx.x; i < n; i += kMB) d[i] = (float)(r[i] / sc);
         __syncthreads();
-        cta_lu_solve(w, n, pv, d, 0);
+        mb::cta_lu_solve_blocked<float>(w, n, pv, d);
         for (int i = threadIdx.x; i < n; i += kMB) x[i] += sc * (double)d[i];
         __syncthreads();
         // r = b - A x (FP64), backward error
         double rn = 0.0, xn = 0.0;
-        for (int i = threadIdx.x; i < n; i += kMB) {
-          double s = rhs[m.v_off + i];
-          for (int j = 0; j < n; ++j) s = fma(-a[(int64_t)j * n + i], x[j], s);
-          r[i] = s;
-          rn = fmax(rn, fabs(s));
-          xn = fmax(xn, fabs(x[i]));
-        }
+        cta_residual(a, n, b, x, r, rn, xn);
         rn = block_max(rn, rvd);
         xn = block_max(xn, rvd);
         const double den = anorm * xn + bmax;
@@ -314,7 +354,8 @@ mbatch_ir_kernel(const MItem* __restrict__ items, int count, const double* __res
         if (be <= tol) { result = step; break; }
         if (!(be == be)) break;
       }
-      for (int i = threadIdx.x; i < n; i += kMB) X[m.v_off + i] = x[i];
+      if (result >= 0)
+        for (int i = threadIdx.x; i < n; i += kMB) X[m.v_off + i] = x[i];
     }
     if (threadIdx.x == 0) status[it] = result;
     __syncthreads();
@@ -329,11 +370,14 @@ mbatch_ir_kernel(const MItem* __restrict__ items, int count, const double* __res
 constexpr int kFeat = 16;
 
 __global__ void __launch_bounds__(kMB)
-mbatch_features_kernel(const MItem* __restrict__ items, int count, const double* __restrict__ A, float* __restrict__ F)
+mbatch_features_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                       const double* __restrict__ A, float* __restrict__ F)
 {
   __shared__ float x[kMaxN], y[kMaxN];
   __shared__ float rv[kMB / 32];
-  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;      // ignore out-of-range indices (uniform over the CTA)
     const MItem m = items[it];
     const int n = m.n;
     const double* a = A + m.a_off;
@@ -416,9 +460,20 @@ struct gbs_mbatch {
   std::vector<int64_t> a_off, v_off;
   int64_t total_a = 0, total_v = 0;
   DevBuf items;
+  DevBuf order;      // item indices by decreasing n: the default processing order
 };
 
-static int mb_grid(int64_t count) { return (int)std::min<int64_t>(count, 8LL * device_sm_count()); }
+// One CTA per selected item: the block scheduler hands the next item to the
+// first CTA slot that frees up, and the default order (largest first) keeps
+// the tail of the launch short.
+static int mb_grid(int64_t count) { return (int)std::min<int64_t>(count, 0x7fffffff); }
+
+template <typename K>
+static int mb_smem(K kernel, size_t bytes)
+{
+  GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return GBS_SUCCESS;
+}
 
 extern "C" int gbs_mbatch_create(gbs_mbatch** out, int64_t count, const int* sizes)
 {
@@ -447,9 +502,14 @@ extern "C" int gbs_mbatch_create(gbs_mbatch** out, int64_t count, const int* siz
   }
   p->total_a = ao;
   p->total_v = vo;
+  std::vector<int> order((size_t)count);
+  for (int64_t i = 0; i < count; ++i) order[(size_t)i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sizes[x] > sizes[y]; });
   int rc = p->items.reserve(sizeof(MItem) * (size_t)std::max<int64_t>(count, 1));
+  if (rc == GBS_SUCCESS) rc = p->order.reserve(sizeof(int) * (size_t)std::max<int64_t>(count, 1));
   if (rc == GBS_SUCCESS && count > 0 &&
-      cudaMemcpy(p->items.p, items.data(), sizeof(MItem) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+      (cudaMemcpy(p->items.p, items.data(), sizeof(MItem) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(p->order.p, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice) != cudaSuccess))
     rc = GBS_CUDA_ERROR;
   if (rc != GBS_SUCCESS) {
     delete p;
@@ -476,40 +536,88 @@ extern "C" int gbs_mbatch_offsets(const gbs_mbatch* p, int64_t* a_off, int64_t* 
   return GBS_SUCCESS;
 }
 
-extern "C" int gbs_mbatch_lu_rcond(gbs_mbatch* p, double* d_a, int* d_piv, double* d_rhs, double* d_rcond, int* d_info,
-                                   void* stream)
+// d_items: device list of n_items item indices to process (NULL: all items,
+// largest first)
+static int mb_select(const gbs_mbatch* p, const int* d_items, int64_t n_items, int* count, const int** sel)
 {
-  if (!p || (p->count > 0 && (!d_a || !d_piv || !d_rcond || !d_info))) return GBS_INVALID_ARGUMENT;
-  if (p->count == 0) return GBS_SUCCESS;
-  cudaStream_t s = (cudaStream_t)stream;
-  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
-  mbatch_lu_rcond_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_piv, d_rhs,
-                                                          d_rcond, d_info);
-  GBS_CUDA_TRY(cudaGetLastError());
+  if (d_items) {
+    if (n_items < 0 || n_items > p->count) return GBS_INVALID_ARGUMENT;
+    *count = (int)n_items;
+    *sel = d_items;
+  } else {
+    *count = (int)p->count;
+    *sel = p->order.as<int>();
+  }
   return GBS_SUCCESS;
 }
 
-extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const double* d_a, float* d_work, int* d_piv, const double* d_rhs,
-                             double* d_x, double tol, int max_iter, int* d_status, void* stream)
+extern "C" int gbs_mbatch_lu_rcond(gbs_mbatch* p, const int* d_items, int64_t n_items, double* d_a, int* d_piv,
+                                   double* d_rhs, double* d_rcond, int* d_info, void* stream)
 {
-  if (!p || (p->count > 0 && (!d_a || !d_work || !d_piv || !d_rhs || !d_x || !d_status)) || max_iter < 0)
-    return GBS_INVALID_ARGUMENT;
-  if (p->count == 0) return GBS_SUCCESS;
+  if (!p) return GBS_INVALID_ARGUMENT;
+  int count = 0;
+  const int* sel = nullptr;
+  GBS_TRY(mb_select(p, d_items, n_items, &count, &sel));
+  if (count == 0) return GBS_SUCCESS;
+  if (!d_a || !d_piv || !d_info) return GBS_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
-  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
-  mbatch_ir_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_work, d_piv, d_rhs,
-                                                    d_x, tol, max_iter, d_status);
-  GBS_CUDA_TRY(cudaGetLastError());
+  constexpr size_t smem = mb::Layout<double, kNB64>::bytes;
+  GBS_TRY(mb_smem(mbatch_getrf64_kernel, smem));
+  {
+    PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+    mbatch_getrf64_kernel<<<mb_grid(count), kMB, smem, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a,
+                                                           d_piv, d_rcond, d_info);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  if (d_rhs || d_rcond) {
+    PhaseScope ps(s, PH_TRI_SOLVE, 0.0, 0.0);
+    mbatch_solve_rcond_kernel<<<mb_grid(count), kMB, 0, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a,
+                                                            d_piv, d_rhs, d_rcond);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
   return GBS_SUCCESS;
 }
 
-extern "C" int gbs_mbatch_features(gbs_mbatch* p, const double* d_a, float* d_feat, void* stream)
+extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const int* d_items, int64_t n_items, const double* d_a, float* d_work,
+                             int* d_piv, const double* d_rhs, double* d_x, double tol, int max_iter, int* d_status,
+                             void* stream)
 {
-  if (!p || (p->count > 0 && (!d_a || !d_feat))) return GBS_INVALID_ARGUMENT;
-  if (p->count == 0) return GBS_SUCCESS;
+  if (!p || max_iter < 0) return GBS_INVALID_ARGUMENT;
+  int count = 0;
+  const int* sel = nullptr;
+  GBS_TRY(mb_select(p, d_items, n_items, &count, &sel));
+  if (count == 0) return GBS_SUCCESS;
+  if (!d_a || !d_work || !d_piv || !d_rhs || !d_x || !d_status) return GBS_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  constexpr size_t smem = mb::Layout<float, kNB32>::bytes;
+  GBS_TRY(mb_smem(mbatch_getrf32_kernel, smem));
+  {
+    PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+    mbatch_getrf32_kernel<<<mb_grid(count), kMB, smem, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a,
+                                                           d_work, d_piv, d_status);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  {
+    PhaseScope ps(s, PH_RESIDUAL, 0.0, 0.0);
+    mbatch_ir_kernel<<<mb_grid(count), kMB, 0, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a, d_work,
+                                                   d_piv, d_rhs, d_x, tol, max_iter, d_status);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_features(gbs_mbatch* p, const int* d_items, int64_t n_items, const double* d_a,
+                                   float* d_feat, void* stream)
+{
+  if (!p) return GBS_INVALID_ARGUMENT;
+  int count = 0;
+  const int* sel = nullptr;
+  GBS_TRY(mb_select(p, d_items, n_items, &count, &sel));
+  if (count == 0) return GBS_SUCCESS;
+  if (!d_a || !d_feat) return GBS_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
   PhaseScope ps(s, PH_ROUTER, 0.0, 0.0);
-  mbatch_features_kernel<<<mb_grid(p->count), kMB, 0, s>>>(p->items.as<MItem>(), (int)p->count, d_a, d_feat);
+  mbatch_features_kernel<<<mb_grid(count), kMB, 0, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a, d_feat);
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }

@@ -17,7 +17,7 @@ extern "C" int gbs_tc_gemm_sub(int kind, int m, int n, int k, const float* d_a, 
   WorkspaceLease lease;
   if (lease.status != GBS_SUCCESS) return lease.status;
   Workspace& w = *lease.ws;
-  cudaStream_t s = stream ? (cudaStream_t)stream : w.stream;
+  cudaStream_t s = (cudaStream_t)stream;     // NULL: the legacy default stream
   GBS_TRY(w.status.reserve(sizeof(DeviceStatus)));
   GBS_TRY(reset_status(w.status.as<DeviceStatus>(), s));
   static thread_local TcWorkspace tws;
@@ -94,7 +94,7 @@ static int run_device(MixedFn fn, int n, int nrhs, const double* d_a, int lda, c
   GBS_TRY(ensure_device());
   WorkspaceLease lease;
   if (lease.status != GBS_SUCCESS) return lease.status;
-  cudaStream_t s = stream ? (cudaStream_t)stream : lease.ws->stream;
+  cudaStream_t s = (cudaStream_t)stream;     // NULL: the legacy default stream
   MixedResult r;
   const int rc = fn(s, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, o, &r);
   fill_info(info, r);

@@ -357,7 +357,7 @@ extern "C" int gbs_mlp_predict(const gbs_mlp* o, const float* d_x, int count, fl
 {
   if (!o || count < 0 || (count > 0 && (!d_x || !d_y))) return GBS_INVALID_ARGUMENT;
   if (count == 0) return GBS_SUCCESS;
-  cudaStream_t s = stream ? (cudaStream_t)stream : o->stream;
+  cudaStream_t s = (cudaStream_t)stream;     // NULL: the legacy default stream
   const int grid = std::min((count + kSamplesPerCTA - 1) / kSamplesPerCTA, 8 * device_sm_count());
   PhaseScope ps(s, PH_ROUTER, 2.0 * count * (double)o->P, 4.0 * count * (o->in + 1));
   mlp_predict_kernel<<<grid, kSamplesPerCTA, sizeof(float) * o->P, s>>>(o->in, o->params.as<float>(), d_x, count, d_y);

@@ -49,17 +49,34 @@ class MediumBatch:
     def _p(t):
         return C.c_void_p(t.data_ptr()) if t is not None else None
 
-    def lu_rcond(self, d_a, d_piv, d_rhs, d_rcond, d_info, stream=0):
-        L.check(L.lib().gbs_mbatch_lu_rcond(self._h, self._p(d_a), self._p(d_piv), self._p(d_rhs), self._p(d_rcond),
-                                            self._p(d_info), C.c_void_p(stream)), "mbatch.lu_rcond")
+    @staticmethod
+    def _sel(items):
+        """(device pointer, count) of an int32 CUDA tensor of item indices, or all items."""
+        if items is None:
+            return None, 0
+        assert items.dtype.is_floating_point is False and items.element_size() == 4 and items.is_cuda
+        return C.c_void_p(items.data_ptr()), int(items.numel())
 
-    def ir(self, d_a, d_work, d_piv, d_rhs, d_x, d_status, tol=1e-13, max_iter=10, stream=0):
-        L.check(L.lib().gbs_mbatch_ir(self._h, self._p(d_a), self._p(d_work), self._p(d_piv), self._p(d_rhs),
+    def lu_rcond(self, d_a, d_piv, d_rhs, d_rcond, d_info, items=None, stream=0):
+        sp, sn = self._sel(items)
+        if items is not None and sn == 0:
+            return
+        L.check(L.lib().gbs_mbatch_lu_rcond(self._h, sp, sn, self._p(d_a), self._p(d_piv), self._p(d_rhs),
+                                            self._p(d_rcond), self._p(d_info), C.c_void_p(stream)), "mbatch.lu_rcond")
+
+    def ir(self, d_a, d_work, d_piv, d_rhs, d_x, d_status, tol=1e-13, max_iter=10, items=None, stream=0):
+        sp, sn = self._sel(items)
+        if items is not None and sn == 0:
+            return
+        L.check(L.lib().gbs_mbatch_ir(self._h, sp, sn, self._p(d_a), self._p(d_work), self._p(d_piv), self._p(d_rhs),
                                       self._p(d_x), tol, max_iter, self._p(d_status), C.c_void_p(stream)),
                 "mbatch.ir")
 
-    def features(self, d_a, d_feat, stream=0):
-        L.check(L.lib().gbs_mbatch_features(self._h, self._p(d_a), self._p(d_feat), C.c_void_p(stream)),
+    def features(self, d_a, d_feat, items=None, stream=0):
+        sp, sn = self._sel(items)
+        if items is not None and sn == 0:
+            return
+        L.check(L.lib().gbs_mbatch_features(self._h, sp, sn, self._p(d_a), self._p(d_feat), C.c_void_p(stream)),
                 "mbatch.features")
 
     def matrix(self, d_a, i):
@@ -75,10 +92,23 @@ def feature_count() -> int:
     return int(L.lib().gbs_router_feature_count())
 
 
+def haar(k, n, generator):
+    """k Haar-random n x n orthogonal matrices: the Q factor (diag(R) > 0) of
+    seeded Gaussian matrices, computed as Cholesky-QR applied twice (G = Q R
+    with R = chol(G^T G), once more on Q for orthogonality to rounding level);
+    batched Cholesky and triangular solves instead of one QR per matrix."""
+    import torch
+    q = torch.randn(k, n, n, dtype=torch.float64, device="cuda", generator=generator)
+    for _ in range(2):
+        r = torch.linalg.cholesky(q.transpose(-1, -2) @ q, upper=True)
+        q = torch.linalg.solve_triangular(r, q, upper=True, left=False)
+    return q
+
+
 def generate(count, seed, nmin=32, nmax=512, logk=(1.0, 12.0)):
-    """A = U diag(s) V^T with Haar-random orthogonal U, V (QR of seeded
-    Gaussians, signs fixed by diag(R)) and s log-spaced from 1 to 1/kappa,
-    log10(kappa) uniform in logk.  Returns (batch, packed A, packed b, log10 kappa)."""
+    """A = U diag(s) V^T with Haar-random orthogonal U, V and s log-spaced
+    from 1 to 1/kappa, log10(kappa) uniform in logk; b iid N(0, 1).
+    Returns (batch, packed A, packed b, log10 kappa)."""
     import torch
     rng = np.random.default_rng(seed)
     sizes = rng.integers(nmin, nmax + 1, count).astype(np.int32)
@@ -87,22 +117,21 @@ def generate(count, seed, nmin=32, nmax=512, logk=(1.0, 12.0)):
     g = torch.Generator(device="cuda").manual_seed(int(seed))
     A = torch.empty(mb.a_elems, dtype=torch.float64, device="cuda")
     B = torch.randn(mb.v_elems, dtype=torch.float64, device="cuda", generator=g)
+    a_off = torch.as_tensor(mb.a_off[:count], device="cuda")
     for n in np.unique(sizes):
+        n = int(n)
         idx = np.nonzero(sizes == n)[0]
-        k = len(idx)
-        for c0 in range(0, k, 512):
-            sel = idx[c0:c0 + 512]
-            q1, r1 = torch.linalg.qr(torch.randn(len(sel), n, n, dtype=torch.float64, device="cuda", generator=g))
-            q1 = q1 * torch.sign(torch.diagonal(r1, dim1=-2, dim2=-1)).unsqueeze(-2)
-            q2, r2 = torch.linalg.qr(torch.randn(len(sel), n, n, dtype=torch.float64, device="cuda", generator=g))
-            q2 = q2 * torch.sign(torch.diagonal(r2, dim1=-2, dim2=-1)).unsqueeze(-2)
+        for c0 in range(0, len(idx), 256):
+            sel = idx[c0:c0 + 256]
+            u = haar(len(sel), n, g)
+            v = haar(len(sel), n, g)
             lk = torch.as_tensor(logkappa[sel], dtype=torch.float64, device="cuda")
-            t = torch.linspace(0, 1, int(n), dtype=torch.float64, device="cuda")
+            t = torch.linspace(0, 1, n, dtype=torch.float64, device="cuda")
             s = torch.pow(10.0, -lk[:, None] * t[None, :])
-            mats = (q1 * s[:, None, :]) @ q2.transpose(-1, -2)
+            mats = (u * s[:, None, :]) @ v.transpose(-1, -2)
             flat = mats.transpose(-1, -2).reshape(len(sel), -1)      # column-major per matrix
-            offs = torch.as_tensor(mb.a_off[sel], device="cuda")
-            ar = torch.arange(int(n) * int(n), device="cuda")
+            offs = a_off[torch.as_tensor(sel, device="cuda")]
+            ar = torch.arange(n * n, device="cuda")
             A[(offs[:, None] + ar[None, :]).reshape(-1)] = flat.reshape(-1)
     torch.cuda.synchronize()
     return mb, A, B, logkappa
@@ -126,6 +155,16 @@ def features(mb, A):
     f = torch.empty(mb.count, feature_count(), dtype=torch.float32, device="cuda")
     mb.features(A, f)
     return f
+
+
+def route_and_solve(router, mb, A, B):
+    """The routed solve: features, network, tier per item (on the GPU), then
+    FP32 + refinement for the items routed low and FP64 for the rest and for
+    every low item that did not reach the bound."""
+    import torch
+    tier = router.route(router.predict(features(mb, A)))
+    lo = torch.nonzero(tier == 1).flatten().to(torch.int32)
+    return solve_with_fallback(mb, A, B, lo)
 
 
 class Router:
@@ -190,61 +229,50 @@ class Router:
 
 
 # ----------------------------------------------------------------- solving strategies
-def _subset(mb, A, B, idx):
-    """Gather items idx into a new packed batch (device copies)."""
+def _items(idx):
     import torch
-    sizes = mb.sizes[idx]
-    sub = MediumBatch(sizes)
-    a_src = np.concatenate([np.arange(mb.a_off[i], mb.a_off[i] + int(mb.sizes[i]) ** 2) for i in idx]) if len(idx) \
-        else np.zeros(0, dtype=np.int64)
-    v_src = np.concatenate([np.arange(mb.v_off[i], mb.v_off[i] + int(mb.sizes[i])) for i in idx]) if len(idx) \
-        else np.zeros(0, dtype=np.int64)
-    a_idx = torch.as_tensor(a_src, device="cuda")
-    v_idx = torch.as_tensor(v_src, device="cuda")
-    return sub, A[a_idx].contiguous(), B[v_idx].contiguous(), v_idx
+    if hasattr(idx, "is_cuda"):
+        return idx.to(torch.int32).contiguous()
+    return torch.as_tensor(np.asarray(idx, dtype=np.int32), device="cuda")
 
 
-def solve_fp64(mb, A, B):
-    """FP64 LU + solve of every item: returns X (packed)."""
+def solve_fp64(mb, A, B, items=None, X=None):
+    """FP64 LU + solve of the items (all by default) on a copy of A: returns X
+    (packed; B's values for the items not solved unless X is given)."""
     import torch
     a = A.clone()
-    x = B.clone()
+    x = B.clone() if X is None else X
     piv = torch.empty(mb.v_elems, dtype=torch.int32, device="cuda")
-    rc = torch.empty(mb.count, dtype=torch.float64, device="cuda")
     info = torch.empty(mb.count, dtype=torch.int32, device="cuda")
-    mb.lu_rcond(a, piv, x, rc, info)
+    mb.lu_rcond(a, piv, x, None, info, items=None if items is None else _items(items))
     return x
 
 
-def solve_fp32_ir(mb, A, B, tol=1e-13, max_iter=10):
+def solve_fp32_ir(mb, A, B, tol=1e-13, max_iter=10, items=None, X=None):
+    """FP32 LU + FP64 refinement; returns (X, status) with status -1 for the
+    items that did not reach tol (their X entries are left as they were) and
+    -2 for items not attempted."""
     import torch
     work = torch.empty(mb.a_elems, dtype=torch.float32, device="cuda")
     piv = torch.empty(mb.v_elems, dtype=torch.int32, device="cuda")
-    x = torch.zeros(mb.v_elems, dtype=torch.float64, device="cuda")
-    st = torch.empty(mb.count, dtype=torch.int32, device="cuda")
-    mb.ir(A, work, piv, B, x, st, tol, max_iter)
+    x = torch.zeros(mb.v_elems, dtype=torch.float64, device="cuda") if X is None else X
+    st = torch.full((mb.count,), -2, dtype=torch.int32, device="cuda")
+    mb.ir(A, work, piv, B, x, st, tol, max_iter, items=None if items is None else _items(items))
     return x, st
 
 
 def solve_with_fallback(mb, A, B, first_fp32_idx):
-    """FP32 + refinement on first_fp32_idx, FP64 on the rest and on every item
-    the FP32 tier did not bring to the bound.  Returns (X, stats)."""
+    """FP32 + refinement on first_fp32_idx (host indices or an int CUDA
+    tensor), FP64 on the rest and on every item the FP32 tier did not bring to
+    the bound.  Returns (X, stats)."""
     import torch
-    X = torch.empty(mb.v_elems, dtype=torch.float64, device="cuda")
-    all_idx = np.arange(mb.count)
-    lo = np.asarray(first_fp32_idx, dtype=np.int64)
-    hi = np.setdiff1d(all_idx, lo)
-    failed = np.zeros(0, dtype=np.int64)
-    if len(lo):
-        sub, a, b, v_idx = _subset(mb, A, B, lo)
-        x, st = solve_fp32_ir(sub, a, b)
-        X[v_idx] = x
-        failed = lo[(st.cpu().numpy() < 0)]
-    redo = np.concatenate([hi, failed]).astype(np.int64)
-    if len(redo):
-        sub, a, b, v_idx = _subset(mb, A, B, redo)
-        X[v_idx] = solve_fp64(sub, a, b)
-    return X, {"fp32_attempts": int(len(lo)), "fp32_failed": int(len(failed)), "fp64_solves": int(len(redo))}
+    X = B.clone()
+    lo = _items(first_fp32_idx)
+    _, st = solve_fp32_ir(mb, A, B, items=lo, X=X)
+    redo = torch.nonzero(st < 0).flatten().to(torch.int32)
+    solve_fp64(mb, A, B, items=redo, X=X)
+    failed = int((st == -1).sum().item())
+    return X, {"fp32_attempts": int(lo.numel()), "fp32_failed": failed, "fp64_solves": int(redo.numel())}
 
 
 def backward_errors(mb, A, X, B):

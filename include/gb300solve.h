@@ -250,7 +250,9 @@ typedef struct gbs_refine_info {
 void gbs_refine_options_default(gbs_refine_options* opt);
 
 /* General A (PartialPivLU).  Device buffers, stream-ordered on `stream`
- * (NULL: the library's own); returns when X is final.  opt NULL: defaults. */
+ * (a cudaStream_t; NULL is the legacy default stream, as in every other
+ * `void* stream` argument of this header); returns when X is final.  opt
+ * NULL: defaults. */
 int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
                            int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
 /* Host buffers (copied in and out inside the call). */
@@ -305,30 +307,35 @@ int gbs_batched_config(const gbs_batched* plan, int* warps_small, int* warps_lar
  * per PartialPivLU object; each item reproduces PartialPivLU (pivots:
  * PartialPivLU.h:365-409), its solve and rcond() (ConditionEstimator.h:56-169).
  *   gbs_mbatch_lu_rcond  FP64 LU in place, 0-based pivots, solve of d_rhs in
- *                        place (may be NULL), rcond per item, info = first zero
- *                        pivot or -1
+ *                        place (may be NULL), rcond per item (d_rcond may be
+ *                        NULL: not estimated), info = first zero pivot or -1
  *   gbs_mbatch_ir        FP32 LU of a working copy (d_work: matrix-sized FP32
  *                        scratch) + FP64 refinement of x to backward error
  *                        <= tol; status = refinement steps, or -1 when the bound
- *                        was not reached (solve those items in FP64)
+ *                        was not reached (solve those items in FP64); x is
+ *                        written only for the items that reached it
  *   gbs_mbatch_features  gbs_router_feature_count() floats per item: size,
  *                        diagonal and row-norm statistics, four power-iteration
  *                        estimates of ||A||_2 / ||A||_F and their ratios
  * The router network is a 3-layer MLP (in -> 64 -> 64 -> 1, ReLU) trained on
  * the GPU by its own kernels (Adam on the mean squared error of the predicted
  * log10 condition number against rcond-derived labels); gbs_router_route maps
- * predictions to tiers: 1 = FP32 + refinement, 0 = FP64. */
+ * predictions to tiers: 1 = FP32 + refinement, 0 = FP64.
+ * d_items (device, n_items indices) restricts a call to those items; NULL
+ * processes every item.  Per-item outputs (info, rcond, status, features) are
+ * indexed by item, so a subset call leaves the other items' entries alone. */
 typedef struct gbs_mbatch gbs_mbatch;
 int gbs_mbatch_create(gbs_mbatch** out, int64_t count, const int* sizes);
 int gbs_mbatch_destroy(gbs_mbatch* plan);
 int64_t gbs_mbatch_matrix_elements(const gbs_mbatch* plan);
 int64_t gbs_mbatch_vector_elements(const gbs_mbatch* plan);
 int gbs_mbatch_offsets(const gbs_mbatch* plan, int64_t* a_offsets, int64_t* v_offsets);
-int gbs_mbatch_lu_rcond(gbs_mbatch* plan, double* d_a, int* d_piv, double* d_rhs, double* d_rcond, int* d_info,
+int gbs_mbatch_lu_rcond(gbs_mbatch* plan, const int* d_items, int64_t n_items, double* d_a, int* d_piv,
+                        double* d_rhs, double* d_rcond, int* d_info, void* stream);
+int gbs_mbatch_ir(gbs_mbatch* plan, const int* d_items, int64_t n_items, const double* d_a, float* d_work, int* d_piv,
+                  const double* d_rhs, double* d_x, double tol, int max_iter, int* d_status, void* stream);
+int gbs_mbatch_features(gbs_mbatch* plan, const int* d_items, int64_t n_items, const double* d_a, float* d_features,
                         void* stream);
-int gbs_mbatch_ir(gbs_mbatch* plan, const double* d_a, float* d_work, int* d_piv, const double* d_rhs, double* d_x,
-                  double tol, int max_iter, int* d_status, void* stream);
-int gbs_mbatch_features(gbs_mbatch* plan, const double* d_a, float* d_features, void* stream);
 int gbs_router_feature_count(void);
 
 typedef struct gbs_mlp gbs_mlp;

@@ -124,3 +124,25 @@ def test_mixed_device_buffers():
     a = np.asfortranarray(A.cpu().numpy())
     assert O.backward_error(a, X.cpu().numpy(), B.cpu().numpy()) <= BAR
     assert not info["fell_back"]
+
+
+@pytest.mark.parametrize("spd", [False, True])
+def test_mixed_device_orders_after_pending_default_stream_work(spd):
+    """A NULL stream is the legacy default stream: a solve queued right after
+    an unfinished producer of A on that stream must read the finished A."""
+    torch = pytest.importorskip("torch")
+    from eigen_gb300 import solve_spd_mixed
+    n = 3072
+    g = torch.Generator(device="cuda").manual_seed(9)
+    G = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(2, n, dtype=torch.float64, device="cuda", generator=g).t()
+    torch.cuda.synchronize()
+    assert torch.cuda.current_stream().cuda_stream == 0
+    fn = solve_spd_mixed if spd else solve_mixed
+    for _ in range(2):
+        A = (G @ G.t() + n * torch.eye(n, dtype=torch.float64, device="cuda")).t()   # ~50 ms of FP64 GEMM, async
+        X, info = fn(A, B, tier="fp64")
+        X2, _ = fn(A, B, tier="fp64")
+        assert torch.equal(X, X2)
+        a = np.asfortranarray(A.cpu().numpy())
+        assert O.backward_error(a, X.cpu().numpy(), B.cpu().numpy()) <= BAR

@@ -146,3 +146,24 @@ def test_router_trains_and_beats_always_fp64():
     r2 = R.Router(seed=99)
     r2.load(path)
     assert np.array_equal(r2.params(), r.params())
+
+
+def test_mbatch_subset_calls_touch_only_their_items():
+    mb, A, B, _ = R.generate(30, seed=21, nmin=32, nmax=100)
+    sel = [3, 7, 19, 29]
+    X = R.solve_fp64(mb, A, B, items=sel, X=B.clone())
+    full = R.solve_fp64(mb, A, B)
+    for i in range(mb.count):
+        want = mb.vector(full if i in sel else B, i)
+        assert torch.equal(mb.vector(X, i), want), i
+    F = R.features(mb, A)
+    f = torch.full_like(F, 7.0)
+    mb.features(A, f, items=R._items(sel))
+    for i in range(mb.count):
+        assert torch.equal(f[i], F[i]) if i in sel else bool((f[i] == 7.0).all()), i
+    x32, st = R.solve_fp32_ir(mb, A, B, items=sel, X=B.clone())
+    st = st.cpu().numpy()
+    assert set(np.nonzero(st != -2)[0]) == set(sel)
+    for i in range(mb.count):
+        if st[i] == -2 or st[i] == -1:
+            assert torch.equal(mb.vector(x32, i), mb.vector(B, i)), i
