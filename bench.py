@@ -571,7 +571,7 @@ def run_batched(args):
 def run_router(args):
     """20,000 general systems n ~ U{32..512}, A = U diag(s) V^T, log10 kappa ~
     U[1, 12]; the router (trained on rcond labels the method produces) against
-    always-FP64 and try-FP32-then-FP64, all at backward error <= 1e-13."""
+    always-FP64 and try-lowest-then-fallback, all at backward error <= 1e-13."""
     import numpy as np
     import torch
 
@@ -600,19 +600,38 @@ def run_router(args):
     # always FP64 (the batched FP64 kernel; the plain GPU FP64 path per matrix is sampled below)
     R.solve_fp64(mt, At, Bt)
     X64, t64 = R.timed(lambda: R.solve_fp64(mt, At, Bt))
-    # try the FP32 tier on everything, FP64 for the failures
-    (Xtry, st_try), t_try = R.timed(lambda: R.solve_with_fallback(mt, At, Bt, np.arange(mt.count)))
-    # kernel phases of both (separate, profiled runs)
+    # try-lowest-then-fallback: FP32 + IR on everything, GMRES-IR on the same
+    # factors for what it leaves, FP64 for the rest
+    R.solve_cascade(mt, At, Bt)
+    (Xtry, st_try), t_try = R.timed(lambda: R.solve_cascade(mt, At, Bt))
+    # kernel phases of the FP64 and FP32 tiers on everything (separate, profiled runs)
     Lb.gbs_profile_reset()
     Lb.gbs_profile_enable(1)
     R.solve_fp64(mt, At, Bt)
     torch.cuda.synchronize()
     ph64 = collect_phases(Lb, 1)
-    R.solve_fp32_ir(mt, At, Bt)
+    ws = R.Fp32Work(mt)
+    R.solve_fp32_ir(mt, At, Bt, ws=ws)
     torch.cuda.synchronize()
     ph32 = collect_phases(Lb, 1)
+    st_ir = ws.status.cpu().numpy().copy()
+    R.solve_fp32_gmres(mt, At, Bt, items=torch.nonzero(ws.status == -1).flatten().to(torch.int32), ws=ws,
+                       factored=True)
+    torch.cuda.synchronize()
+    phgm = collect_phases(Lb, 1)
     Lb.gbs_profile_enable(0)
-    # routed: features + network + tier choice on the GPU, then the same fallback rule
+    st_gm = ws.status.cpu().numpy()
+    inner = ws.inner.cpu().numpy()
+    by_kappa = {}
+    for lo in range(1, 12):
+        sel = (logk >= lo) & (logk < lo + 1)
+        fail_ir = sel & (st_ir < 0)
+        by_kappa[f"{lo}-{lo + 1}"] = {
+            "ir_converged": float((st_ir[sel] >= 0).mean()),
+            "gmres_converged_of_ir_failures": float((st_gm[fail_ir] >= 0).mean()) if fail_ir.any() else None,
+            "gmres_mean_inner": float(inner[fail_ir].mean()) if fail_ir.any() else None}
+    # routed: features + network + tier choice on the GPU, then each tier
+    R.route_and_solve(r, mt, At, Bt)
     (Xr, st_r), t_r = R.timed(lambda: R.route_and_solve(r, mt, At, Bt))
     _, t_features = R.timed(lambda: R.features(mt, At))
     import eigen_gb300 as gb
@@ -631,18 +650,20 @@ def run_router(args):
     pred = r.predict(R.features(mt, At))
     ytest = R.labels(mt, At)
     res = {"always_fp64": {"solves_per_s": mt.count / t64, "s": t64, "worst_backward_error_sample": worst(X64)},
-           "try_fp32_then_fp64": {"solves_per_s": mt.count / t_try, "s": t_try, **st_try,
-                                  "worst_backward_error_sample": worst(Xtry)},
+           "try_lowest_then_fallback": {"solves_per_s": mt.count / t_try, "s": t_try, **st_try,
+                                        "worst_backward_error_sample": worst(Xtry)},
            "router": {"solves_per_s": mt.count / t_r, "s": t_r, **st_r, "worst_backward_error_sample": worst(Xr)},
            "per_matrix_plain_gpu_fp64": {"solves_per_s": per_matrix, "sample": len(psample)},
            "phases_ms": {"fp64_all": {k: v["ms"] for k, v in ph64.items()},
-                         "fp32_ir_all": {k: v["ms"] for k, v in ph32.items()}},
+                         "fp32_ir_all": {k: v["ms"] for k, v in ph32.items()},
+                         "gmres_ir_on_ir_failures": {k: v["ms"] for k, v in phgm.items()}},
+           "tier_convergence_by_log10_kappa": by_kappa,
            "features_s": t_features,
            "network": {"train_systems": int(ntrain), "generate_s": t_gen, "labels_s": t_lab, "features_s": t_feat,
                        "fit_s": t_fit,
                        "final_train_mse_scaled": loss,
                        "test_median_abs_err_log10_kappa": float((pred - ytest).abs().median().item()),
-                       "threshold_log10_kappa": r.threshold}}
+                       "t_ir_log10_kappa": r.t_ir, "t_gmres_log10_kappa": r.t_gmres}}
     line = {"metric": METRIC, "value": res["router"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1,
             "warmup": 0, "ms_per_step": 1e3 * t_r, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic: A = U diag(s) V^T, Haar U, V, log10 kappa ~ U[1,12], seeded",

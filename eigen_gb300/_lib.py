@@ -110,7 +110,10 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_mbatch_vector_elements": (c_i64, [c_vp]),
     "gbs_mbatch_offsets": (c_int, [c_vp, c_vp, c_vp]),
     "gbs_mbatch_lu_rcond": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
-    "gbs_mbatch_ir": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_vp, c_vp]),
+    "gbs_mbatch_ir": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_int, c_vp,
+                              c_vp]),
+    "gbs_mbatch_gmres_ir": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, C.c_double, c_int, c_int, c_int,
+                                    c_vp, c_vp, c_vp]),
     "gbs_mbatch_features": (c_int, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "gbs_router_feature_count": (c_int, []),
     "gbs_mlp_create": (c_int, [C.POINTER(c_vp), c_int, c_int, C.c_uint64]),
@@ -122,7 +125,7 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_mlp_train_step": (c_int, [c_vp, c_vp, c_vp, c_int, C.c_float, c_dp]),
     "gbs_mlp_fit": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, C.c_float, C.c_uint64, c_dp]),
     "gbs_mlp_predict": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp]),
-    "gbs_router_route": (c_int, [c_vp, c_int, C.c_float, c_vp, c_vp]),
+    "gbs_router_route": (c_int, [c_vp, c_int, C.c_float, C.c_float, c_vp, c_vp]),
     # tracing
     "gbs_kernel_launch_count": (C.c_uint64, []),
     "gbs_profile_enable": (c_int, [c_int]),

@@ -304,9 +304,11 @@ mbatch_solve_rcond_kernel(const MItem* __restrict__ items, const int* __restrict
 }
 
 // FP64 refinement of items factored in FP32 by mbatch_getrf32_kernel.
-// status[it] on entry: the factor kernel's info (-1: no zero pivot); on exit:
-// refinement steps taken (>= 0) when the backward error reached tol, -1 when it
-// did not (the caller re-solves those in FP64).  X is written only on success.
+// status[it] on entry: -1 when the FP32 factors are usable (the factor
+// kernel's info for a factorization without a zero pivot); on exit: refinement
+// steps taken (>= 0) when the backward error reached tol, -1 when it did not,
+// -2 when the FP32 factorization had a zero pivot (the caller re-solves both in
+// FP64).  X is written only on success.
 __global__ void __launch_bounds__(kMB, 4)
 mbatch_ir_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
                  const double* __restrict__ A, const float* __restrict__ W, const int* __restrict__ piv,
@@ -327,8 +329,8 @@ mbatch_ir_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, i
     const double* b = rhs + m.v_off;
     const int fz = status[it];
     __syncthreads();
-    int result = -1;
-    if (fz < 0) {
+    int result = fz == -1 ? -1 : -2;
+    if (fz == -1) {
       const double anorm = block_max(cta_row_abs_max(a, n), rvd);      // ||A||_inf
       double bmax = 0.0;
       for (int i = threadIdx.x; i < n; i += kMB) { x[i] = 0.0; r[i] = b[i]; bmax = fmax(bmax, fabs(r[i])); }
@@ -358,6 +360,192 @@ mbatch_ir_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, i
         for (int i = threadIdx.x; i < n; i += kMB) X[m.v_off + i] = x[i];
     }
     if (threadIdx.x == 0) status[it] = result;
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ GMRES-IR
+// FP64 GMRES (restarted every outer step, CGS2 Arnoldi, Givens rotations) on
+// M^-1 A d = M^-1 r with the FP32 LU as M, inside FP64 iterative refinement
+// (Carson & Higham's GMRES-IR).  Reaches the FP64 backward-error bound for
+// condition numbers well past the FP32 factorization's own limit.
+constexpr int kMaxKrylov = 16;
+
+// vout = M^-1 vin with the FP32 factors applied in FP64 arithmetic (vin, vout
+// FP64 shared vectors, may alias)
+__device__ void cta_precond(const float* __restrict__ w32, int n, const int* __restrict__ pv, const double* vin,
+                            double* vout)
+{
+  if (vin != vout) {
+    for (int i = threadIdx.x; i < n; i += kMB) vout[i] = vin[i];
+    __syncthreads();
+  }
+  mb::cta_lu_solve_blocked<double, float>(w32, n, pv, vout);
+}
+
+// y = A v (FP64, v in shared memory), 16 loads in flight per row
+__device__ __forceinline__ void cta_matvec(const double* __restrict__ a, int n, const double* v, double* y)
+{
+  for (int i = threadIdx.x; i < n; i += kMB) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int j0 = 0; j0 < n; j0 += 16) {
+      double q16[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) q16[q] = j0 + q < n ? a[(int64_t)(j0 + q) * n + i] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (j0 + q < n) s[q & 3] = fma(q16[q], v[j0 + q], s[q & 3]);
+    }
+    y[i] = (s[0] + s[1]) + (s[2] + s[3]);
+  }
+}
+
+// status[it] on entry and exit as for mbatch_ir_kernel (so a refinement
+// failure, -1, may be handed straight to this kernel); on exit outer steps
+// taken (>= 0) when the backward error reached tol.  inner[it]: total
+// GMRES iterations.  V: Krylov basis, (kMaxKrylov + 1) vectors per item at
+// element offset v_off * (kMaxKrylov + 1).
+__global__ void __launch_bounds__(kMB, 3)
+mbatch_gmres_kernel(const MItem* __restrict__ items, const int* __restrict__ sel, int count, int total,
+                    const double* __restrict__ A, const float* __restrict__ W, const int* __restrict__ piv,
+                    const double* __restrict__ rhs, double* __restrict__ X, double* __restrict__ V, double tol,
+                    int max_outer, int restart, double inner_tol, int* __restrict__ status, int* __restrict__ inner)
+{
+  __shared__ double x[kMaxN], r[kMaxN], wv[kMaxN];
+  __shared__ double H[(kMaxKrylov + 1) * kMaxKrylov];
+  __shared__ double cs[kMaxKrylov], sn[kMaxKrylov], g[kMaxKrylov + 1], yv[kMaxKrylov];
+  __shared__ double hcol[kMaxKrylov + 1];
+  __shared__ double red[kMB / 32][kMaxKrylov + 1];
+  __shared__ double rvd[kMB / 32];
+  __shared__ int s_stop;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int it = sel[t];
+    if (it < 0 || it >= total) continue;
+    const MItem m = items[it];
+    const int n = m.n;
+    const double* a = A + m.a_off;
+    const float* w32 = W + m.a_off;
+    const int* pv = piv + m.v_off;
+    const double* b = rhs + m.v_off;
+    double* Vb = V + m.v_off * (int64_t)(kMaxKrylov + 1);
+    const int fz = status[it];
+    __syncthreads();
+    int result = fz == -1 ? -1 : -2, inner_total = 0;
+    if (fz == -1) {
+      const double anorm = block_max(cta_row_abs_max(a, n), rvd);
+      double bmax = 0.0;
+      for (int i = tid; i < n; i += kMB) { x[i] = 0.0; r[i] = b[i]; bmax = fmax(bmax, fabs(b[i])); }
+      bmax = block_max(bmax, rvd);
+      for (int outer = 0; outer < max_outer; ++outer) {
+        cta_precond(w32, n, pv, r, wv);                               // z = M^-1 r
+        double ss = 0.0;
+        for (int i = tid; i < n; i += kMB) ss += wv[i] * wv[i];
+        const double beta = sqrt(block_sum(ss, rvd));
+        if (!(beta > 0.0)) break;
+        for (int i = tid; i < n; i += kMB) Vb[i] = wv[i] / beta;
+        if (tid == 0) {
+          g[0] = beta;
+          for (int q = 1; q <= kMaxKrylov; ++q) g[q] = 0.0;
+        }
+        __syncthreads();
+        int kdone = 0;
+        for (int k = 0; k < restart; ++k) {
+          for (int i = tid; i < n; i += kMB) wv[i] = Vb[(int64_t)k * n + i];
+          __syncthreads();
+          cta_matvec(a, n, wv, r);                                   // r <- A v_k (r is rebuilt after the cycle)
+          __syncthreads();
+          cta_precond(w32, n, pv, r, wv);                             // w = M^-1 A v_k
+          // classical Gram-Schmidt, twice
+          for (int pass = 0; pass < 2; ++pass) {
+            double part[kMaxKrylov + 1];
+#pragma unroll
+            for (int q = 0; q <= kMaxKrylov; ++q) part[q] = 0.0;
+            for (int i = tid; i < n; i += kMB) {
+              const double wi = wv[i];
+#pragma unroll
+              for (int q = 0; q <= kMaxKrylov; ++q)
+                if (q <= k) part[q] = fma(Vb[(int64_t)q * n + i], wi, part[q]);
+            }
+#pragma unroll
+            for (int q = 0; q <= kMaxKrylov; ++q)
+              if (q <= k) {
+                const double v = warp_sum(part[q]);
+                if (lane == 0) red[warp][q] = v;
+              }
+            __syncthreads();
+            if (tid <= k) {
+              double h = 0.0;
+              for (int w8 = 0; w8 < kMB / 32; ++w8) h += red[w8][tid];
+              hcol[tid] = pass == 0 ? h : hcol[tid] + h;
+              yv[tid] = h;                                            // this pass's coefficients
+            }
+            __syncthreads();
+            for (int i = tid; i < n; i += kMB) {
+              double s0 = wv[i];
+              for (int q = 0; q <= k; ++q) s0 = fma(-Vb[(int64_t)q * n + i], yv[q], s0);
+              wv[i] = s0;
+            }
+            __syncthreads();
+          }
+          double s2 = 0.0;
+          for (int i = tid; i < n; i += kMB) s2 += wv[i] * wv[i];
+          const double hnext = sqrt(block_sum(s2, rvd));
+          if (tid == 0) {
+            for (int q = 0; q < k; ++q) {                               // earlier rotations
+              const double h0 = hcol[q], h1 = hcol[q + 1];
+              hcol[q] = cs[q] * h0 + sn[q] * h1;
+              hcol[q + 1] = -sn[q] * h0 + cs[q] * h1;
+            }
+            const double hk = hcol[k];
+            const double rr = sqrt(hk * hk + hnext * hnext);
+            const double c = rr > 0 ? hk / rr : 1.0, sgn = rr > 0 ? hnext / rr : 0.0;
+            cs[k] = c;
+            sn[k] = sgn;
+            hcol[k] = rr;
+            g[k + 1] = -sgn * g[k];
+            g[k] = c * g[k];
+            for (int q = 0; q <= k; ++q) H[q + (kMaxKrylov + 1) * k] = hcol[q];
+            s_stop = !(hnext > 0.0) || !(rr > 0.0) || fabs(g[k + 1]) <= inner_tol * beta;
+          }
+          __syncthreads();
+          kdone = k + 1;
+          if (s_stop) break;
+          if (k + 1 < restart)
+            for (int i = tid; i < n; i += kMB) Vb[(int64_t)(k + 1) * n + i] = wv[i] / hnext;
+          __syncthreads();
+        }
+        inner_total += kdone;
+        if (tid == 0) {                                               // y = H^-1 g (upper triangular)
+          for (int q = kdone - 1; q >= 0; --q) {
+            double s0 = g[q];
+            for (int l = q + 1; l < kdone; ++l) s0 -= H[q + (kMaxKrylov + 1) * l] * yv[l];
+            yv[q] = s0 / H[q + (kMaxKrylov + 1) * q];
+          }
+        }
+        __syncthreads();
+        for (int i = tid; i < n; i += kMB) {
+          double s0 = x[i];
+          for (int q = 0; q < kdone; ++q) s0 = fma(Vb[(int64_t)q * n + i], yv[q], s0);
+          x[i] = s0;
+        }
+        __syncthreads();
+        double rn = 0.0, xn = 0.0;
+        cta_residual(a, n, b, x, r, rn, xn);
+        rn = block_max(rn, rvd);
+        xn = block_max(xn, rvd);
+        const double den = anorm * xn + bmax;
+        const double be = den > 0 ? rn / den : rn;
+        if (be <= tol) { result = outer; break; }
+        if (!(be == be)) break;
+      }
+      if (result >= 0)
+        for (int i = tid; i < n; i += kMB) X[m.v_off + i] = x[i];
+    }
+    if (tid == 0) {
+      status[it] = result;
+      if (inner) inner[it] = inner_total;
+    }
     __syncthreads();
   }
 }
@@ -461,6 +649,7 @@ struct gbs_mbatch {
   int64_t total_a = 0, total_v = 0;
   DevBuf items;
   DevBuf order;      // item indices by decreasing n: the default processing order
+  DevBuf krylov;     // GMRES-IR basis, reserved on first use
 };
 
 // One CTA per selected item: the block scheduler hands the next item to the
@@ -579,8 +768,8 @@ extern "C" int gbs_mbatch_lu_rcond(gbs_mbatch* p, const int* d_items, int64_t n_
 }
 
 extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const int* d_items, int64_t n_items, const double* d_a, float* d_work,
-                             int* d_piv, const double* d_rhs, double* d_x, double tol, int max_iter, int* d_status,
-                             void* stream)
+                             int* d_piv, const double* d_rhs, double* d_x, double tol, int max_iter, int factored,
+                             int* d_status, void* stream)
 {
   if (!p || max_iter < 0) return GBS_INVALID_ARGUMENT;
   int count = 0;
@@ -589,9 +778,9 @@ extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const int* d_items, int64_t n_items,
   if (count == 0) return GBS_SUCCESS;
   if (!d_a || !d_work || !d_piv || !d_rhs || !d_x || !d_status) return GBS_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
-  constexpr size_t smem = mb::Layout<float, kNB32>::bytes;
-  GBS_TRY(mb_smem(mbatch_getrf32_kernel, smem));
-  {
+  if (!factored) {
+    constexpr size_t smem = mb::Layout<float, kNB32>::bytes;
+    GBS_TRY(mb_smem(mbatch_getrf32_kernel, smem));
     PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
     mbatch_getrf32_kernel<<<mb_grid(count), kMB, smem, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a,
                                                            d_work, d_piv, d_status);
@@ -601,6 +790,37 @@ extern "C" int gbs_mbatch_ir(gbs_mbatch* p, const int* d_items, int64_t n_items,
     PhaseScope ps(s, PH_RESIDUAL, 0.0, 0.0);
     mbatch_ir_kernel<<<mb_grid(count), kMB, 0, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a, d_work,
                                                    d_piv, d_rhs, d_x, tol, max_iter, d_status);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_mbatch_gmres_ir(gbs_mbatch* p, const int* d_items, int64_t n_items, const double* d_a,
+                                   float* d_work, int* d_piv, const double* d_rhs, double* d_x, double tol,
+                                   int max_outer, int restart, int factored, int* d_status, int* d_inner,
+                                   void* stream)
+{
+  if (!p || max_outer < 0 || restart < 1 || restart > kMaxKrylov) return GBS_INVALID_ARGUMENT;
+  int count = 0;
+  const int* sel = nullptr;
+  GBS_TRY(mb_select(p, d_items, n_items, &count, &sel));
+  if (count == 0) return GBS_SUCCESS;
+  if (!d_a || !d_work || !d_piv || !d_rhs || !d_x || !d_status) return GBS_INVALID_ARGUMENT;
+  GBS_TRY(p->krylov.reserve(sizeof(double) * (size_t)p->total_v * (kMaxKrylov + 1)));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!factored) {
+    constexpr size_t smem = mb::Layout<float, kNB32>::bytes;
+    GBS_TRY(mb_smem(mbatch_getrf32_kernel, smem));
+    PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+    mbatch_getrf32_kernel<<<mb_grid(count), kMB, smem, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a,
+                                                           d_work, d_piv, d_status);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  {
+    PhaseScope ps(s, PH_RESIDUAL, 0.0, 0.0);
+    mbatch_gmres_kernel<<<mb_grid(count), kMB, 0, s>>>(p->items.as<MItem>(), sel, count, (int)p->count, d_a, d_work,
+                                                      d_piv, d_rhs, d_x, p->krylov.as<double>(), tol, max_outer,
+                                                      restart, 1e-10, d_status, d_inner);
     GBS_CUDA_TRY(cudaGetLastError());
   }
   return GBS_SUCCESS;

@@ -100,14 +100,17 @@ __device__ int cta_blocked_getrf(T* __restrict__ a, int n, int* __restrict__ piv
       }
       cta_argmax(s, idx, rv, ri);
       const int p = idx;
+      // the two rows involved are published by their owners only: row kk
+      // lives in thread j (slot 0), row p in thread (p - k0) mod kMB
+      const int p_owner = (p - k0) & (kMB - 1);
+      const bool p_hi = (p - k0) >= kMB;
+      if (tid == p_owner) {
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        if (rows[i] == p)
+        for (int jj = 0; jj < NB; ++jj) prow[jj] = p_hi ? v[1][jj] : v[0][jj];
+      }
+      if (tid == j) {
 #pragma unroll
-          for (int jj = 0; jj < NB; ++jj) prow[jj] = v[i][jj];
-        if (rows[i] == kk)
-#pragma unroll
-          for (int jj = 0; jj < NB; ++jj) krow[jj] = v[i][jj];
+        for (int jj = 0; jj < NB; ++jj) krow[jj] = v[0][jj];
       }
       __syncthreads();
       const T pv = prow[j];
@@ -115,16 +118,23 @@ __device__ int cta_blocked_getrf(T* __restrict__ a, int n, int* __restrict__ piv
       if (tid == 0) spiv[j] = p;
       if (!swap && first_zero < 0) first_zero = kk;
       const T* u = swap ? prow : krow;
+      if (swap && p != kk) {
+        if (tid == j) {
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj) v[0][jj] = prow[jj];
+        }
+        if (tid == p_owner) {
+          if (p_hi) {
+#pragma unroll
+            for (int jj = 0; jj < NB; ++jj) v[1][jj] = krow[jj];
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < NB; ++jj) v[0][jj] = krow[jj];
+          }
+        }
+      }
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
-        if (swap && p != kk) {
-          if (rows[i] == kk)
-#pragma unroll
-            for (int jj = 0; jj < NB; ++jj) v[i][jj] = prow[jj];
-          else if (rows[i] == p)
-#pragma unroll
-            for (int jj = 0; jj < NB; ++jj) v[i][jj] = krow[jj];
-        }
         if (rows[i] > kk && rows[i] < n) {
           if (swap) v[i][j] = v[i][j] / pv;
           const T l = v[i][j];
@@ -268,12 +278,12 @@ __device__ int cta_blocked_getrf(T* __restrict__ a, int n, int* __restrict__ piv
 }
 
 // x[i] - sum_{j < nb} a(i, b0 + j) x[b0 + j], the nb <= 32 loads issued together
-template <typename T>
-__device__ __forceinline__ T block_dot_sub(const T* __restrict__ a, int n, int i, int b0, int nb, const T* x)
+template <typename TA, typename T>
+__device__ __forceinline__ T block_dot_sub(const TA* __restrict__ a, int n, int i, int b0, int nb, const T* x)
 {
   T v[32];
 #pragma unroll
-  for (int j = 0; j < 32; ++j) v[j] = j < nb ? a[(int64_t)(b0 + j) * n + i] : T(0);
+  for (int j = 0; j < 32; ++j) v[j] = j < nb ? T(a[(int64_t)(b0 + j) * n + i]) : T(0);
   T s[4] = {x[i], T(0), T(0), T(0)};
 #pragma unroll
   for (int j = 0; j < 32; ++j)
@@ -283,9 +293,11 @@ __device__ __forceinline__ T block_dot_sub(const T* __restrict__ a, int n, int i
 
 // x <- U^-1 L^-1 P x for PA = LU in a (ld n); x in shared memory.  Blocked by
 // 32 rows: warp 0 solves each diagonal block with shuffles from a register copy
-// of its rows, then every thread updates the rows beyond it.
-template <typename T>
-__device__ void cta_lu_solve_blocked(const T* __restrict__ a, int n, const int* __restrict__ piv, T* x)
+// of its rows, then every thread updates the rows beyond it.  The arithmetic
+// is T's; the factors may be stored narrower (TA = float with T = double: FP32
+// factors applied in FP64, as GMRES-IR's preconditioner needs).
+template <typename T, typename TA = T>
+__device__ void cta_lu_solve_blocked(const TA* __restrict__ a, int n, const int* __restrict__ piv, T* x)
 {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (warp == 0)                        // row interchanges in order, pivots fetched 32 at a time
@@ -304,7 +316,7 @@ __device__ void cta_lu_solve_blocked(const T* __restrict__ a, int n, const int* 
     if (warp == 0) {
       T row[32];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = (lane < nb && j < lane) ? a[(int64_t)(b0 + j) * n + b0 + lane] : T(0);
+      for (int j = 0; j < 32; ++j) row[j] = (lane < nb && j < lane) ? T(a[(int64_t)(b0 + j) * n + b0 + lane]) : T(0);
       T xi = lane < nb ? x[b0 + lane] : T(0);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
@@ -314,7 +326,7 @@ __device__ void cta_lu_solve_blocked(const T* __restrict__ a, int n, const int* 
       if (lane < nb) x[b0 + lane] = xi;
     }
     __syncthreads();
-    for (int i = b0 + nb + tid; i < n; i += kMB) x[i] = block_dot_sub<T>(a, n, i, b0, nb, x);
+    for (int i = b0 + nb + tid; i < n; i += kMB) x[i] = block_dot_sub<TA, T>(a, n, i, b0, nb, x);
     __syncthreads();
   }
   // backward: upper, non-unit
@@ -323,7 +335,7 @@ __device__ void cta_lu_solve_blocked(const T* __restrict__ a, int n, const int* 
     if (warp == 0) {
       T row[32];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = (lane < nb && j >= lane && j < nb) ? a[(int64_t)(b0 + j) * n + b0 + lane] : T(0);
+      for (int j = 0; j < 32; ++j) row[j] = (lane < nb && j >= lane && j < nb) ? T(a[(int64_t)(b0 + j) * n + b0 + lane]) : T(0);
       T xi = lane < nb ? x[b0 + lane] : T(0);
 #pragma unroll
       for (int j = 31; j >= 0; --j) {
@@ -336,7 +348,7 @@ __device__ void cta_lu_solve_blocked(const T* __restrict__ a, int n, const int* 
       if (lane < nb) x[b0 + lane] = xi;
     }
     __syncthreads();
-    for (int i = tid; i < b0; i += kMB) x[i] = block_dot_sub<T>(a, n, i, b0, nb, x);
+    for (int i = tid; i < b0; i += kMB) x[i] = block_dot_sub<TA, T>(a, n, i, b0, nb, x);
     __syncthreads();
   }
 }

@@ -185,11 +185,16 @@ mlp_predict_kernel(int in, const float* __restrict__ params, const float* __rest
   }
 }
 
-// tier[i] = pred[i] <= threshold ? 1 (FP32 + refinement) : 0 (FP64)
-__global__ void router_route_kernel(const float* __restrict__ pred, int count, float threshold, int* __restrict__ tier)
+// predicted log10 kappa -> tier: 1 = FP32 LU + refinement, 2 = FP32 LU +
+// GMRES-IR, 0 = FP64 LU
+__global__ void router_route_kernel(const float* __restrict__ pred, int count, float t_ir, float t_gmres,
+                                    int* __restrict__ tier)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count) tier[i] = pred[i] <= threshold ? 1 : 0;
+  if (i < count) {
+    const float v = pred[i];
+    tier[i] = v <= t_ir ? 1 : (v <= t_gmres ? 2 : 0);
+  }
 }
 
 uint64_t splitmix(uint64_t& s)
@@ -365,12 +370,12 @@ extern "C" int gbs_mlp_predict(const gbs_mlp* o, const float* d_x, int count, fl
   return GBS_SUCCESS;
 }
 
-extern "C" int gbs_router_route(const float* d_pred, int count, float threshold, int* d_tier, void* stream)
+extern "C" int gbs_router_route(const float* d_pred, int count, float t_ir, float t_gmres, int* d_tier, void* stream)
 {
   if (count < 0 || (count > 0 && (!d_pred || !d_tier))) return GBS_INVALID_ARGUMENT;
   if (count == 0) return GBS_SUCCESS;
   count_launch();
-  router_route_kernel<<<(count + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_pred, count, threshold, d_tier);
+  router_route_kernel<<<(count + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_pred, count, t_ir, t_gmres, d_tier);
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }

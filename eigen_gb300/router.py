@@ -8,7 +8,8 @@ Pipeline (every numeric step runs in libgb300solve kernels):
                        power-iteration estimates (gbs_mbatch_features)
   * ``Router``         3-layer width-64 MLP trained on the GPU by its own
                        forward / backward / Adam kernels (gbs_mlp_*), routing
-                       each system to FP32 + FP64 refinement or to FP64
+                       each system to FP32 LU + FP64 refinement, FP32 LU +
+                       GMRES-IR, or FP64 LU
   * ``solve_*``        routed solve, always-FP64, and try-FP32-then-FP64
                        fallback; the FP64 tier decides every result the FP32
                        tier cannot bring to the backward-error bound
@@ -64,13 +65,31 @@ class MediumBatch:
         L.check(L.lib().gbs_mbatch_lu_rcond(self._h, sp, sn, self._p(d_a), self._p(d_piv), self._p(d_rhs),
                                             self._p(d_rcond), self._p(d_info), C.c_void_p(stream)), "mbatch.lu_rcond")
 
-    def ir(self, d_a, d_work, d_piv, d_rhs, d_x, d_status, tol=1e-13, max_iter=10, items=None, stream=0):
+    def ir(self, d_a, d_work, d_piv, d_rhs, d_x, d_status, tol=1e-13, max_iter=10, items=None, factored=False,
+           stream=0):
         sp, sn = self._sel(items)
         if items is not None and sn == 0:
             return
         L.check(L.lib().gbs_mbatch_ir(self._h, sp, sn, self._p(d_a), self._p(d_work), self._p(d_piv), self._p(d_rhs),
-                                      self._p(d_x), tol, max_iter, self._p(d_status), C.c_void_p(stream)),
-                "mbatch.ir")
+                                      self._p(d_x), tol, max_iter, int(factored), self._p(d_status),
+                                      C.c_void_p(stream)), "mbatch.ir")
+
+    def gmres_ir(self, d_a, d_work, d_piv, d_rhs, d_x, d_status, tol=1e-13, max_outer=6, restart=16, d_inner=None,
+                 items=None, factored=False, stream=0):
+        sp, sn = self._sel(items)
+        if items is not None and sn == 0:
+            return
+        L.check(L.lib().gbs_mbatch_gmres_ir(self._h, sp, sn, self._p(d_a), self._p(d_work), self._p(d_piv),
+                                            self._p(d_rhs), self._p(d_x), tol, max_outer, restart, int(factored),
+                                            self._p(d_status), self._p(d_inner), C.c_void_p(stream)),
+                "mbatch.gmres_ir")
+
+    def largest_first(self, idx):
+        """idx (int32 CUDA tensor) reordered by decreasing n (shorter launch tail)."""
+        import torch
+        if getattr(self, "_sizes_dev", None) is None:
+            self._sizes_dev = torch.as_tensor(self.sizes, device="cuda")
+        return idx[torch.argsort(self._sizes_dev[idx.long()], descending=True, stable=True)].contiguous()
 
     def features(self, d_a, d_feat, items=None, stream=0):
         sp, sn = self._sel(items)
@@ -158,20 +177,19 @@ def features(mb, A):
 
 
 def route_and_solve(router, mb, A, B):
-    """The routed solve: features, network, tier per item (on the GPU), then
-    FP32 + refinement for the items routed low and FP64 for the rest and for
-    every low item that did not reach the bound."""
-    import torch
+    """The routed solve: features, network and tier per item (on the GPU),
+    then each tier on its items and FP64 for every item a refinement tier did
+    not bring to the bound."""
     tier = router.route(router.predict(features(mb, A)))
-    lo = torch.nonzero(tier == 1).flatten().to(torch.int32)
-    return solve_with_fallback(mb, A, B, lo)
+    return solve_tiers(mb, A, B, tier)
 
 
 class Router:
-    def __init__(self, seed=0, threshold=6.0):
+    def __init__(self, seed=0, t_ir=7.3, t_gmres=8.5):
         self._h = C.c_void_p()
         L.check(L.lib().gbs_mlp_create(C.byref(self._h), feature_count(), 64, seed), "mlp.create")
-        self.threshold = threshold      # route to FP32 + refinement when predicted log10 kappa <= threshold
+        self.t_ir = t_ir          # FP32 + refinement when predicted log10 kappa <= t_ir
+        self.t_gmres = t_gmres    # FP32 + GMRES-IR when <= t_gmres, FP64 above
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -211,20 +229,20 @@ class Router:
     def route(self, pred_logk):
         import torch
         tier = torch.empty(pred_logk.shape[0], dtype=torch.int32, device="cuda")
-        L.check(L.lib().gbs_router_route(C.c_void_p(pred_logk.data_ptr()), pred_logk.shape[0], self.threshold,
+        L.check(L.lib().gbs_router_route(C.c_void_p(pred_logk.data_ptr()), pred_logk.shape[0], self.t_ir, self.t_gmres,
                                          C.c_void_p(tier.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream)),
                 "router.route")
         return tier
 
     def save(self, path):
         with open(path, "w") as f:
-            json.dump({"in_dim": feature_count(), "width": 64, "threshold": self.threshold,
+            json.dump({"in_dim": feature_count(), "width": 64, "t_ir": self.t_ir, "t_gmres": self.t_gmres,
                        "label_scale": LABEL_SCALE, "params": self.params().tolist()}, f)
 
     def load(self, path):
         with open(path) as f:
             d = json.load(f)
-        self.threshold = d["threshold"]
+        self.t_ir, self.t_gmres = d["t_ir"], d["t_gmres"]
         self.set_params(np.asarray(d["params"], dtype=np.float32))
 
 
@@ -248,31 +266,98 @@ def solve_fp64(mb, A, B, items=None, X=None):
     return x
 
 
-def solve_fp32_ir(mb, A, B, tol=1e-13, max_iter=10, items=None, X=None):
-    """FP32 LU + FP64 refinement; returns (X, status) with status -1 for the
-    items that did not reach tol (their X entries are left as they were) and
-    -2 for items not attempted."""
+class Fp32Work:
+    """FP32 factor storage shared by the refinement tiers of one batch."""
+
+    def __init__(self, mb):
+        import torch
+        self.work = torch.empty(mb.a_elems, dtype=torch.float32, device="cuda")
+        self.piv = torch.empty(mb.v_elems, dtype=torch.int32, device="cuda")
+        self.status = torch.full((mb.count,), NOT_ATTEMPTED, dtype=torch.int32, device="cuda")
+        self.inner = torch.zeros(mb.count, dtype=torch.int32, device="cuda")
+
+
+NOT_ATTEMPTED = -3      # status of items no refinement tier was asked to solve
+
+
+def solve_fp32_ir(mb, A, B, tol=1e-13, max_iter=10, items=None, X=None, ws=None):
+    """FP32 LU + FP64 refinement; returns (X, status): status >= 0 converged,
+    -1 not converged, -2 FP32 zero pivot (X entries left as they were),
+    NOT_ATTEMPTED for items not in `items`."""
     import torch
-    work = torch.empty(mb.a_elems, dtype=torch.float32, device="cuda")
-    piv = torch.empty(mb.v_elems, dtype=torch.int32, device="cuda")
+    ws = ws or Fp32Work(mb)
     x = torch.zeros(mb.v_elems, dtype=torch.float64, device="cuda") if X is None else X
-    st = torch.full((mb.count,), -2, dtype=torch.int32, device="cuda")
-    mb.ir(A, work, piv, B, x, st, tol, max_iter, items=None if items is None else _items(items))
-    return x, st
+    mb.ir(A, ws.work, ws.piv, B, x, ws.status, tol, max_iter, items=None if items is None else _items(items))
+    return x, ws.status
+
+
+def solve_fp32_gmres(mb, A, B, tol=1e-13, max_outer=4, restart=16, items=None, X=None, ws=None, factored=False):
+    """FP32 LU preconditioning FP64 GMRES-IR; returns (X, status, inner
+    iterations).  factored=True continues from ws's FP32 factors (the items
+    a solve_fp32_ir call left at -1)."""
+    import torch
+    ws = ws or Fp32Work(mb)
+    x = torch.zeros(mb.v_elems, dtype=torch.float64, device="cuda") if X is None else X
+    mb.gmres_ir(A, ws.work, ws.piv, B, x, ws.status, tol, max_outer, restart, ws.inner,
+                items=None if items is None else _items(items), factored=factored)
+    return x, ws.status, ws.inner
+
+
+def _fp64_rest(mb, A, B, X, status):
+    """FP64 LU + solve of every item whose status is negative."""
+    import torch
+    redo = torch.nonzero(status < 0).flatten().to(torch.int32)
+    solve_fp64(mb, A, B, items=mb.largest_first(redo), X=X)
+    return int(redo.numel())
 
 
 def solve_with_fallback(mb, A, B, first_fp32_idx):
     """FP32 + refinement on first_fp32_idx (host indices or an int CUDA
     tensor), FP64 on the rest and on every item the FP32 tier did not bring to
     the bound.  Returns (X, stats)."""
+    X = B.clone()
+    ws = Fp32Work(mb)
+    lo = mb.largest_first(_items(first_fp32_idx))
+    solve_fp32_ir(mb, A, B, items=lo, X=X, ws=ws)
+    failed = int(((ws.status == -1) | (ws.status == -2)).sum().item())
+    fp64 = _fp64_rest(mb, A, B, X, ws.status)
+    return X, {"fp32_attempts": int(lo.numel()), "fp32_failed": failed, "fp64_solves": fp64}
+
+
+def solve_cascade(mb, A, B):
+    """Try-lowest-then-fallback without a router: every item FP32 + IR, the
+    items it leaves unconverged FP32 GMRES-IR on the same factors, the rest
+    FP64.  Returns (X, stats)."""
     import torch
     X = B.clone()
-    lo = _items(first_fp32_idx)
-    _, st = solve_fp32_ir(mb, A, B, items=lo, X=X)
-    redo = torch.nonzero(st < 0).flatten().to(torch.int32)
-    solve_fp64(mb, A, B, items=redo, X=X)
-    failed = int((st == -1).sum().item())
-    return X, {"fp32_attempts": int(lo.numel()), "fp32_failed": failed, "fp64_solves": int(redo.numel())}
+    ws = Fp32Work(mb)
+    solve_fp32_ir(mb, A, B, X=X, ws=ws)
+    ir_ok = int((ws.status >= 0).sum().item())
+    retry = mb.largest_first(torch.nonzero(ws.status == -1).flatten().to(torch.int32))
+    solve_fp32_gmres(mb, A, B, items=retry, X=X, ws=ws, factored=True)
+    gm_ok = int((ws.status >= 0).sum().item()) - ir_ok
+    fp64 = _fp64_rest(mb, A, B, X, ws.status)
+    return X, {"ir_converged": ir_ok, "gmres_attempts": int(retry.numel()), "gmres_converged": gm_ok,
+               "fp64_solves": fp64}
+
+
+def solve_tiers(mb, A, B, tier):
+    """Per-item tiers (int CUDA tensor: 1 FP32 + IR, 2 FP32 + GMRES-IR, 0
+    FP64); every item a refinement tier leaves unconverged is solved in FP64.
+    Returns (X, stats)."""
+    import torch
+    X = B.clone()
+    ws = Fp32Work(mb)
+    t1 = mb.largest_first(torch.nonzero(tier == 1).flatten().to(torch.int32))
+    t2 = mb.largest_first(torch.nonzero(tier == 2).flatten().to(torch.int32))
+    solve_fp32_ir(mb, A, B, items=t1, X=X, ws=ws)
+    solve_fp32_gmres(mb, A, B, items=t2, X=X, ws=ws)
+    st = ws.status
+    stats = {"ir_routed": int(t1.numel()), "gmres_routed": int(t2.numel()),
+             "ir_failed": int(((st < 0) & (st != NOT_ATTEMPTED) & (tier == 1)).sum().item()),
+             "gmres_failed": int(((st < 0) & (st != NOT_ATTEMPTED) & (tier == 2)).sum().item())}
+    stats["fp64_solves"] = _fp64_rest(mb, A, B, X, st)
+    return X, stats
 
 
 def backward_errors(mb, A, X, B):

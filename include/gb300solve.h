@@ -311,16 +311,28 @@ int gbs_batched_config(const gbs_batched* plan, int* warps_small, int* warps_lar
  *                        NULL: not estimated), info = first zero pivot or -1
  *   gbs_mbatch_ir        FP32 LU of a working copy (d_work: matrix-sized FP32
  *                        scratch) + FP64 refinement of x to backward error
- *                        <= tol; status = refinement steps, or -1 when the bound
- *                        was not reached (solve those items in FP64); x is
- *                        written only for the items that reached it
+ *                        <= tol; status = refinement steps, -1 when the bound
+ *                        was not reached, -2 when the FP32 factorization hit a
+ *                        zero pivot (solve those items in FP64); x is written
+ *                        only for the items that reached it.  factored != 0
+ *                        reuses the FP32 factors already in d_work / d_piv and
+ *                        refines the items whose d_status is -1
+ *   gbs_mbatch_gmres_ir  the same FP32 LU as the preconditioner of FP64 GMRES
+ *                        (restart <= 16, CGS2 Arnoldi) inside FP64 refinement
+ *                        (GMRES-IR): at most max_outer cycles; factored and
+ *                        status as for gbs_mbatch_ir (so the items a
+ *                        gbs_mbatch_ir call left at -1 can be passed on as
+ *                        they are); d_inner (may be NULL) = GMRES iterations
+ *                        per item; the Krylov basis is held by the plan
+ *                        (allocated on the first call)
  *   gbs_mbatch_features  gbs_router_feature_count() floats per item: size,
  *                        diagonal and row-norm statistics, four power-iteration
  *                        estimates of ||A||_2 / ||A||_F and their ratios
  * The router network is a 3-layer MLP (in -> 64 -> 64 -> 1, ReLU) trained on
  * the GPU by its own kernels (Adam on the mean squared error of the predicted
  * log10 condition number against rcond-derived labels); gbs_router_route maps
- * predictions to tiers: 1 = FP32 + refinement, 0 = FP64.
+ * predictions to tiers: 1 = FP32 + refinement (prediction <= t_ir), 2 = FP32 +
+ * GMRES-IR (<= t_gmres), 0 = FP64.
  * d_items (device, n_items indices) restricts a call to those items; NULL
  * processes every item.  Per-item outputs (info, rcond, status, features) are
  * indexed by item, so a subset call leaves the other items' entries alone. */
@@ -333,7 +345,11 @@ int gbs_mbatch_offsets(const gbs_mbatch* plan, int64_t* a_offsets, int64_t* v_of
 int gbs_mbatch_lu_rcond(gbs_mbatch* plan, const int* d_items, int64_t n_items, double* d_a, int* d_piv,
                         double* d_rhs, double* d_rcond, int* d_info, void* stream);
 int gbs_mbatch_ir(gbs_mbatch* plan, const int* d_items, int64_t n_items, const double* d_a, float* d_work, int* d_piv,
-                  const double* d_rhs, double* d_x, double tol, int max_iter, int* d_status, void* stream);
+                  const double* d_rhs, double* d_x, double tol, int max_iter, int factored, int* d_status,
+                  void* stream);
+int gbs_mbatch_gmres_ir(gbs_mbatch* plan, const int* d_items, int64_t n_items, const double* d_a, float* d_work,
+                        int* d_piv, const double* d_rhs, double* d_x, double tol, int max_outer, int restart,
+                        int factored, int* d_status, int* d_inner, void* stream);
 int gbs_mbatch_features(gbs_mbatch* plan, const int* d_items, int64_t n_items, const double* d_a, float* d_features,
                         void* stream);
 int gbs_router_feature_count(void);
@@ -350,7 +366,7 @@ int gbs_mlp_train_step(gbs_mlp* mlp, const float* d_x, const float* d_t, int cou
 int gbs_mlp_fit(gbs_mlp* mlp, const float* d_x, const float* d_t, int count, int epochs, int batch, float lr,
                 uint64_t seed, double* final_loss);
 int gbs_mlp_predict(const gbs_mlp* mlp, const float* d_x, int count, float* d_y, void* stream);
-int gbs_router_route(const float* d_pred, int count, float threshold, int* d_tier, void* stream);
+int gbs_router_route(const float* d_pred, int count, float t_ir, float t_gmres, int* d_tier, void* stream);
 
 /* ------------------------------------------------------------------ tracing
  * The reference has no runtime tracing (bench/BenchTimer.h times whole calls

@@ -134,11 +134,13 @@ def test_router_trains_and_beats_always_fp64():
     assert np.median(err) < 1.0          # within a decade of the method's own estimate
     # routed solve on fresh systems
     mt, At, Bt, _ = R.generate(400, seed=12, nmin=32, nmax=160)
-    tier = r.route(r.predict(R.features(mt, At))).cpu().numpy()
-    Xr, stats = R.solve_with_fallback(mt, At, Bt, np.nonzero(tier == 1)[0])
+    tier = r.route(r.predict(R.features(mt, At)))
+    Xr, stats = R.solve_tiers(mt, At, Bt, tier)
     errs = R.backward_errors(mt, At, Xr, Bt)
     assert (errs <= 1e-13).all()
-    assert stats["fp32_attempts"] > 0 and stats["fp32_failed"] <= 0.2 * stats["fp32_attempts"]
+    assert stats["ir_routed"] > 0 and stats["ir_failed"] <= 0.2 * stats["ir_routed"]
+    assert stats["gmres_routed"] > 0 and stats["gmres_failed"] <= 0.5 * stats["gmres_routed"]
+    assert stats["fp64_solves"] < mt.count
     # save / load round trip
     import tempfile, os
     path = os.path.join(tempfile.mkdtemp(), "router.json")
@@ -163,7 +165,36 @@ def test_mbatch_subset_calls_touch_only_their_items():
         assert torch.equal(f[i], F[i]) if i in sel else bool((f[i] == 7.0).all()), i
     x32, st = R.solve_fp32_ir(mb, A, B, items=sel, X=B.clone())
     st = st.cpu().numpy()
-    assert set(np.nonzero(st != -2)[0]) == set(sel)
+    assert set(np.nonzero(st != R.NOT_ATTEMPTED)[0]) == set(sel)
     for i in range(mb.count):
-        if st[i] == -2 or st[i] == -1:
+        if st[i] < 0:
             assert torch.equal(mb.vector(x32, i), mb.vector(B, i)), i
+
+
+def test_mbatch_gmres_ir_extends_the_fp32_tier():
+    """Systems FP32 + classic refinement mostly cannot solve (kappa 1e7.5..1e9)
+    reach the bound with GMRES-IR on the same FP32 factors."""
+    mb, A, B, logk = R.generate(150, seed=31, nmin=32, nmax=300, logk=(7.5, 9.0))
+    ws = R.Fp32Work(mb)
+    X = B.clone()
+    R.solve_fp32_ir(mb, A, B, X=X, ws=ws)
+    st_ir = ws.status.cpu().numpy().copy()
+    retry = torch.nonzero(ws.status == -1).flatten().to(torch.int32)
+    assert retry.numel() > 0.5 * mb.count
+    R.solve_fp32_gmres(mb, A, B, items=retry, X=X, ws=ws, factored=True)
+    st = ws.status.cpu().numpy()
+    inner = ws.inner.cpu().numpy()
+    done = st >= 0
+    assert done[st_ir == -1].mean() > 0.6, (done[st_ir == -1].mean(), inner[st_ir == -1])
+    errs = R.backward_errors(mb, A, X, B)
+    assert (errs[done] <= 1e-13).all()
+    for i in np.nonzero(~done)[0]:
+        assert torch.equal(mb.vector(X, i), mb.vector(B, i)), i
+
+
+def test_cascade_meets_the_bound_everywhere():
+    mb, A, B, _ = R.generate(200, seed=32, nmin=32, nmax=256)
+    X, stats = R.solve_cascade(mb, A, B)
+    errs = R.backward_errors(mb, A, X, B)
+    assert (errs <= 1e-13).all(), (errs.max(), stats)
+    assert stats["ir_converged"] > 0 and stats["gmres_converged"] > 0
