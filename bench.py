@@ -69,7 +69,8 @@ def args_parse():
     p.add_argument("--config", default="lu8192", choices=["lu8192", "llt16384", "batched", "router", "mbatch"],
                    help="lu8192 is the headline workload; the others are the LLT kappa sweep, the batched "
                         "small systems and the learned router")
-    p.add_argument("--train-labels", type=int, default=200000, help="router: training systems (rcond labels)")
+    p.add_argument("--train-labels", type=int, default=1000000, help="router: training systems (rcond labels)")
+    p.add_argument("--save-router", default="", help="router: write the trained network here (JSON)")
     p.add_argument("--count", type=int, default=20000, help="mbatch: systems of the router workload (n 32..512)")
     return p.parse_args()
 
@@ -580,8 +581,10 @@ def run_router(args):
     feats, labs = [], []
     t_gen = t_lab = t_feat = 0.0
     chunk = 20000
+    pool = R.HaarPool(16, torch.Generator(device="cuda").manual_seed(99))
     for c0 in range(0, ntrain, chunk):
-        (mb, A, _, _), dt = R.timed(lambda: R.generate(min(chunk, ntrain - c0), seed=1000 + c0, nmin=32, nmax=512))
+        (mb, A, _, _), dt = R.timed(lambda: R.generate(min(chunk, ntrain - c0), seed=1000 + c0, nmin=32, nmax=512,
+                                                       pool=pool))
         t_gen += dt
         y, dt = R.timed(lambda: R.labels(mb, A))
         labs.append(y)
@@ -592,8 +595,11 @@ def run_router(args):
         del A, mb
     Ftr = torch.cat(feats).contiguous()
     Ytr = torch.cat(labs).contiguous()
+    del pool
     r = R.Router(seed=1)
     (loss, t_fit) = R.timed(lambda: r.fit(Ftr, Ytr, epochs=12, batch=2048, lr=2e-3))
+    if args.save_router:
+        r.save(args.save_router)
     mt, At, Bt, logk = R.generate(20000, seed=7, nmin=32, nmax=512)
     from eigen_gb300 import _lib
     Lb = _lib.lib()

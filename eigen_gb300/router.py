@@ -124,10 +124,31 @@ def haar(k, n, generator):
     return q
 
 
-def generate(count, seed, nmin=32, nmax=512, logk=(1.0, 12.0)):
+class HaarPool:
+    """k Haar matrices per size, drawn once; ``draw`` composes one of them with
+    a random signed permutation (Q P is Haar-distributed when Q is), so a large
+    training set costs one n^3 product per system instead of two QRs."""
+
+    def __init__(self, k, generator):
+        self.k = k
+        self.g = generator
+        self.pool = {}
+
+    def draw(self, count, n):
+        import torch
+        if n not in self.pool:
+            self.pool[n] = haar(self.k, n, self.g)
+        q = self.pool[n][torch.randint(0, self.k, (count,), device="cuda", generator=self.g)]
+        perm = torch.argsort(torch.rand(count, n, device="cuda", generator=self.g), dim=1)
+        sign = torch.where(torch.rand(count, n, device="cuda", generator=self.g) < 0.5, -1.0, 1.0).to(q.dtype)
+        return torch.gather(q, 2, perm[:, None, :].expand(count, n, n)) * sign[:, None, :]
+
+
+def generate(count, seed, nmin=32, nmax=512, logk=(1.0, 12.0), pool=None):
     """A = U diag(s) V^T with Haar-random orthogonal U, V and s log-spaced
-    from 1 to 1/kappa, log10(kappa) uniform in logk; b iid N(0, 1).
-    Returns (batch, packed A, packed b, log10 kappa)."""
+    from 1 to 1/kappa, log10(kappa) uniform in logk; b iid N(0, 1).  With a
+    HaarPool, U and V come from it (training sets); otherwise each is a fresh
+    Haar matrix.  Returns (batch, packed A, packed b, log10 kappa)."""
     import torch
     rng = np.random.default_rng(seed)
     sizes = rng.integers(nmin, nmax + 1, count).astype(np.int32)
@@ -142,8 +163,8 @@ def generate(count, seed, nmin=32, nmax=512, logk=(1.0, 12.0)):
         idx = np.nonzero(sizes == n)[0]
         for c0 in range(0, len(idx), 256):
             sel = idx[c0:c0 + 256]
-            u = haar(len(sel), n, g)
-            v = haar(len(sel), n, g)
+            u = pool.draw(len(sel), n) if pool else haar(len(sel), n, g)
+            v = pool.draw(len(sel), n) if pool else haar(len(sel), n, g)
             lk = torch.as_tensor(logkappa[sel], dtype=torch.float64, device="cuda")
             t = torch.linspace(0, 1, n, dtype=torch.float64, device="cuda")
             s = torch.pow(10.0, -lk[:, None] * t[None, :])
@@ -238,6 +259,16 @@ class Router:
         with open(path, "w") as f:
             json.dump({"in_dim": feature_count(), "width": 64, "t_ir": self.t_ir, "t_gmres": self.t_gmres,
                        "label_scale": LABEL_SCALE, "params": self.params().tolist()}, f)
+
+    @classmethod
+    def pretrained(cls):
+        """The network shipped with the package: trained on 1,000,000 systems
+        of the n 32..512, log10 kappa 1..12 distribution with rcond labels
+        from gbs_mbatch_lu_rcond (bench.py --config router --save-router)."""
+        import os
+        r = cls()
+        r.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "router_weights.json"))
+        return r
 
     def load(self, path):
         with open(path) as f:

@@ -198,3 +198,18 @@ def test_cascade_meets_the_bound_everywhere():
     errs = R.backward_errors(mb, A, X, B)
     assert (errs <= 1e-13).all(), (errs.max(), stats)
     assert stats["ir_converged"] > 0 and stats["gmres_converged"] > 0
+
+
+def test_pretrained_router_routes_fresh_systems():
+    """The shipped network (1M rcond labels) on fresh systems of its
+    distribution: within half a decade of rcond's estimate, few refinement
+    failures, every result within the bound."""
+    r = R.Router.pretrained()
+    mt, At, Bt, _ = R.generate(300, seed=41, nmin=32, nmax=512)
+    err = (r.predict(R.features(mt, At)) - R.labels(mt, At)).abs().cpu().numpy()
+    assert np.median(err) < 0.6
+    X, stats = R.route_and_solve(r, mt, At, Bt)
+    assert (R.backward_errors(mt, At, X, Bt) <= 1e-13).all()
+    routed = stats["ir_routed"] + stats["gmres_routed"]
+    assert routed > 0.3 * mt.count
+    assert stats["ir_failed"] + stats["gmres_failed"] <= 0.05 * routed
