@@ -6,6 +6,7 @@
 #include "dense_driver.cuh"
 #include "dense_kernels.cuh"
 #include "gbs_profile.cuh"
+#include "panel_cluster.cuh"
 
 namespace gbs {
 
@@ -36,10 +37,73 @@ static int panel_capacity()
   return cap;
 }
 
+// Largest cluster (power of two, <= 16) the device schedules for this kernel.
+template <typename T, int RPT>
+static int cluster_panel_limit()
+{
+  static int lim = -1;
+  if (lim < 0) {
+    lim = 0;
+    const void* k = (const void*)panel_lu_cluster_kernel<T, kPanelNB, RPT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) cudaGetLastError();
+    for (int c = kMaxPanelCluster; c >= 1 && lim == 0; c /= 2) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(kClusterPanelThreads);
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters > 0) lim = c;
+      else cudaGetLastError();
+    }
+  }
+  return lim;
+}
+
+template <typename T, int RPT>
+static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr,
+                                DeviceStatus* st, int C)
+{
+  PhaseScope ps(s, PH_PANEL, (double)m * nbc * nbc, sizeof(T) * 2.0 * m * nbc);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kClusterPanelThreads);
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st));
+  return GBS_SUCCESS;
+}
+
+// The panel on one cluster when its rows fit (one row per thread, two for
+// FP32), else on the cooperative grid kernel.
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
                         DeviceStatus* st)
 {
+  {
+    constexpr int rpt_max = sizeof(T) == 8 ? 1 : 2;
+    int C = 1;
+    while (C * kClusterPanelThreads < m && C < kMaxPanelCluster) C *= 2;
+    const int rpt = C * kClusterPanelThreads >= m ? 1 : 2;
+    if (rpt <= rpt_max && C * kClusterPanelThreads * rpt >= m) {
+      const int lim = rpt == 1 ? cluster_panel_limit<T, 1>() : cluster_panel_limit<T, rpt_max>();
+      if (C <= lim) {
+        if (rpt == 1) return launch_cluster_panel<T, 1>(s, a, lda, m, nbc, k0, tr, st, C);
+        return launch_cluster_panel<T, rpt_max>(s, a, lda, m, nbc, k0, tr, st, C);
+      }
+    }
+  }
   // rows per thread: smallest power of two that keeps the grid co-resident
   // and below one CTA per SM (fewer CTAs make the per-column barrier cheaper)
   const int sms = device_sm_count();
