@@ -297,6 +297,18 @@ __global__ void laswp_gather_kernel(T* __restrict__ a, int64_t lda, const int* _
 }
 
 template <typename T>
+int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, int c1, int c2, int c3)
+{
+  const int nc = (c1 - c0) + (c3 - c2);
+  if (nc <= 0) return GBS_SUCCESS;
+  PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * 2 * kPanelNB);
+  const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
+  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map, c0, c1, c2, c3);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+template <typename T>
 int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0, int i1, int c0, int c1, int c2,
                         int c3, DevBuf& map)
 {
@@ -306,7 +318,7 @@ int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0
     gbs_set_last_message("laswp_gather: at most 128 interchanges per call");
     return GBS_INVALID_ARGUMENT;
   }
-  GBS_TRY(map.reserve(sizeof(int) * 520));
+  GBS_TRY(map.reserve(sizeof(int) * kLaswpMapInts));
   PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * (i1 - i0));
   laswp_map_kernel<<<1, 32, 0, s>>>(tr, i0, i1, map.as<int>());
   count_launch();
@@ -334,10 +346,14 @@ int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, Dev
   for (int k = 0; k < size; k += kPanelNB) {
     const int kb = std::min(kPanelNB, size - k);
     T* Akk = dA + (int64_t)k * lda + k;
-    GBS_TRY(panel_factor<T>(s, Akk, lda, m - k, kb, k, dTr + k, scratch, dSt));
-    // apply the panel's interchanges to A_0 (left) and A_2 (right)
+    const int* map = nullptr;
+    GBS_TRY(panel_factor<T>(s, Akk, lda, m - k, kb, k, dTr + k, scratch, dSt, &map));
+    // apply the panel's interchanges to A_0 (left) and A_2 (right): one gather
+    // of the panel's row map, or the interchanges in order
     const int left = k, right0 = k + kb, nright = n - right0;
-    if (left + nright > 0) {
+    if (map) {
+      GBS_TRY(laswp_map_apply<T>(s, dA, lda, map, 0, left, right0, n));
+    } else if (left + nright > 0) {
       PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)(left + nright) * kb);
       laswp_kernel<T><<<ceil_div(left + nright, 128), 128, 0, s>>>(dA, lda, dTr, k, k + kb, 0, left, right0, n, 0);
       GBS_CUDA_TRY(cudaGetLastError());
@@ -646,7 +662,8 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
   template int gemm_sub_device<T>(cudaStream_t, int, int, int, int, const T*, int64_t, int64_t, const T*, int64_t, \
                                   int64_t, T*, int64_t);                                                       \
   template int trsm_lunit_wide<T>(cudaStream_t, int, int, const T*, int64_t, T*, int64_t);                     \
-  template int laswp_gather_device<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int, int, int, DevBuf&);
+  template int laswp_gather_device<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int, int, int, DevBuf&); \
+  template int laswp_map_apply<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int);
 
 GBS_INSTANTIATE(double)
 GBS_INSTANTIATE(float)

@@ -70,10 +70,19 @@ int read_status(const DeviceStatus* d_st, DeviceStatus* h_st, cudaStream_t s);
 constexpr int kPanelNB = 32;   // columns factored per panel launch
 
 // Unblocked partial-pivoting LU of the m x nbc panel at `a` (nbc <= kPanelNB);
-// writes absolute pivot rows k0 + p into tr[0..nbc).  Cooperative launch.
+// writes absolute pivot rows k0 + p into tr[0..nbc).  With map_out, may also
+// leave the interchanges as a device row map for laswp_map_apply (*map_out
+// is null when it did not).
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                 DeviceStatus* st);
+                 DeviceStatus* st, const int** map_out = nullptr);
+
+constexpr int kLaswpMapInts = 520;     // count, 256 target rows, 256 source rows (+ pad)
+
+// Applies a row map (as written by laswp_map_kernel or the cluster panel) to
+// the columns [c0, c1) and [c2, c3) of A, all SMs.
+template <typename T>
+int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, int c1, int c2, int c3);
 
 template <typename T>
 int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, DeviceStatus* dSt, DevBuf& scratch);

@@ -152,14 +152,44 @@ __global__ void row_abs_sum_kernel(int n, const double* __restrict__ A, int64_t 
 }
 
 // W32 = fp32(R / s_c), s_c = max_i |R(i,c)| (1 when zero); W packed n x nrhs
+// W = R / s_c in FP32; with perm, rows are gathered: W(i) = R(perm[i]) / s_c
+// (the row interchanges of P A = L U applied on the way)
 __global__ void scale_to_f32_kernel(int n, int nrhs, const double* __restrict__ R, int64_t ldr,
-                                    const double* __restrict__ scale, float* __restrict__ W)
+                                    const double* __restrict__ scale, float* __restrict__ W,
+                                    const int* __restrict__ perm)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * nrhs) return;
   const int row = (int)(t % n), c = (int)(t / n);
   const double s = scale[c] > 0.0 ? scale[c] : 1.0;
-  W[t] = (float)(R[(int64_t)c * ldr + row] / s);
+  W[t] = (float)(R[(int64_t)c * ldr + (perm ? perm[row] : row)] / s);
+}
+
+// perm = the row order of P from the transpositions tr[0..n) (applied in
+// order to the identity, PermutationMatrix.h:82-88): x = P b is x(i) = b(perm[i]).
+// One CTA; the index array lives in shared memory, one warp applies the swaps.
+__global__ void perm_from_transpositions_kernel(int n, const int* __restrict__ tr, int* __restrict__ perm)
+{
+  extern __shared__ int sp[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    for (int k0 = 0; k0 < n; k0 += 32) {
+      const int pl = k0 + lane < n ? tr[k0 + lane] : 0;
+      const int cnt = min(32, n - k0);
+      for (int q = 0; q < cnt; ++q) {
+        const int p = __shfl_sync(0xffffffffu, pl, q);
+        if (lane == 0 && p != k0 + q) {
+          const int t = sp[k0 + q];
+          sp[k0 + q] = sp[p];
+          sp[p] = t;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
 }
 
 // X = init ? s_c W : X + s_c W   (FP64)
@@ -252,7 +282,7 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
 // ------------------------------------------------------------------ workspace pool
 struct MixedWork {
   cudaStream_t stream = nullptr;
-  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef;
+  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm;
   SolveWork sw;
   TcWorkspace tc;
   HostBuf hstats;
@@ -292,6 +322,7 @@ static int tc_kind(int tier)
 
 // ------------------------------------------------------------------ factorizations
 constexpr int kMixedNB = 128;
+constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
                 TcWorkspace& tcw, SolveWork& sw, DevBuf& map)
@@ -302,8 +333,10 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
     for (int j = k; j < k + kb; j += kPanelNB) {
       const int jb = std::min(kPanelNB, k + kb - j);
       float* Ajj = A + (int64_t)j * lda + j;
-      GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st));
-      GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, k, j, j + jb, k + kb, map));
+      const int* pmap = nullptr;
+      GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap));
+      if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, j + jb, n));
+      else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, 0, j, j + jb, n, map));
       const int rest = k + kb - (j + jb);
       if (rest > 0) {
         float* A12 = A + (int64_t)(j + jb) * lda + j;
@@ -317,7 +350,6 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
           GBS_TRY(tc_gemm_sub(s, kind, rows, rest, jb, Ajj + jb, 1, lda, A12, 1, lda, A12 + jb, lda, 0, st, tcw));
       }
     }
-    GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, k, k + kb, 0, k, k + kb, n, map));
     const int nr = n - k - kb;
     if (nr > 0) {
       float* Akk = A + (int64_t)k * lda + k;
@@ -385,10 +417,17 @@ struct Precond {
   float* F;
   const int* tr;
   const float* d;
+  const int* perm;    // LU: row order of P, applied when the right-hand side is converted (may be null)
 };
 
+// W <- M^-1 W.  LU with perm: W was gathered by perm on conversion, so only
+// the two triangular solves remain.
 static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, SolveWork& sw)
 {
+  if (M.kind == 0 && M.perm) {
+    GBS_TRY(tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 1, 0, 1, W, M.n, sw));
+    return tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, 0, 0, W, M.n, sw);
+  }
   if (M.kind == 0) return lu_solve_device<float>(s, M.n, nrhs, M.F, M.n, M.tr, W, M.n, 0, sw);
   const int64_t tot = (int64_t)M.n * nrhs;
   count_launch();
@@ -456,7 +495,7 @@ static int precond_f64(cudaStream_t s, const Precond& M, const double* Y, double
   count_launch();
   col_absmax3_kernel<<<dim3(nrhs, 1), 256, 0, s>>>(n, nrhs, Y, n, Y, n, Y, n, sc);
   count_launch();
-  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, Y, n, sc, w.w32.as<float>());
+  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, Y, n, sc, w.w32.as<float>(), M.perm);
   GBS_CUDA_TRY(cudaGetLastError());
   GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
   count_launch();
@@ -597,7 +636,8 @@ static int refine(cudaStream_t s, const Problem& P, const Precond& M, bool use_g
       double* sc = w.stats.as<double>();
       const int64_t tot = (int64_t)n * nrhs;
       count_launch();
-      scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.r.as<double>(), n, sc, w.w32.as<float>());
+      scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, w.r.as<double>(), n, sc, w.w32.as<float>(),
+                                                          M.perm);
       GBS_CUDA_TRY(cudaGetLastError());
       GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
       count_launch();
@@ -642,7 +682,7 @@ static int initial_solve(cudaStream_t s, const Problem& P, const Precond& M, Mix
   count_launch();
   col_absmax3_kernel<<<dim3(nrhs, 1), 256, 0, s>>>(n, nrhs, P.B, P.ldb, P.B, P.ldb, P.B, P.ldb, sc);
   count_launch();
-  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, P.B, P.ldb, sc, w.w32.as<float>());
+  scale_to_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(n, nrhs, P.B, P.ldb, sc, w.w32.as<float>(), M.perm);
   GBS_CUDA_TRY(cudaGetLastError());
   GBS_TRY(precond_apply(s, M, w.w32.as<float>(), nrhs, w.sw));
   count_launch();
@@ -709,7 +749,17 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {
-      Precond M{0, n, w.a32.as<float>(), w.tr.as<int>(), nullptr};
+      const int* perm = nullptr;
+      if (n <= kPermSmemMax) {
+        GBS_TRY(w.perm.reserve(sizeof(int) * (size_t)n));
+        GBS_CUDA_TRY(cudaFuncSetAttribute(perm_from_transpositions_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(sizeof(int) * kPermSmemMax)));
+        PhaseScope ps(s, PH_LASWP, 0.0, 8.0 * n);
+        perm_from_transpositions_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, w.tr.as<int>(), w.perm.as<int>());
+        GBS_CUDA_TRY(cudaGetLastError());
+        perm = w.perm.as<int>();
+      }
+      Precond M{0, n, w.a32.as<float>(), w.tr.as<int>(), nullptr, perm};
       GBS_TRY(initial_solve(s, P, M, w));
       const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
       out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
@@ -792,7 +842,7 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
         sigma = sigma > 0 ? sigma * 10.0 : 8.0 * uf;
         continue;
       }
-      Precond M{1, n, w.a32.as<float>(), nullptr, w.d32.as<float>()};
+      Precond M{1, n, w.a32.as<float>(), nullptr, w.d32.as<float>(), nullptr};
       GBS_TRY(initial_solve(s, P, M, w));
       const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
       out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;

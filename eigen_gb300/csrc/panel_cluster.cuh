@@ -35,12 +35,16 @@ struct ClusterPanelShared {
   T wval[kClusterPanelThreads / 32];
   int widx[kClusterPanelThreads / 32];
   int win, piv, wrank;
+  int spiv[NB];         // the panel's pivots (rows relative to the panel)
 };
 
+// a: the panel (m rows, nbc <= NB columns) at row and column k0 of its
+// matrix.  map (may be null): the panel's interchanges as a row map (count,
+// 256 target rows, 256 source rows; absolute rows) for laswp_gather_kernel.
 template <typename T, int NB, int RPT>
 __global__ void __launch_bounds__(kClusterPanelThreads)
 panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, int* __restrict__ tr,
-                        DeviceStatus* st)
+                        DeviceStatus* st, int* __restrict__ map)
 {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
@@ -131,6 +135,7 @@ panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, 
     const int p = sh.piv;
     const T piv = sh.u[j];
     const bool nz = (piv != T(0));   // biggest_in_corner != 0 (NaN counts as nonzero)
+    if (tid == 0) sh.spiv[j] = p;
     if (rank == 0 && tid == 0) {
       tr[j] = k0 + p;
       if (nz && p != j) st->nb_transpositions += 1;
@@ -165,6 +170,29 @@ panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, 
 #pragma unroll
       for (int c = 0; c < NB; ++c)
         if (c < nbc) a[(int64_t)c * lda + r] = v[q][c];
+    }
+  }
+
+  // the panel's interchanges as a row map for laswp_gather_kernel: targets
+  // are the panel's rows and the pivot rows below them; the source of a target
+  // runs the transpositions backwards (the row that ends up there).  Unused
+  // slots repeat target 0, so the map always has 2 NB entries.
+  if (map && rank == 0) {
+    __syncthreads();
+    if (tid < 2 * NB) {
+      int row = -1;
+      if (tid < nbc) row = tid;
+      else if (tid >= NB && tid - NB < nbc && sh.spiv[tid - NB] >= nbc) row = sh.spiv[tid - NB];
+      if (row < 0) row = 0;
+      int pos = row;
+      for (int jj = nbc - 1; jj >= 0; --jj) {
+        const int pj = sh.spiv[jj];
+        if (pos == jj) pos = pj;
+        else if (pos == pj) pos = jj;
+      }
+      map[1 + tid] = k0 + row;
+      map[257 + tid] = k0 + pos;
+      if (tid == 0) map[0] = 2 * NB;
     }
   }
   cluster.sync();      // no CTA leaves while another may still read its shared memory

@@ -2,5 +2,6 @@
 #include "panel_lu_impl.cuh"
 
 namespace gbs {
-template int panel_factor<double>(cudaStream_t, double*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*);
+template int panel_factor<double>(cudaStream_t, double*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
+                                  const int**);
 }  // namespace gbs

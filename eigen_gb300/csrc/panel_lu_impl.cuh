@@ -67,7 +67,7 @@ static int cluster_panel_limit()
 
 template <typename T, int RPT>
 static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr,
-                                DeviceStatus* st, int C)
+                                DeviceStatus* st, int C, int* map)
 {
   PhaseScope ps(s, PH_PANEL, (double)m * nbc * nbc, sizeof(T) * 2.0 * m * nbc);
   cudaLaunchConfig_t cfg = {};
@@ -81,16 +81,19 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st));
+  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st, map));
   return GBS_SUCCESS;
 }
 
 // The panel on one cluster when its rows fit (one row per thread, two for
-// FP32), else on the cooperative grid kernel.
+// FP32), else on the cooperative grid kernel.  With map_out, the cluster
+// kernel also leaves the panel's interchanges as a row map in scratch and
+// *map_out points to it (null after the cooperative kernel).
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                        DeviceStatus* st)
+                        DeviceStatus* st, const int** map_out)
 {
+  if (map_out) *map_out = nullptr;
   {
     constexpr int rpt_max = sizeof(T) == 8 ? 1 : 2;
     int C = 1;
@@ -99,8 +102,14 @@ int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int*
     if (rpt <= rpt_max && C * kClusterPanelThreads * rpt >= m) {
       const int lim = rpt == 1 ? cluster_panel_limit<T, 1>() : cluster_panel_limit<T, rpt_max>();
       if (C <= lim) {
-        if (rpt == 1) return launch_cluster_panel<T, 1>(s, a, lda, m, nbc, k0, tr, st, C);
-        return launch_cluster_panel<T, rpt_max>(s, a, lda, m, nbc, k0, tr, st, C);
+        int* map = nullptr;
+        if (map_out) {
+          GBS_TRY(scratch.reserve(sizeof(int) * kLaswpMapInts));
+          map = scratch.as<int>();
+          *map_out = map;
+        }
+        if (rpt == 1) return launch_cluster_panel<T, 1>(s, a, lda, m, nbc, k0, tr, st, C, map);
+        return launch_cluster_panel<T, rpt_max>(s, a, lda, m, nbc, k0, tr, st, C, map);
       }
     }
   }
