@@ -464,12 +464,19 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
   const int nblk = ceil_div(n, NB);
   GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
   const int grid = std::min(nblk, 2 * device_sm_count());
+  constexpr size_t smem = trsm_persistent_smem<T, NB, RC>();
+  static bool attr = false;
+  if (!attr) {
+    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_persistent_kernel<T, NB, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    attr = true;
+  }
   for (int c0 = 0; c0 < nrhs; c0 += RC) {
     const int nc = std::min(RC, nrhs - c0);
     GBS_CUDA_TRY(cudaMemsetAsync(w.flags.p, 0, sizeof(int) * (size_t)(nblk + 2), s));
     PhaseScope ps(s, PH_TRI_SOLVE, (double)n * n * nc, sizeof(T) * (0.5 * (double)n * n + 2.0 * n * nc));
-    trsm_persistent_kernel<T, NB, RC><<<grid, RC * 32, 0, s>>>(n, nc, tri, rs, cs, forward, unit,
-                                                                B + (int64_t)c0 * ldb, ldb, w.flags.as<int>());
+    trsm_persistent_kernel<T, NB, RC><<<grid, RC * 32, smem, s>>>(n, nc, tri, rs, cs, forward, unit,
+                                                                   B + (int64_t)c0 * ldb, ldb, w.flags.as<int>());
     GBS_CUDA_TRY(cudaGetLastError());
   }
   return GBS_SUCCESS;

@@ -411,29 +411,51 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
 
 // --------------------------------------------------------------------- persistent TRSM
 // op(Tri) X = B for up to RC right-hand sides in ONE launch.  Block rows of NB
-// are handed out in solve order by a ticket counter; block i waits (bounded)
-// on the ready flag of every earlier block j, subtracts op(Tri)(i,j) x_j, then
-// solves its diagonal block with one warp per right-hand side (rows spread
-// over lanes, shuffles carry x_r), writes x_i and raises its flag.  A CTA
-// only takes a ticket while running and only waits on lower tickets, so the
-// lowest unfinished block always progresses.  work: [0] ticket counter,
-// [1] timeout flag, [2..] one ready flag per block; zeroed before launch.
+// are handed out in solve order by a ticket counter.  Block i subtracts
+// op(Tri)(i,j) x_j for every earlier block j: it waits (bounded) for the first
+// block it still needs, takes every further block already finished (up to
+// SUPER of them) and applies them as one streamed super-tile (all loads of the
+// tile issued before the barrier), so a block that fell behind catches up in a
+// few passes.  It then solves its diagonal block with one warp per right-hand
+// side (rows spread over lanes, shuffles carry x_r), writes x_i and raises its
+// flag.  A CTA only takes a ticket while running and only waits on lower
+// tickets, so the lowest unfinished block always progresses.  work: [0] ticket
+// counter, [1] timeout flag, [2..] one ready flag per block; zeroed before
+// launch.  Dynamic shared memory: trsm_persistent_smem<T, NB, RC>().
+template <typename T, int NB>
+struct TrsmSuper { static constexpr int value = 256 / NB; };
+
+template <typename T, int NB, int RC>
+constexpr size_t trsm_persistent_smem()
+{
+  constexpr int K = TrsmSuper<T, NB>::value * NB;
+  return sizeof(T) * ((size_t)K * (NB + 1) + (size_t)K * RC + (size_t)NB * RC + (size_t)NB * (NB + 1));
+}
+
 template <typename T, int NB, int RC>
 __global__ void __launch_bounds__(RC * 32)
 trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, int64_t cs, int forward, int unit,
                        T* B, int64_t ldb, int* work)
 {
   constexpr int PER = NB / 32;
+  constexpr int SUPER = TrsmSuper<T, NB>::value;
+  constexpr int KMAX = SUPER * NB;
+  constexpr int G = (RC * 32) / NB;          // right-hand-side groups of the accumulation
+  constexpr int CPT = RC / G;                // right-hand sides per thread
+  static_assert(G * NB == RC * 32 && CPT * G == RC, "thread mapping");
   const int nblk = (n + NB - 1) / NB;
   int* counter = work;
   int* err = work + 1;
   int* flags = work + 2;
-  __shared__ T sT[NB][NB + 1];
-  __shared__ T sY[NB][RC];
-  __shared__ T sX[NB][RC];
-  __shared__ int s_t, s_ok;
+  extern __shared__ __align__(16) unsigned char trsm_sm[];
+  T(*sT)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(trsm_sm);                         // [KMAX][NB+1], k-major
+  T(*sX)[RC] = reinterpret_cast<T(*)[RC]>(trsm_sm + sizeof(T) * KMAX * (NB + 1));     // [KMAX][RC]
+  T(*sY)[RC] = reinterpret_cast<T(*)[RC]>(trsm_sm + sizeof(T) * (KMAX * (NB + 1) + KMAX * RC));
+  T(*sD)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(trsm_sm + sizeof(T) * (KMAX * (NB + 1) + KMAX * RC + NB * RC));
+  __shared__ int s_t, s_ok, s_hi;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
+  const int ar = tid % NB, ag = tid / NB;     // accumulation: row, right-hand-side group
   const bool unit_rows_fast = (rs == 1);
   for (;;) {
     if (tid == 0) s_t = atomicAdd(counter, 1);
@@ -442,19 +464,45 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
     if (t >= nblk) break;
     const int bi = forward ? t : nblk - 1 - t;
     const int i0 = bi * NB, ni = min(NB, n - i0);
-    for (int e = tid; e < NB * RC; e += nthr) {
-      const int r = e % NB, c = e / NB;
-      sY[r][c] = (r < ni && c < nrhs) ? B[(int64_t)c * ldb + i0 + r] : T(0);
+    // the diagonal tile and the first off-diagonal tile do not depend on any
+    // other block: load them before waiting
+    for (int e = tid; e < NB * NB; e += nthr) {
+      int r, c;
+      if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
+      sD[r][c] = (r < ni && c < ni) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(i0 + c) * cs] : T(0);
     }
-    for (int tt = 0; tt < t; ++tt) {
-      const int bj = forward ? tt : nblk - 1 - tt;
-      const int j0 = bj * NB, nj = min(NB, n - j0);
+    T acc[CPT];
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int c = ag + q * G;
+      acc[q] = (ar < ni && c < nrhs) ? B[(int64_t)c * ldb + i0 + ar] : T(0);
+    }
+    int done = 0;
+    int loaded = 0;                            // T tiles of blocks done..loaded-1 already in sT
+    auto load_tiles = [&](int from, int to) {  // op(Tri) columns of blocks [from, to) into sT rows (b - done) * NB
+      const int K = (to - from) * NB, base = (from - done) * NB;
+#pragma unroll 8
+      for (int e = tid; e < NB * K; e += nthr) {
+        int r, kk;
+        if (unit_rows_fast) { r = e % NB; kk = e / NB; } else { kk = e % K; r = e / K; }
+        const int jb = from + kk / NB, w = kk % NB;
+        const int bj = forward ? jb : nblk - 1 - jb;
+        const int col = bj * NB + w;
+        sT[base + kk][r] = (r < ni && col < n) ? tri[(int64_t)(i0 + r) * rs + (int64_t)col * cs] : T(0);
+      }
+    };
+    while (done < t) {
+      if (loaded == done) {                    // prefetch the tile the wait below is for
+        load_tiles(done, done + 1);
+        loaded = done + 1;
+      }
       if (tid == 0) {
         int ok = 1;
-        if (ld_acquire_u32((const unsigned int*)&flags[bj]) == 0u) {
+        const int bj0 = forward ? done : nblk - 1 - done;
+        if (ld_acquire_u32((const unsigned int*)&flags[bj0]) == 0u) {
           const uint64_t t0 = globaltimer_ns();
           unsigned int spins = 0;
-          while (ld_acquire_u32((const unsigned int*)&flags[bj]) == 0u) {
+          while (ld_acquire_u32((const unsigned int*)&flags[bj0]) == 0u) {
             if ((++spins & 63u) == 0 &&
                 (ld_volatile_i32(err) || globaltimer_ns() - t0 > kSpinDeadlineNs)) {
               atomicExch(err, 1);
@@ -464,34 +512,46 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
             __nanosleep(32);
           }
         }
+        int hi = done + 1;
+        while (ok && hi < t && hi - done < SUPER &&
+               ld_acquire_u32((const unsigned int*)&flags[forward ? hi : nblk - 1 - hi]) != 0u)
+          ++hi;
         s_ok = ok;
+        s_hi = hi;
       }
       __syncthreads();
       if (!s_ok) return;
-      for (int e = tid; e < NB * RC; e += nthr) {
-        const int r = e % NB, c = e / NB;
-        sX[r][c] = (r < nj && c < nrhs) ? __ldcg(&B[(int64_t)c * ldb + j0 + r]) : T(0);
-      }
-      for (int e = tid; e < NB * NB; e += nthr) {
-        int r, c;
-        if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
-        sT[r][c] = (r < ni && c < nj) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(j0 + c) * cs] : T(0);
+      const int hi = s_hi;
+      const int K = (hi - done) * NB;
+      if (hi > loaded) load_tiles(loaded, hi);
+#pragma unroll 4
+      for (int e = tid; e < K * RC; e += nthr) {
+        const int kk = e % K, c = e / K;
+        const int jb = done + kk / NB, w = kk % NB;
+        const int bj = forward ? jb : nblk - 1 - jb;
+        const int col = bj * NB + w;
+        sX[kk][c] = (col < n && c < nrhs) ? __ldcg(&B[(int64_t)c * ldb + col]) : T(0);
       }
       __syncthreads();
-      for (int e = tid; e < NB * RC; e += nthr) {
-        const int r = e % NB, c = e / NB;
-        T acc = T(0);
+      for (int k0 = 0; k0 < K; k0 += NB) {   // one partial sum per tile: rounding grows with NB, not with n
+        T part[CPT];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) part[q] = T(0);
 #pragma unroll 8
-        for (int k = 0; k < NB; ++k) acc = fma(sT[r][k], sX[k][c], acc);
-        sY[r][c] -= acc;
+        for (int kk = k0; kk < k0 + NB; ++kk) {
+          const T tv = sT[kk][ar];
+#pragma unroll
+          for (int q = 0; q < CPT; ++q) part[q] = fma(tv, sX[kk][ag + q * G], part[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) acc[q] -= part[q];
       }
       __syncthreads();
+      done = hi;
+      loaded = hi;
     }
-    for (int e = tid; e < NB * NB; e += nthr) {
-      int r, c;
-      if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
-      sT[r][c] = (r < ni && c < ni) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(i0 + c) * cs] : T(0);
-    }
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) sY[ar][ag + q * G] = acc[q];
     __syncthreads();
     if (warp < nrhs) {
       T yl[PER];
@@ -502,11 +562,11 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
         for (int r = 0; r < NB; ++r) {
           if (r < ni) {
             T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
-            if (!unit) xr = xr / sT[r][r];
+            if (!unit) xr = xr / sD[r][r];
 #pragma unroll
             for (int p = 0; p < PER; ++p) {
               const int row = lane + 32 * p;
-              if (row > r && row < ni) yl[p] = fma(-sT[row][r], xr, yl[p]);
+              if (row > r && row < ni) yl[p] = fma(-sD[row][r], xr, yl[p]);
             }
             if (lane == r % 32) yl[r / 32] = xr;
           }
@@ -516,11 +576,11 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
         for (int r = NB - 1; r >= 0; --r) {
           if (r < ni) {
             T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
-            if (!unit) xr = xr / sT[r][r];
+            if (!unit) xr = xr / sD[r][r];
 #pragma unroll
             for (int p = 0; p < PER; ++p) {
               const int row = lane + 32 * p;
-              if (row < r) yl[p] = fma(-sT[row][r], xr, yl[p]);
+              if (row < r) yl[p] = fma(-sD[row][r], xr, yl[p]);
             }
             if (lane == r % 32) yl[r / 32] = xr;
           }
@@ -539,6 +599,7 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
     if (tid == 0) atomicExch(&flags[bi], 1);
   }
 }
+
 
 // --------------------------------------------------------------------- norms
 __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v)

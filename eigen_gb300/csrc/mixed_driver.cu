@@ -4,8 +4,10 @@
 // Factorizations (FP32 working storage, tensor-core updates in the tier's
 // precision: BF16 / FP16 / TF32 / 3xTF32):
 //   mixed_getrf  P A = L U: 128-column outer panels, each factored 32 columns
-//                at a time by the cooperative register kernel; inner and outer
-//                trailing updates A22 -= A21 A12 on tensor cores
+//                at a time by the panel kernel; the outer U12 = L11^-1 A12 as
+//                A12 - (I - L11^-1) A12 on tensor cores (explicit inverse of
+//                the unit-lower diagonal block); inner and outer trailing
+//                updates A22 -= A21 A12 on tensor cores
 //   mixed_potrf  D A D + sigma I = L L^T, D = diag(A)^-1/2 (unit diagonal, so
 //                FP16 cannot overflow), the reference's block size; diagonal
 //                blocks and TRSM on FP32 cores, SYRK on tensor cores
@@ -282,7 +284,7 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
 // ------------------------------------------------------------------ workspace pool
 struct MixedWork {
   cudaStream_t stream = nullptr;
-  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm;
+  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv;
   SolveWork sw;
   TcWorkspace tc;
   HostBuf hstats;
@@ -322,12 +324,52 @@ static int tc_kind(int tier)
 
 // ------------------------------------------------------------------ factorizations
 constexpr int kMixedNB = 128;
+
+// M = I - L^-1 for the unit-lower nb x nb block L (nb <= kMixedNB, ld), M
+// column-major with ld kMixedNB.  Row-by-row substitution on the identity,
+// X(i, j) = -sum_{j <= k < i} L(i, k) X(k, j), four threads per column each
+// summing a quarter of the k range.  One CTA of 4 kMixedNB threads.
+constexpr size_t kInvSmem = sizeof(float) * 2 * kMixedNB * (kMixedNB + 1) + sizeof(float) * 4 * kMixedNB;
+
+__global__ void __launch_bounds__(4 * kMixedNB)
+unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M)
+{
+  extern __shared__ float sm[];
+  float(*Ls)[kMixedNB + 1] = reinterpret_cast<float(*)[kMixedNB + 1]>(sm);
+  float(*X)[kMixedNB + 1] = reinterpret_cast<float(*)[kMixedNB + 1]>(sm + kMixedNB * (kMixedNB + 1));
+  float* red = sm + 2 * kMixedNB * (kMixedNB + 1);             // [4][kMixedNB]
+  const int tid = threadIdx.x, j = tid % kMixedNB, q = tid / kMixedNB;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    const int r = e % nb, c = e / nb;
+    Ls[r][c] = L[(int64_t)c * ld + r];
+  }
+  __syncthreads();
+  for (int i = 0; i < nb; ++i) {
+    float s = 0.f;
+    if (j < i)
+      for (int k = j + q; k < i; k += 4) s = fmaf(Ls[i][k], X[k][j], s);
+    red[q * kMixedNB + j] = s;
+    __syncthreads();
+    if (q == 0 && j < nb) {
+      const float t = (red[j] + red[kMixedNB + j]) + (red[2 * kMixedNB + j] + red[3 * kMixedNB + j]);
+      X[i][j] = i == j ? 1.f : (i > j ? -t : 0.f);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
+    const int r = e % kMixedNB, c = e / kMixedNB;
+    M[e] = (r < nb && c < nb && r > c) ? -X[r][c] : 0.f;
+  }
+}
 constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
-                TcWorkspace& tcw, SolveWork& sw, DevBuf& map)
+                TcWorkspace& tcw, SolveWork& sw, DevBuf& map, DevBuf& minv)
 {
   (void)sw;
+  GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
+  GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kInvSmem));
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
     for (int j = k; j < k + kb; j += kPanelNB) {
@@ -354,7 +396,13 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
     if (nr > 0) {
       float* Akk = A + (int64_t)k * lda + k;
       float* A12 = A + (int64_t)(k + kb) * lda + k;
-      GBS_TRY(trsm_lunit_wide<float>(s, kb, nr, Akk, lda, A12, lda));
+      {
+        PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * kb / 3.0, sizeof(float) * 2.0 * kb * kb);
+        unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, kb, minv.as<float>());
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
+      // U12 = A12 - (I - L11^-1) A12 (the GEMM packs its operands first, so C may alias B)
+      GBS_TRY(tc_gemm_sub(s, kind, kb, nr, kb, minv.as<float>(), 1, kMixedNB, A12, 1, lda, A12, lda, 0, st, tcw));
       GBS_TRY(tc_gemm_sub(s, kind, nr, nr, kb, Akk + kb, 1, lda, A12, 1, lda, A12 + kb, lda, 0, st, tcw));
     }
   }
@@ -745,7 +793,7 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
       GBS_CUDA_TRY(cudaGetLastError());
     }
     GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.sw,
-                        w.map));
+                        w.map, w.minv));
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {
