@@ -72,10 +72,12 @@ constexpr int kPanelNB = 32;   // columns factored per panel launch
 // Unblocked partial-pivoting LU of the m x nbc panel at `a` (nbc <= kPanelNB);
 // writes absolute pivot rows k0 + p into tr[0..nbc).  With map_out, may also
 // leave the interchanges as a device row map for laswp_map_apply (*map_out
-// is null when it did not).
+// is null when it did not).  With trsm_done, may also interchange the
+// trsm_cols columns right of the panel and solve their top rows with L11
+// (*trsm_done says whether it did; the caller then skips those columns).
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                 DeviceStatus* st, const int** map_out = nullptr);
+                 DeviceStatus* st, const int** map_out = nullptr, int trsm_cols = 0, bool* trsm_done = nullptr);
 
 constexpr int kLaswpMapInts = 520;     // count, 256 target rows, 256 source rows (+ pad)
 

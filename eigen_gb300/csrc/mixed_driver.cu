@@ -324,35 +324,65 @@ static int tc_kind(int tier)
 
 // ------------------------------------------------------------------ factorizations
 constexpr int kMixedNB = 128;
+constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 // M = I - L^-1 for the unit-lower nb x nb block L (nb <= kMixedNB, ld), M
-// column-major with ld kMixedNB.  Row-by-row substitution on the identity,
-// X(i, j) = -sum_{j <= k < i} L(i, k) X(k, j), four threads per column each
-// summing a quarter of the k range.  One CTA of 4 kMixedNB threads.
-constexpr size_t kInvSmem = sizeof(float) * 2 * kMixedNB * (kMixedNB + 1) + sizeof(float) * 4 * kMixedNB;
+// column-major with ld kMixedNB.  Blocked by 32: the four diagonal blocks are
+// inverted at once (row-by-row substitution on the identity, four threads per
+// column), then block row i of X = L^-1 follows from
+// X(i,j) = -X(i,i) sum_{j <= k < i} L(i,k) X(k,j), one block row at a time.
+// One CTA of 4 kMixedNB threads; rows and columns beyond nb are the identity.
+constexpr int kInvLd = kMixedNB + 1;
+constexpr size_t kInvSmem = sizeof(float) * (2 * kMixedNB * kInvLd + 32 * kInvLd + 4 * kMixedNB);
 
 __global__ void __launch_bounds__(4 * kMixedNB)
 unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M)
 {
   extern __shared__ float sm[];
-  float(*Ls)[kMixedNB + 1] = reinterpret_cast<float(*)[kMixedNB + 1]>(sm);
-  float(*X)[kMixedNB + 1] = reinterpret_cast<float(*)[kMixedNB + 1]>(sm + kMixedNB * (kMixedNB + 1));
-  float* red = sm + 2 * kMixedNB * (kMixedNB + 1);             // [4][kMixedNB]
-  const int tid = threadIdx.x, j = tid % kMixedNB, q = tid / kMixedNB;
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    const int r = e % nb, c = e / nb;
-    Ls[r][c] = L[(int64_t)c * ld + r];
+  float(*Ls)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm);
+  float(*X)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
+  float(*Tb)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + 2 * kMixedNB * kInvLd);   // [32][..]
+  float* red = sm + 2 * kMixedNB * kInvLd + 32 * kInvLd;                                  // [4 kMixedNB]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
+    const int r = e % kMixedNB, c = e / kMixedNB;
+    Ls[r][c] = (r < nb && c < nb) ? L[(int64_t)c * ld + r] : (r == c ? 1.f : 0.f);
+    X[r][c] = 0.f;
   }
   __syncthreads();
-  for (int i = 0; i < nb; ++i) {
-    float s = 0.f;
-    if (j < i)
-      for (int k = j + q; k < i; k += 4) s = fmaf(Ls[i][k], X[k][j], s);
-    red[q * kMixedNB + j] = s;
+  // diagonal 32 x 32 blocks: thread = (block b, column j, quarter q)
+  {
+    const int b = tid / 128, loc = tid % 128, j = loc % 32, q = loc / 32;
+    const int o = 32 * b;
+    for (int i = 0; i < 32; ++i) {
+      float s = 0.f;
+      for (int k = j + q; k < i; k += 4) s = fmaf(Ls[o + i][o + k], X[o + k][o + j], s);
+      red[tid] = s;
+      __syncthreads();
+      if (q == 0) {
+        const float t = (red[b * 128 + j] + red[b * 128 + 32 + j]) + (red[b * 128 + 64 + j] + red[b * 128 + 96 + j]);
+        X[o + i][o + j] = i == j ? 1.f : (i > j ? -t : 0.f);
+      }
+      __syncthreads();
+    }
+  }
+  // off-diagonal blocks, block row by block row
+  for (int bi = 1; bi < kMixedNB / 32; ++bi) {
+    const int oi = 32 * bi;
+    // Tb(:, 32 bj + c) = sum_{bj <= bk < bi} L(bi, bk) X(bk, bj)
+    for (int e = tid; e < 32 * 32 * bi; e += blockDim.x) {
+      const int r = e % 32, cc = e / 32, bj = cc / 32, c = cc % 32;
+      float s = 0.f;
+      for (int k = 32 * bj; k < oi; ++k) s = fmaf(Ls[oi + r][k], X[k][32 * bj + c], s);
+      Tb[r][cc] = s;
+    }
     __syncthreads();
-    if (q == 0 && j < nb) {
-      const float t = (red[j] + red[kMixedNB + j]) + (red[2 * kMixedNB + j] + red[3 * kMixedNB + j]);
-      X[i][j] = i == j ? 1.f : (i > j ? -t : 0.f);
+    // X(bi, bj) = -X(bi, bi) Tb
+    for (int e = tid; e < 32 * 32 * bi; e += blockDim.x) {
+      const int r = e % 32, cc = e / 32;
+      float s = 0.f;
+      for (int k = 0; k <= r; ++k) s = fmaf(X[oi + r][oi + k], Tb[k][cc], s);
+      X[oi + r][cc] = -s;
     }
     __syncthreads();
   }
@@ -361,7 +391,6 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
     M[e] = (r < nb && c < nb && r > c) ? -X[r][c] : 0.f;
   }
 }
-constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
                 TcWorkspace& tcw, SolveWork& sw, DevBuf& map, DevBuf& minv)
@@ -375,14 +404,16 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
     for (int j = k; j < k + kb; j += kPanelNB) {
       const int jb = std::min(kPanelNB, k + kb - j);
       float* Ajj = A + (int64_t)j * lda + j;
-      const int* pmap = nullptr;
-      GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap));
-      if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, j + jb, n));
-      else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, 0, j, j + jb, n, map));
       const int rest = k + kb - (j + jb);
+      const int* pmap = nullptr;
+      bool fused = false;       // interchanges + U12 of the block's columns right of the panel done in the panel
+      GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap, rest, &fused));
+      if (pmap && fused) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, k + kb, n));
+      else if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, j + jb, n));
+      else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, 0, j, j + jb, n, map));
       if (rest > 0) {
         float* A12 = A + (int64_t)(j + jb) * lda + j;
-        {
+        if (!fused) {
           PhaseScope ps(s, PH_TRSM_LU, (double)jb * jb * rest, 8.0 * jb * rest);
           trsm_lunit_kernel<float, kPanelNB><<<cdiv(rest, 128), 128, 0, s>>>(Ajj, lda, jb, A12, lda, rest);
           GBS_CUDA_TRY(cudaGetLastError());

@@ -3,5 +3,5 @@
 
 namespace gbs {
 template int panel_factor<float>(cudaStream_t, float*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
-                                  const int**);
+                                  const int**, int, bool*);
 }  // namespace gbs

@@ -3,5 +3,5 @@
 
 namespace gbs {
 template int panel_factor<double>(cudaStream_t, double*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
-                                  const int**);
+                                  const int**, int, bool*);
 }  // namespace gbs

@@ -67,7 +67,7 @@ static int cluster_panel_limit()
 
 template <typename T, int RPT>
 static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr,
-                                DeviceStatus* st, int C, int* map)
+                                DeviceStatus* st, int C, int* map, int trsm_cols)
 {
   PhaseScope ps(s, PH_PANEL, (double)m * nbc * nbc, sizeof(T) * 2.0 * m * nbc);
   cudaLaunchConfig_t cfg = {};
@@ -81,19 +81,23 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st, map));
+  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st, map,
+                                  trsm_cols));
   return GBS_SUCCESS;
 }
 
 // The panel on one cluster when its rows fit (one row per thread, two for
 // FP32), else on the cooperative grid kernel.  With map_out, the cluster
 // kernel also leaves the panel's interchanges as a row map in scratch and
-// *map_out points to it (null after the cooperative kernel).
+// *map_out points to it (null after the cooperative kernel).  trsm_cols > 0
+// asks the cluster kernel to also interchange and solve (U12 = L11^-1 A12) the
+// trsm_cols columns right of the panel; *trsm_done says whether it did.
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                        DeviceStatus* st, const int** map_out)
+                        DeviceStatus* st, const int** map_out, int trsm_cols, bool* trsm_done)
 {
   if (map_out) *map_out = nullptr;
+  if (trsm_done) *trsm_done = false;
   {
     constexpr int rpt_max = sizeof(T) == 8 ? 1 : 2;
     int C = 1;
@@ -108,8 +112,10 @@ int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int*
           map = scratch.as<int>();
           *map_out = map;
         }
-        if (rpt == 1) return launch_cluster_panel<T, 1>(s, a, lda, m, nbc, k0, tr, st, C, map);
-        return launch_cluster_panel<T, rpt_max>(s, a, lda, m, nbc, k0, tr, st, C, map);
+        const int tc = (trsm_done && nbc == kPanelNB) ? trsm_cols : 0;
+        if (trsm_done) *trsm_done = tc > 0;
+        if (rpt == 1) return launch_cluster_panel<T, 1>(s, a, lda, m, nbc, k0, tr, st, C, map, tc);
+        return launch_cluster_panel<T, rpt_max>(s, a, lda, m, nbc, k0, tr, st, C, map, tc);
       }
     }
   }

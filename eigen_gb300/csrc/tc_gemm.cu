@@ -339,11 +339,12 @@ __device__ __forceinline__ float round_tf32(float x)
 // converted to the tier's type; x3 tiers write three K-blocks per row with
 // `pattern` selecting hi (0) or lo (1) for each block.  Zero padding up to Kp.
 template <typename TO>
-__global__ void pack_kmajor_kernel(const float* __restrict__ src, int64_t rs, int64_t cs, int R, int K, int Kp,
-                                   TO* __restrict__ out, int64_t ldk, int kind, int pattern)
+__device__ __forceinline__ void pack_kmajor_tile(const float* __restrict__ src, int64_t rs, int64_t cs, int R, int K,
+                                                 int Kp, TO* __restrict__ out, int64_t ldk, int kind, int pattern)
 {
   __shared__ float tile[32][33];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  if (r0 >= R) return;                       // uniform over the CTA
   const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
   const int nblk = (kind == TC_TF32X3) ? 3 : 1;
   const int Kt = K * nblk;
@@ -382,6 +383,22 @@ __global__ void pack_kmajor_kernel(const float* __restrict__ src, int64_t rs, in
     else if (kind == TC_BF16) ((__nv_bfloat16*)out)[(int64_t)r * ldk + k] = __float2bfloat16_rn(o);
     else ((__half*)out)[(int64_t)r * ldk + k] = __float2half_rn(o);
   }
+}
+
+struct PackJob {
+  const float* src;
+  int64_t rs, cs;
+  int R;
+  int pattern;
+};
+
+// Both operands in one launch: blockIdx.z picks A (0) or B (1).
+template <typename TO>
+__global__ void pack_pair_kernel(PackJob a, PackJob b, int K, int Kp, TO* __restrict__ outa, TO* __restrict__ outb,
+                                 int64_t ldk, int kind)
+{
+  if (blockIdx.z == 0) pack_kmajor_tile<TO>(a.src, a.rs, a.cs, a.R, K, Kp, outa, ldk, kind, a.pattern);
+  else pack_kmajor_tile<TO>(b.src, b.rs, b.cs, b.R, K, Kp, outb, ldk, kind, b.pattern);
 }
 
 // ------------------------------------------------------------------ host
@@ -442,17 +459,15 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   {
     PhaseScope ps(s, PH_COPY, 0.0, (double)(M + N) * (4.0 * K + esize * (double)Kp));
     dim3 blk(32, 8);
-    dim3 ga((Kp + 31) / 32, (M + 31) / 32), gb((Kp + 31) / 32, (N + 31) / 32);
+    dim3 grid((Kp + 31) / 32, (std::max(M, N) + 31) / 32, 2);
     // x3 pattern bits (block -> lo?): A = [hi, hi, lo] (0b100), B = [hi, lo, hi] (0b010)
-    if (esize == 4) {
-      pack_kmajor_kernel<float><<<ga, blk, 0, s>>>(A, a_rs, a_cs, M, K, Kp, ws.ak.as<float>(), ldk, kind, 4);
-      pack_kmajor_kernel<float><<<gb, blk, 0, s>>>(B, b_cs, b_rs, N, K, Kp, ws.bk.as<float>(), ldk, kind, 2);
-    } else {
-      pack_kmajor_kernel<uint16_t><<<ga, blk, 0, s>>>(A, a_rs, a_cs, M, K, Kp, ws.ak.as<uint16_t>(), ldk, kind, 0);
-      pack_kmajor_kernel<uint16_t><<<gb, blk, 0, s>>>(B, b_cs, b_rs, N, K, Kp, ws.bk.as<uint16_t>(), ldk, kind, 0);
-    }
+    const PackJob ja{A, a_rs, a_cs, M, esize == 4 ? 4 : 0}, jb{B, b_cs, b_rs, N, esize == 4 ? 2 : 0};
+    if (esize == 4)
+      pack_pair_kernel<float><<<grid, blk, 0, s>>>(ja, jb, K, Kp, ws.ak.as<float>(), ws.bk.as<float>(), ldk, kind);
+    else
+      pack_pair_kernel<uint16_t><<<grid, blk, 0, s>>>(ja, jb, K, Kp, ws.ak.as<uint16_t>(), ws.bk.as<uint16_t>(), ldk,
+                                                      kind);
     GBS_CUDA_TRY(cudaGetLastError());
-    count_launch();
   }
   CUtensorMap tmA, tmB;
   GBS_TRY(make_tmap(&tmA, ws.ak.p, esize, M, Kp, ldk, BM));
