@@ -66,7 +66,7 @@ def args_parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
                    help="factor one seeded n x n system on the chosen path and exit (small ncu captures)")
-    p.add_argument("--config", default="lu8192", choices=["lu8192", "llt16384", "batched", "router", "mbatch"],
+    p.add_argument("--config", default="lu8192", choices=["lu8192", "llt512", "llt16384", "batched", "router", "mbatch"],
                    help="lu8192 is the headline workload; the others are the LLT kappa sweep, the batched "
                         "small systems and the learned router")
     p.add_argument("--train-labels", type=int, default=1000000, help="router: training systems (rcond labels)")
@@ -445,6 +445,76 @@ def _event_time(fn, reps=1):
     return out, e0.elapsed_time(e1) / 1e3 / reps
 
 
+def run_llt512(args):
+    """LLT<MatrixXd> n = 512: A = G G^T / 512 + I (G iid N(0,1)), one RHS,
+    plain FP64 through the LLT object on device buffers (and end to end from
+    host buffers), parity against the oracle on the same input, the oracle
+    port timed beside it on the host cores."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    import eigen_gb300 as gb
+    n = 512
+    G = O.gauss(42, n, n)
+    a = np.asfortranarray(G @ G.T / n + np.eye(n))
+    b = O.gauss(43, n, 1)
+    A = torch.from_numpy(a).cuda().t().contiguous().t()
+    Bd = torch.from_numpy(b).cuda().t().contiguous().t()
+    llt = gb.LLT(dtype=np.float64)
+    L = gb.lib()
+    stream = torch.cuda.current_stream()
+    L.gbs_llt_set_stream(llt._h, C.c_void_p(stream.cuda_stream))
+
+    def step():
+        llt.compute(A)
+        return llt.solve(Bd)
+    for _ in range(args.warmup):
+        step()
+    l0 = L.gbs_kernel_launch_count()
+    X, dt = _event_time(step, reps=args.steps)
+    launches = (L.gbs_kernel_launch_count() - l0) // args.steps
+    L.gbs_profile_reset()
+    L.gbs_profile_enable(1)
+    step()
+    torch.cuda.synchronize()
+    phases = {k: round(v["ms"], 4) for k, v in collect_phases(L, 1).items()}
+    L.gbs_profile_enable(0)
+    x = X.cpu().numpy()
+    f_o, _ = O.llt(a)
+    x_o = O.llt_solve(f_o, b)
+    fwd = float(np.linalg.norm(x - x_o) / np.linalg.norm(x_o))
+    be = O.backward_error(a, x, b)
+    # end to end: host buffers through the same object (copies inside the timed region)
+    llt_h = gb.LLT(dtype=np.float64)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        llt_h.compute(a)
+        llt_h.solve(b)
+    e2e = args.steps / (time.perf_counter() - t0)
+    # CPU oracle (the reference algorithm, same input)
+    t0 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        f_c, _ = O.llt(a)
+        O.llt_solve(f_c, b)
+    cpu = reps / (time.perf_counter() - t0)
+    flops = n ** 3 / 3 + 2 * n * n
+    line = {"metric": METRIC, "value": 1.0 / dt, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: A = G G^T / 512 + I, G iid N(0,1) (seed 42), b (seed 43)",
+            "config": {"workload": "LLT<MatrixXd> n=512 + solve 1 RHS, plain FP64", "n": n, "nrhs": 1},
+            "tflops": flops / dt / 1e12, "backward_error": be, "forward_diff_vs_oracle": fwd,
+            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": 8 * (n * n + n),
+                    "d2h_bytes_per_step": 8 * n, "api": "gbs_llt_compute / gbs_llt_solve on host buffers"},
+            "cpu_baseline": {"value": cpu, "unit": "solves/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": f"{reps} factor + solve of the same system"},
+            "gpu_launches": int(launches), "phases_ms_per_step": phases,
+            "roofline": {"bound": "latency", "note": "n = 512: 4.5e7 flop per solve, far below any roofline"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_llt16384(args):
     """LLT n = 16384, A = Q diag(sigma) Q^T (Haar Q, sigma log-spaced 1..kappa),
     4 right-hand sides, kappa in {1e2, 1e6, 1e10}: every tier's solves/s at
@@ -469,14 +539,21 @@ def run_llt16384(args):
         A = ((A + A.t()) / 2).contiguous().t()
         x64, _ = gb.solve_spd_mixed(A, B, tier="fp64")
         rows = {}
+        Lb = gb.lib()
         for tier in ("fp64", "tf32x3", "fp16", "bf16"):
             gb.solve_spd_mixed(A, B, tier=tier)
             (X, info), dt = _event_time(lambda: gb.solve_spd_mixed(A, B, tier=tier))
+            Lb.gbs_profile_reset()
+            Lb.gbs_profile_enable(1)
+            gb.solve_spd_mixed(A, B, tier=tier)
+            torch.cuda.synchronize()
+            phases = {k: round(v["ms"], 3) for k, v in collect_phases(Lb, 1).items()}
+            Lb.gbs_profile_enable(0)
             be = backward_error_gpu(A, X, B)
             fe = float(((X - x64).abs().amax(0) / x64.abs().amax(0)).max().item())
             rows[tier] = {"solves_per_s": 1.0 / dt if be <= BE_BAR else 0.0, "ms": 1e3 * dt,
                           "tflops": flops / dt / 1e12, "backward_error": be, "forward_error_vs_fp64": fe,
-                          "refine": info}
+                          "refine": info, "phases_ms": phases}
         fastest = max(rows, key=lambda t: rows[t]["solves_per_s"])
         per_kappa[f"{kappa:.0e}"] = {"tiers": rows, "fastest": fastest,
                                      "speedup_vs_fp64": rows[fastest]["solves_per_s"] / rows["fp64"]["solves_per_s"]}
@@ -700,7 +777,7 @@ def main():
     if args.factor_once:
         return factor_once(args)
     if args.impl == "ours" and args.config != "lu8192":
-        return {"llt16384": run_llt16384, "batched": run_batched, "router": run_router,
+        return {"llt512": run_llt512, "llt16384": run_llt16384, "batched": run_batched, "router": run_router,
                 "mbatch": run_mbatch}[args.config](args)
     if args.impl == "reference":
         return run_reference(args)

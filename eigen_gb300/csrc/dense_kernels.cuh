@@ -8,7 +8,7 @@
 //   trsm_lunit_kernel    A12 <- L11^{-1} A12, unit lower (PartialPivLU.h:490)
 //   gemm_sub_kernel      C -= op(A) op(B), optional lower-triangle-only mode for
 //                        SYRK (PartialPivLU.h:492, LLT.h:357)
-//   potrf_diag_kernel    left-looking Cholesky of one diagonal block (LLT.h:305-328)
+//   potrf_diag_kernel    Cholesky of one diagonal block (LLT.h:305-328), right-looking in smem
 //   trsm_rlt_kernel      A21 <- A21 L11^{-T} (LLT.h:356)
 //   trsm_persistent_kernel  whole triangular solve in one launch (LLT.h:499-505,
 //                        PartialPivLU.h:224-271, TriangularSolverMatrix.h)
@@ -312,11 +312,15 @@ gemm_sub_kernel(int M, int N, int K, const T* __restrict__ A, int64_t a_rs, int6
 }
 
 // --------------------------------------------------------------------- LLT diag
-// Left-looking Cholesky of the bs x bs diagonal block in shared memory,
-// exactly the order of LLT.h:305-328: x = a_kk - ||A10||^2, fail if x <= 0,
-// x = sqrt(x), A21 = (A21 - A20 A10^T) / x.  On failure writes k0 + k into
-// st->info and leaves later columns untouched (as the reference returns).
-// Only the lower triangle is read or written.  Dynamic smem: bs*(bs+1)*sizeof(T).
+// Cholesky of the bs x bs diagonal block in shared memory, the reference's
+// unblocked algorithm (LLT.h:305-328: x = a_kk - ||l_k||^2, fail if x <= 0,
+// x = sqrt(x), column divided by x) in right-looking order: after column k is
+// final its rank-1 update goes to the whole trailing triangle at once, so each
+// column costs three barriers and (bs - k)^2 / 2 independent FMAs spread over
+// the CTA.  On failure writes k0 + k into st->info and writes back only the
+// columns already final (the trailing columns in global memory were never
+// touched, as the reference's early return leaves them).  Only the lower
+// triangle is read or written.  Dynamic smem: bs*(bs+1)*sizeof(T).
 template <typename T>
 __global__ void __launch_bounds__(256)
 potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* st)
@@ -325,48 +329,46 @@ potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = (T*)smem_raw;
   const int ld = bs + 1;
-  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
-    int i = e % bs, j = e / bs;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < bs * bs; e += nt) {
+    const int i = e % bs, j = e / bs;
     if (i >= j) s[j * ld + i] = a[(int64_t)j * lda + i];
   }
   __syncthreads();
   __shared__ T s_x;
   __shared__ int s_fail;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k < bs; ++k) {
-    if (warp == 0) {
-      T acc = T(0);
-      for (int j = lane; j < k; j += 32) acc = fma(s[j * ld + k], s[j * ld + k], acc);
-      acc = warp_sum(acc);
-      if (lane == 0) {
-        T x = s[k * ld + k] - acc;
-        s_fail = !(x > T(0)) && !(x != x) ? 1 : 0;   // x <= 0 (a NaN does not fail, as in the reference)
-        s_x = x;
-      }
+    if (tid == 0) {
+      const T x = s[k * ld + k];
+      const int fail = !(x > T(0)) && !(x != x) ? 1 : 0;   // x <= 0 (a NaN does not fail, as in the reference)
+      s_fail = fail;
+      const T r = fail ? x : sqrt(x);
+      s_x = r;
+      if (!fail) s[k * ld + k] = r;
     }
     __syncthreads();
     if (s_fail) {
-      if (threadIdx.x == 0) st->info = k0 + k;
-      // write back the columns already final (0..k-1); column k.. untouched
-      for (int e = threadIdx.x; e < bs * k; e += blockDim.x) {
-        int i = e % bs, j = e / bs;
+      if (tid == 0) st->info = k0 + k;
+      for (int e = tid; e < bs * k; e += nt) {
+        const int i = e % bs, j = e / bs;
         if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
       }
       return;
     }
-    const T x = sqrt(s_x);
-    // rows i > k: one warp per row, dot product over j < k
-    for (int i = k + 1 + warp; i < bs; i += nw) {
-      T acc = T(0);
-      for (int j = lane; j < k; j += 32) acc = fma(s[j * ld + i], s[j * ld + k], acc);
-      acc = warp_sum(acc);
-      if (lane == 0) s[k * ld + i] = (s[k * ld + i] - acc) / x;
+    const T x = s_x;
+    for (int i = k + 1 + tid; i < bs; i += nt) s[k * ld + i] = s[k * ld + i] / x;
+    __syncthreads();
+    {
+      const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;   // warp per column, lanes down the rows
+      for (int j = k + 1 + w; j < bs; j += nw) {
+        const T ljk = s[k * ld + j];
+        for (int i = j + lane; i < bs; i += 32) s[j * ld + i] = fma(-s[k * ld + i], ljk, s[j * ld + i]);
+      }
     }
-    if (threadIdx.x == 0) s[k * ld + k] = x;
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
-    int i = e % bs, j = e / bs;
+  for (int e = tid; e < bs * bs; e += nt) {
+    const int i = e % bs, j = e / bs;
     if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
   }
 }
@@ -397,9 +399,16 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
   __syncthreads();
   const int t = threadIdx.x;
   for (int j = 0; j < bs; ++j) {
-    T s = sX[j * RT + t];
-    for (int l = 0; l < j; ++l) s = fma(-sX[l * RT + t], sL[j * ldL + l], s);
-    sX[j * RT + t] = s / sL[j * ldL + j];
+    T s0 = sX[j * RT + t], s1 = T(0), s2 = T(0), s3 = T(0);   // four chains: FMA latency, not issue, bounds this
+    int l = 0;
+    for (; l + 3 < j; l += 4) {
+      s0 = fma(-sX[l * RT + t], sL[j * ldL + l], s0);
+      s1 = fma(-sX[(l + 1) * RT + t], sL[j * ldL + l + 1], s1);
+      s2 = fma(-sX[(l + 2) * RT + t], sL[j * ldL + l + 2], s2);
+      s3 = fma(-sX[(l + 3) * RT + t], sL[j * ldL + l + 3], s3);
+    }
+    for (; l < j; ++l) s0 = fma(-sX[l * RT + t], sL[j * ldL + l], s0);
+    sX[j * RT + t] = ((s0 + s1) + (s2 + s3)) / sL[j * ldL + j];
   }
   __syncthreads();
   for (int e = threadIdx.x; e < bs * RT; e += RT) {
