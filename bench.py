@@ -49,7 +49,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Solves/s and TFLOP/s at ≤1e-13 backward err: mixed/batched vs plain FP64"
 BE_BAR = 1e-13
 # measured DRAM traffic / algorithmic bytes of a kernel (ncu captures, profiles/)
-TRAFFIC_OVER_ALGORITHMIC = {"gemm": 533.6 / 588.4}
+# DRAM traffic / algorithmic bytes of one launch, from the ncu captures summarised in profiles/
+TRAFFIC_OVER_ALGORITHMIC = {"gemm": 533.6 / 588.4, "tc_gemm": 237.2 / 289.5}
 
 
 def args_parse():
@@ -153,6 +154,15 @@ def max_over_ranks(world, v: float) -> float:
     t = torch.tensor([v], dtype=torch.float64, device="cuda")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def measured_hbm_gbs() -> float:
+    """HBM copy bandwidth of this machine's GB300 (MEASURED_PEAKS.json, written by the pool's own probe)."""
+    try:
+        with open(Path(__file__).resolve().parent / "MEASURED_PEAKS.json") as f:
+            return float(json.load(f)["hbm_gbs"])
+    except Exception:
+        return 6800.0
 
 
 def backward_error_gpu(A, X, B) -> float:
@@ -323,31 +333,43 @@ def run_ours(args):
                  "ms_per_step": 1e3 * pdt / args.plain_steps, "backward_error": pbe,
                  "tflops": lu_flops(n, nrhs) * world * args.plain_steps / pdt / 1e12}
 
-    # dominant kernel of the timed path
-    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else ("none", None)
-    roofline = None
-    if dom is not None:
-        achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12 if dom["ms"] else 0.0
-        if dom_name in ("tc_gemm",):
-            peak = gemm_peak(torch.float32, tf32=True)
-            roofline = {"bound": "tensor", "kernel": "tc_gemm_kernel (tcgen05 kind::tf32, trailing update)",
-                        "peak_source": "cuBLAS TF32 GEMM 8192^3 measured in this run"}
-        elif dom_name in ("gemm", "residual", "syrk"):
-            peak = gemm_peak(torch.float64)
-            roofline = {"bound": "fp64", "kernel": {"gemm": "gemm_sub_kernel<double> (trailing update)",
-                                                    "residual": "residual_partial_kernel (FP64 r = b - A x)",
-                                                    "syrk": "gemm_sub_kernel<double> lower (SYRK)"}[dom_name],
-                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 figure in "
-                                       "MEASURED_PEAKS.json)"}
+    # roofline of every phase, the dominant one first
+    hbm_peak = measured_hbm_gbs()
+    peaks = {}
+
+    def entry(name, ph):
+        t = ph["ms"] / 1e3
+        if name == "tc_gemm":
+            if "tf32" not in peaks:
+                peaks["tf32"] = gemm_peak(torch.float32, tf32=True)
+            e = {"bound": "tensor", "kernel": "tc_gemm_kernel (tcgen05 kind::tf32, 3xTF32 split)",
+                 "achieved": ph["flops"] / t / 1e12 if t else 0.0, "peak": peaks["tf32"], "unit": "TFLOP/s",
+                 "peak_source": "of measured: cuBLAS TF32 GEMM 8192^3 timed in this run"}
+        elif name in ("gemm", "syrk", "residual"):
+            if "fp64" not in peaks:
+                peaks["fp64"] = gemm_peak(torch.float64)
+            e = {"bound": "fp64", "kernel": {"gemm": "gemm_sub_kernel<double> (trailing update)",
+                                             "syrk": "gemm_sub_kernel<double> lower (SYRK)",
+                                             "residual": "mv_partial_kernel (FP64 r = b - A x)"}[name],
+                 "achieved": ph["flops"] / t / 1e12 if t else 0.0, "peak": peaks["fp64"], "unit": "TFLOP/s",
+                 "peak_source": "of measured: cuBLAS DGEMM 8192^3 timed in this run (FP64 has no entry in "
+                                "MEASURED_PEAKS.json)"}
         else:
-            peak = gemm_peak(torch.float64)
-            roofline = {"bound": "latency", "kernel": dom_name,
-                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
-        ratio = TRAFFIC_OVER_ALGORITHMIC.get(dom_name)
-        roofline.update({"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": (ratio * dom["bytes"] / max(dom["launches"], 1)) if ratio else None,
-                         "phase": dom_name, "share_of_step": dom["ms"] / (1e3 * dt / args.steps),
-                         "launches_per_step": dom["launches"]})
+            e = {"bound": "hbm", "kernel": name, "achieved": ph["bytes"] / t / 1e9 if t else 0.0, "peak": hbm_peak,
+                 "unit": "GB/s", "peak_source": "of measured: MEASURED_PEAKS.json hbm_gbs",
+                 "note": "latency-bound (barrier or dependency chain per column / block): the fraction shows "
+                         "the distance from the memory roof"}
+        e["frac"] = e["achieved"] / e["peak"] if e["peak"] else None
+        ratio = TRAFFIC_OVER_ALGORITHMIC.get(name)
+        e["traffic"] = (ratio * ph["bytes"] / max(ph["launches"], 1)) if ratio else None
+        e.update({"phase": name, "share_of_step": ph["ms"] / (1e3 * dt / args.steps),
+                  "launches_per_step": ph["launches"], "algorithmic_bytes_per_launch": ph["bytes"] / max(ph["launches"], 1),
+                  "algorithmic_flops_per_launch": ph["flops"] / max(ph["launches"], 1)})
+        return e
+
+    order = sorted(prof.items(), key=lambda kv: -kv[1]["ms"])
+    roofline = entry(*order[0]) if order else None
+    roofline_phases = [entry(k, v) for k, v in order[1:]]
 
     # end to end through the host-buffer C ABI
     e2e = None
@@ -399,7 +421,8 @@ def run_ours(args):
                            "l2": "inputs (512 MB) larger than L2 (129 MB); no flush needed"},
                 "tflops": lu_flops(n, nrhs) * value / 1e12, "backward_error": be, "refinement": refine,
                 "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "e2e": e2e, "roofline": roofline, "roofline_other_phases": roofline_phases, "cpu_baseline": cpu,
+                "clocks": clk,
                 "gpu_launches": int(launches), "phases_ms_per_step": {k: round(v["ms"], 3) for k, v in prof.items()}}
         print(json.dumps(line), flush=True)
     if world > 1:
