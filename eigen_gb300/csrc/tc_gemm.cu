@@ -27,6 +27,7 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BN = 256;
+constexpr int EPI_COLS = 64;                     // C columns per epilogue pass (loads in flight per lane)
 constexpr int ATOM = 128;                          // bytes of K per stage (one swizzle atom)
 constexpr int STAGES = 4;
 constexpr int NUM_THREADS = 192;
@@ -294,23 +295,34 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       const int row = tm * BM + 32 * q + lane;
       const bool row_ok = row < p.M;
       const uint32_t tbase = tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN);
-      for (int c = 0; c < BN; c += 16) {
-        float v[16];
-        tmem_ld16(tbase + (uint32_t)c, v);
-        const int col0 = tn * BN + c;
-        if (row_ok) {
-          float* cp = p.C + (int64_t)col0 * p.ldc + row;
-          float old[16];
+      // C -= acc in two halves of EPI_COLS columns: each lane first issues the
+      // loads of its row's EPI_COLS old values (one coalesced 128-byte line per
+      // column and warp), so the read-modify-write of C runs with many loads in
+      // flight instead of one chunk of 16 at a time
+      for (int h = 0; h < BN; h += EPI_COLS) {
+        float old[EPI_COLS];
+        const int colh = tn * BN + h;
+        float* cp = p.C + (int64_t)colh * p.ldc + row;
+        {
+          const float* lp = cp;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = col0 + j;
-            const bool ok = col < p.N && (!p.lower || row >= col);
-            old[j] = ok ? cp[(int64_t)j * p.ldc] : 0.f;
+          for (int j = 0; j < EPI_COLS; ++j) {
+            const int col = colh + j;
+            const bool ok = row_ok && col < p.N && (!p.lower || row >= col);
+            old[j] = ok ? *lp : 0.f;
+            lp += p.ldc;
           }
+        }
+#pragma unroll
+        for (int c = 0; c < EPI_COLS; c += 16) {
+          float v[16];
+          tmem_ld16(tbase + (uint32_t)(h + c), v);
+          float* sp = cp + (int64_t)c * p.ldc;
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int col = col0 + j;
-            if (col < p.N && (!p.lower || row >= col)) cp[(int64_t)j * p.ldc] = old[j] - v[j];
+            const int col = colh + c + j;
+            if (row_ok && col < p.N && (!p.lower || row >= col)) *sp = old[c + j] - v[j];
+            sp += p.ldc;
           }
         }
       }
