@@ -326,17 +326,18 @@ static int tc_kind(int tier)
 constexpr int kMixedNB = 128;
 constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
-// M = I - L^-1 for the unit-lower nb x nb block L (nb <= kMixedNB, ld), M
-// column-major with ld kMixedNB.  Blocked by 32: the four diagonal blocks are
-// inverted at once (row-by-row substitution on the identity, four threads per
-// column), then block row i of X = L^-1 follows from
-// X(i,j) = -X(i,i) sum_{j <= k < i} L(i,k) X(k,j), one block row at a time.
-// One CTA of 4 kMixedNB threads; rows and columns beyond nb are the identity.
+// M = I - L^-1 for the lower nb x nb block L (nb <= kMixedNB, ld; unit != 0:
+// unit diagonal, not read), M column-major with ld kMixedNB.  Blocked by 32:
+// the four diagonal blocks are inverted at once (row-by-row substitution on
+// the identity, four threads per column), then block row i of X = L^-1
+// follows from X(i,j) = -X(i,i) sum_{j <= k < i} L(i,k) X(k,j), one block row
+// at a time.  One CTA of 4 kMixedNB threads; rows and columns beyond nb are
+// the identity.
 constexpr int kInvLd = kMixedNB + 1;
 constexpr size_t kInvSmem = sizeof(float) * (2 * kMixedNB * kInvLd + 32 * kInvLd + 4 * kMixedNB);
 
 __global__ void __launch_bounds__(4 * kMixedNB)
-unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M)
+unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M, int unit)
 {
   extern __shared__ float sm[];
   float(*Ls)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm);
@@ -346,7 +347,7 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
   const int tid = threadIdx.x;
   for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
     const int r = e % kMixedNB, c = e / kMixedNB;
-    Ls[r][c] = (r < nb && c < nb) ? L[(int64_t)c * ld + r] : (r == c ? 1.f : 0.f);
+    Ls[r][c] = (r < nb && c < nb && (r != c || !unit)) ? L[(int64_t)c * ld + r] : (r == c ? 1.f : 0.f);
     X[r][c] = 0.f;
   }
   __syncthreads();
@@ -361,7 +362,7 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
       __syncthreads();
       if (q == 0) {
         const float t = (red[b * 128 + j] + red[b * 128 + 32 + j]) + (red[b * 128 + 64 + j] + red[b * 128 + 96 + j]);
-        X[o + i][o + j] = i == j ? 1.f : (i > j ? -t : 0.f);
+        X[o + i][o + j] = (i == j ? 1.f : (i > j ? -t : 0.f)) / Ls[o + i][o + i];
       }
       __syncthreads();
     }
@@ -388,7 +389,7 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
   }
   for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
     const int r = e % kMixedNB, c = e / kMixedNB;
-    M[e] = (r < nb && c < nb && r > c) ? -X[r][c] : 0.f;
+    M[e] = (r < nb && c < nb && r >= c) ? (r == c ? 1.f : 0.f) - X[r][c] : 0.f;
   }
 }
 
@@ -429,7 +430,7 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
       float* A12 = A + (int64_t)(k + kb) * lda + k;
       {
         PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * kb / 3.0, sizeof(float) * 2.0 * kb * kb);
-        unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, kb, minv.as<float>());
+        unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, kb, minv.as<float>(), 1);
         GBS_CUDA_TRY(cudaGetLastError());
       }
       // U12 = A12 - (I - L11^-1) A12 (the GEMM packs its operands first, so C may alias B)
@@ -442,8 +443,12 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
 
 // Cholesky of the lower triangle of As (FP32, ld = lda) with the reference's
 // block size; diagonal blocks and TRSM on FP32 cores, SYRK on tensor cores.
-int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st, int kind, TcWorkspace& tcw)
+int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st, int kind, TcWorkspace& tcw,
+                DevBuf& minv)
 {
+  GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
+  GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kInvSmem));
   static bool attr = false;
   const int max_bs = 128;
   if (!attr) {
@@ -465,7 +470,15 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
     }
     if (rs > 0) {
       float* A21 = Akk + b;
-      {
+      if (b <= kMixedNB) {
+        // A21 L11^-T = A21 - A21 (I - L11^-T): W = I - L11^-1, read transposed as the GEMM's B
+        {
+          PhaseScope ps(s, PH_TRSM_LLT, (double)b * b * b / 3.0, 8.0 * b * b);
+          unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, b, minv.as<float>(), 0);
+          GBS_CUDA_TRY(cudaGetLastError());
+        }
+        GBS_TRY(tc_gemm_sub(s, kind, rs, b, b, A21, 1, lda, minv.as<float>(), kMixedNB, 1, A21, lda, 0, st, tcw));
+      } else {
         PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, 8.0 * rs * b);
         trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64), s>>>(Akk, lda, b, A21,
                                                                                                    lda, rs, st);
@@ -913,7 +926,7 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
                                                                    w.a32.as<float>());
         GBS_CUDA_TRY(cudaGetLastError());
       }
-      GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc));
+      GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc, w.minv));
       DeviceStatus h;
       GBS_TRY(read_status(st, &h, s));
       out.shift = sigma;
