@@ -452,12 +452,12 @@ int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceSta
 // ------------------------------------------------------------------ solves
 template <typename T>
 int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
-                     T* B, int64_t ldb, SolveWork& w)
+                     T* B, int64_t ldb, SolveWork& w, const T* dinv)
 {
   if (n <= 0 || nrhs <= 0) return GBS_SUCCESS;
   // FP64: 32-row blocks keep the per-block DFMA work on the critical path
   // short; FP32: 64-row blocks.
-  constexpr int NB = sizeof(T) == 8 ? 32 : 64;
+  constexpr int NB = tri_solve_nb<T>();
   constexpr int RC = 16;
   const int64_t rs = trans ? ld : 1, cs = trans ? 1 : ld;   // op(Tri)(i,j) = tri[i*rs + j*cs]
   const int forward = (lower != 0) != (trans != 0);
@@ -476,7 +476,8 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
     GBS_CUDA_TRY(cudaMemsetAsync(w.flags.p, 0, sizeof(int) * (size_t)(nblk + 2), s));
     PhaseScope ps(s, PH_TRI_SOLVE, (double)n * n * nc, sizeof(T) * (0.5 * (double)n * n + 2.0 * n * nc));
     trsm_persistent_kernel<T, NB, RC><<<grid, RC * 32, smem, s>>>(n, nc, tri, rs, cs, forward, unit,
-                                                                   B + (int64_t)c0 * ldb, ldb, w.flags.as<int>());
+                                                                   B + (int64_t)c0 * ldb, ldb, w.flags.as<int>(),
+                                                                   dinv);
     GBS_CUDA_TRY(cudaGetLastError());
   }
   return GBS_SUCCESS;
@@ -657,7 +658,7 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
   template int getrf_device<T>(cudaStream_t, int, int, T*, int64_t, int*, DeviceStatus*, DevBuf&);               \
   template int potrf_device<T>(cudaStream_t, int, T*, int64_t, int, DeviceStatus*, DevBuf&);                     \
   template int tri_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, int, int, T*, int64_t,       \
-                                   SolveWork&);                                                              \
+                                   SolveWork&, const T*);                                                    \
   template int laswp_device<T>(cudaStream_t, T*, int64_t, int, const int*, int, int, int);                       \
   template int lu_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, const int*, T*, int64_t, int,       \
                                   SolveWork&);                                                               \

@@ -96,7 +96,11 @@ int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceSta
 // holds the factor; trans: solve with its transpose; unit: unit diagonal.
 template <typename T>
 int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
-                     T* B, int64_t ldb, SolveWork& w);
+                     T* B, int64_t ldb, SolveWork& w, const T* dinv = nullptr);
+
+// Block height of tri_solve_device's persistent kernel (its dinv blocks are NB x NB).
+template <typename T>
+constexpr int tri_solve_nb() { return sizeof(T) == 8 ? 32 : 64; }
 
 // Waits for the stream and reports GBS_TIMEOUT if a solve's wait expired.
 int solve_status(cudaStream_t s, SolveWork& w);

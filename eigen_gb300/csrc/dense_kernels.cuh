@@ -441,10 +441,14 @@ constexpr size_t trsm_persistent_smem()
   return sizeof(T) * ((size_t)K * (NB + 1) + (size_t)K * RC + (size_t)NB * RC + (size_t)NB * (NB + 1));
 }
 
+// dinv (may be null): the inverses of the diagonal blocks of op(Tri), block b
+// at dinv + b NB^2, NB x NB column-major (zero beyond the block's rows and
+// columns); with them a block's own step is X_b = Dinv_b Y_b, a product with
+// independent FMAs instead of an NB-step substitution.
 template <typename T, int NB, int RC>
 __global__ void __launch_bounds__(RC * 32)
 trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, int64_t cs, int forward, int unit,
-                       T* B, int64_t ldb, int* work)
+                       T* B, int64_t ldb, int* work, const T* __restrict__ dinv)
 {
   constexpr int PER = NB / 32;
   constexpr int SUPER = TrsmSuper<T, NB>::value;
@@ -473,12 +477,17 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
     if (t >= nblk) break;
     const int bi = forward ? t : nblk - 1 - t;
     const int i0 = bi * NB, ni = min(NB, n - i0);
-    // the diagonal tile and the first off-diagonal tile do not depend on any
-    // other block: load them before waiting
-    for (int e = tid; e < NB * NB; e += nthr) {
-      int r, c;
-      if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
-      sD[r][c] = (r < ni && c < ni) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(i0 + c) * cs] : T(0);
+    // the diagonal tile (or its inverse) and the first off-diagonal tile do
+    // not depend on any other block: load them before waiting
+    if (dinv) {
+      const T* db = dinv + (int64_t)bi * NB * NB;
+      for (int e = tid; e < NB * NB; e += nthr) sD[e % NB][e / NB] = db[e];
+    } else {
+      for (int e = tid; e < NB * NB; e += nthr) {
+        int r, c;
+        if (unit_rows_fast) { r = e % NB; c = e / NB; } else { c = e % NB; r = e / NB; }
+        sD[r][c] = (r < ni && c < ni) ? tri[(int64_t)(i0 + r) * rs + (int64_t)(i0 + c) * cs] : T(0);
+      }
     }
     T acc[CPT];
 #pragma unroll
@@ -561,6 +570,27 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
     }
 #pragma unroll
     for (int q = 0; q < CPT; ++q) sY[ar][ag + q * G] = acc[q];
+    if (dinv) {                                // X_b = Dinv_b Y_b
+      __syncthreads();
+      T out[CPT];
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) out[q] = T(0);
+#pragma unroll 8
+      for (int k = 0; k < NB; ++k) {
+        const T dv = sD[ar][k];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) out[q] = fma(dv, sY[k][ag + q * G], out[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) {
+        const int c = ag + q * G;
+        if (ar < ni && c < nrhs) B[(int64_t)c * ldb + i0 + ar] = out[q];
+      }
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) atomicExch(&flags[bi], 1);
+      continue;
+    }
     __syncthreads();
     if (warp < nrhs) {
       T yl[PER];

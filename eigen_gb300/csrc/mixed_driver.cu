@@ -284,7 +284,8 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
 // ------------------------------------------------------------------ workspace pool
 struct MixedWork {
   cudaStream_t stream = nullptr;
-  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv;
+  DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv,
+      dinv;
   SolveWork sw;
   TcWorkspace tc;
   HostBuf hstats;
@@ -336,10 +337,10 @@ constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_ker
 constexpr int kInvLd = kMixedNB + 1;
 constexpr size_t kInvSmem = sizeof(float) * (2 * kMixedNB * kInvLd + 32 * kInvLd + 4 * kMixedNB);
 
-__global__ void __launch_bounds__(4 * kMixedNB)
-unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M, int unit)
+// X = L^-1 of the lower nb x nb block (upper != 0: of U^T for the upper block
+// U at L, i.e. X = U^-T) in shared memory; see unit_lower_inverse_kernel.
+__device__ void tri_inverse_smem(const float* __restrict__ L, int64_t ld, int nb, int unit, int upper, float* sm)
 {
-  extern __shared__ float sm[];
   float(*Ls)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm);
   float(*X)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
   float(*Tb)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + 2 * kMixedNB * kInvLd);   // [32][..]
@@ -347,7 +348,8 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
   const int tid = threadIdx.x;
   for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
     const int r = e % kMixedNB, c = e / kMixedNB;
-    Ls[r][c] = (r < nb && c < nb && (r != c || !unit)) ? L[(int64_t)c * ld + r] : (r == c ? 1.f : 0.f);
+    const bool in = r < nb && c < nb && r >= c && (r != c || !unit);
+    Ls[r][c] = in ? (upper ? L[(int64_t)r * ld + c] : L[(int64_t)c * ld + r]) : (r == c ? 1.f : 0.f);
     X[r][c] = 0.f;
   }
   __syncthreads();
@@ -387,9 +389,38 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
     }
     __syncthreads();
   }
-  for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(4 * kMixedNB)
+unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M, int unit)
+{
+  extern __shared__ float sm[];
+  tri_inverse_smem(L, ld, nb, unit, 0, sm);
+  const float(*X)[kInvLd] = reinterpret_cast<const float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
+  for (int e = threadIdx.x; e < kMixedNB * kMixedNB; e += blockDim.x) {
     const int r = e % kMixedNB, c = e / kMixedNB;
     M[e] = (r < nb && c < nb && r >= c) ? (r == c ? 1.f : 0.f) - X[r][c] : 0.f;
+  }
+}
+
+// Inverses of the diagonal blocks (height nbk <= kMixedNB) of the n x n
+// triangle at A, one CTA per block: block b of L (unit lower) or of U (upper,
+// non-unit) inverted into out + b nbk^2, nbk x nbk column-major, zero beyond
+// the block (the persistent TRSM's dinv).
+__global__ void __launch_bounds__(4 * kMixedNB)
+diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int nbk, int upper, int unit,
+                          float* __restrict__ out)
+{
+  extern __shared__ float sm[];
+  const int b0 = blockIdx.x * nbk, nb = min(nbk, n - b0);
+  tri_inverse_smem(A + (int64_t)b0 * lda + b0, lda, nb, unit, upper, sm);
+  const float(*X)[kInvLd] = reinterpret_cast<const float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
+  float* o = out + (int64_t)blockIdx.x * nbk * nbk;
+  for (int e = threadIdx.x; e < nbk * nbk; e += blockDim.x) {
+    const int r = e % nbk, c = e / nbk;
+    // lower: inv(L)(r, c) = X(r, c); upper: inv(U)(r, c) = inv(U^T)(c, r) = X(c, r)
+    o[e] = (r < nb && c < nb) ? (upper ? X[c][r] : X[r][c]) : 0.f;
   }
 }
 
@@ -399,6 +430,8 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
   (void)sw;
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kInvSmem));
+  GBS_CUDA_TRY(cudaFuncSetAttribute(diag_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kInvSmem));
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
@@ -510,6 +543,8 @@ struct Precond {
   const int* tr;
   const float* d;
   const int* perm;    // LU: row order of P, applied when the right-hand side is converted (may be null)
+  const float* dinv_l = nullptr;   // LU: inverses of the diagonal blocks of L and U for the solves (may be null)
+  const float* dinv_u = nullptr;
 };
 
 // W <- M^-1 W.  LU with perm: W was gathered by perm on conversion, so only
@@ -517,8 +552,8 @@ struct Precond {
 static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, SolveWork& sw)
 {
   if (M.kind == 0 && M.perm) {
-    GBS_TRY(tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 1, 0, 1, W, M.n, sw));
-    return tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, 0, 0, W, M.n, sw);
+    GBS_TRY(tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 1, 0, 1, W, M.n, sw, M.dinv_l));
+    return tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, 0, 0, W, M.n, sw, M.dinv_u);
   }
   if (M.kind == 0) return lu_solve_device<float>(s, M.n, nrhs, M.F, M.n, M.tr, W, M.n, 0, sw);
   const int64_t tot = (int64_t)M.n * nrhs;
@@ -852,6 +887,21 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
         perm = w.perm.as<int>();
       }
       Precond M{0, n, w.a32.as<float>(), w.tr.as<int>(), nullptr, perm};
+      if (opt.tier == GBS_TIER_TF32X3) {
+        // inverses of the diagonal blocks of L and U: each correction's block step becomes a product
+        // (FP32-accurate factors only: the 16-bit tiers' blocks are left to substitution)
+        constexpr int nbk = tri_solve_nb<float>();
+        const int nblk = (n + nbk - 1) / nbk;
+        GBS_TRY(w.dinv.reserve(sizeof(float) * 2 * (size_t)nblk * nbk * nbk));
+        float* dl = w.dinv.as<float>();
+        float* du = dl + (size_t)nblk * nbk * nbk;
+        PhaseScope ps(s, PH_TRI_SOLVE, 2.0 * nblk * nbk * nbk * nbk / 3.0, 16.0 * nblk * nbk * nbk);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 0, 1, dl);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 1, 0, du);
+        GBS_CUDA_TRY(cudaGetLastError());
+        M.dinv_l = dl;
+        M.dinv_u = du;
+      }
       GBS_TRY(initial_solve(s, P, M, w));
       const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
       out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
