@@ -405,12 +405,13 @@ unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float
 }
 
 // Inverses of the diagonal blocks (height nbk <= kMixedNB) of the n x n
-// triangle at A, one CTA per block: block b of L (unit lower) or of U (upper,
-// non-unit) inverted into out + b nbk^2, nbk x nbk column-major, zero beyond
-// the block (the persistent TRSM's dinv).
+// triangle at A, one CTA per block: block b of the lower (upper = 0) or upper
+// (upper = 1) triangle, unit or not, inverted into out + b nbk^2, nbk x nbk
+// column-major, zero beyond the block (the persistent TRSM's dinv).
+// transpose_lower = 1 stores inv(L_bb)^T = inv(L_bb^T) (for solves with L^T).
 __global__ void __launch_bounds__(4 * kMixedNB)
 diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int nbk, int upper, int unit,
-                          float* __restrict__ out)
+                          int transpose_lower, float* __restrict__ out)
 {
   extern __shared__ float sm[];
   const int b0 = blockIdx.x * nbk, nb = min(nbk, n - b0);
@@ -420,7 +421,8 @@ diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int n
   for (int e = threadIdx.x; e < nbk * nbk; e += blockDim.x) {
     const int r = e % nbk, c = e / nbk;
     // lower: inv(L)(r, c) = X(r, c); upper: inv(U)(r, c) = inv(U^T)(c, r) = X(c, r)
-    o[e] = (r < nb && c < nb) ? (upper ? X[c][r] : X[r][c]) : 0.f;
+    const bool tr = upper || transpose_lower;
+    o[e] = (r < nb && c < nb) ? (tr ? X[c][r] : X[r][c]) : 0.f;
   }
 }
 
@@ -559,7 +561,12 @@ static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, S
   const int64_t tot = (int64_t)M.n * nrhs;
   count_launch();
   diag_scale_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(M.n, nrhs, M.d, W);
-  GBS_TRY(llt_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, W, M.n, sw));
+  if (M.dinv_l) {                          // L y = w, then L^T z = y, block steps with inverted diagonal blocks
+    GBS_TRY(tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 1, 0, 0, W, M.n, sw, M.dinv_l));
+    GBS_TRY(tri_solve_device<float>(s, M.n, nrhs, M.F, M.n, 1, 1, 0, W, M.n, sw, M.dinv_u));
+  } else {
+    GBS_TRY(llt_solve_device<float>(s, M.n, nrhs, M.F, M.n, 0, W, M.n, sw));
+  }
   count_launch();
   diag_scale_f32_kernel<<<cdiv(tot, 256), 256, 0, s>>>(M.n, nrhs, M.d, W);
   GBS_CUDA_TRY(cudaGetLastError());
@@ -896,8 +903,8 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
         float* dl = w.dinv.as<float>();
         float* du = dl + (size_t)nblk * nbk * nbk;
         PhaseScope ps(s, PH_TRI_SOLVE, 2.0 * nblk * nbk * nbk * nbk / 3.0, 16.0 * nblk * nbk * nbk);
-        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 0, 1, dl);
-        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 1, 0, du);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 0, 1, 0, dl);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 1, 0, 0, du);
         GBS_CUDA_TRY(cudaGetLastError());
         M.dinv_l = dl;
         M.dinv_u = du;
@@ -985,6 +992,21 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
         continue;
       }
       Precond M{1, n, w.a32.as<float>(), nullptr, w.d32.as<float>(), nullptr};
+      if (opt.tier == GBS_TIER_TF32X3) {
+        constexpr int nbk = tri_solve_nb<float>();
+        const int nblk = (n + nbk - 1) / nbk;
+        GBS_TRY(w.dinv.reserve(sizeof(float) * 2 * (size_t)nblk * nbk * nbk));
+        float* dl = w.dinv.as<float>();
+        float* dlt = dl + (size_t)nblk * nbk * nbk;
+        GBS_CUDA_TRY(cudaFuncSetAttribute(diag_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kInvSmem));
+        PhaseScope ps(s, PH_TRI_SOLVE, 2.0 * nblk * nbk * nbk * nbk / 3.0, 16.0 * nblk * nbk * nbk);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 0, 0, 0, dl);
+        diag_block_inverse_kernel<<<nblk, 4 * kMixedNB, kInvSmem, s>>>(w.a32.as<float>(), n, n, nbk, 0, 0, 1, dlt);
+        GBS_CUDA_TRY(cudaGetLastError());
+        M.dinv_l = dl;
+        M.dinv_u = dlt;
+      }
       GBS_TRY(initial_solve(s, P, M, w));
       const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
       out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
