@@ -446,7 +446,7 @@ constexpr size_t trsm_persistent_smem()
 // columns); with them a block's own step is X_b = Dinv_b Y_b, a product with
 // independent FMAs instead of an NB-step substitution.
 template <typename T, int NB, int RC>
-__global__ void __launch_bounds__(RC * 32)
+__global__ void __launch_bounds__(RC * 32, 2)
 trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, int64_t cs, int forward, int unit,
                        T* B, int64_t ldb, int* work, const T* __restrict__ dinv)
 {
