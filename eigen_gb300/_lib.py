@@ -80,6 +80,8 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_lu_rcond": (c_int, [c_vp, c_dp]),
     "gbs_lu_l1_norm": (c_int, [c_vp, c_dp]),
     "gbs_lu_determinant": (c_int, [c_vp, c_dp]),
+    "gbs_lu_inverse": (c_int, [c_vp, c_vp, c_i64]),
+    "gbs_lu_inverse_device": (c_int, [c_vp, c_vp, c_i64]),
     "gbs_lu_matrix": (c_int, [c_vp, c_vp, c_i64]),
     "gbs_lu_transpositions": (c_int, [c_vp, c_vp]),
     "gbs_lu_permutation": (c_int, [c_vp, c_vp]),

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "dense_driver.cuh"
+#include "gbs_profile.cuh"
 
 using namespace gbs;
 
@@ -434,6 +435,52 @@ extern "C" int gbs_lu_solve_device(gbs_lu* o, int64_t nrhs, const void* d_b, int
   if (d_x != d_b)
     GBS_CUDA_TRY(cudaMemcpy2DAsync(d_x, ldx * es, d_b, ldb * es, n * es, nrhs, cudaMemcpyDeviceToDevice, o->stream));
   return lu_solve_inplace(o, (int)nrhs, d_x, ldx, transpose);
+}
+
+template <typename T>
+__global__ void identity_kernel(T* x, int64_t ld, int64_t n)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int64_t r = t % n, c = t / n;
+  x[c * ld + r] = r == c ? T(1) : T(0);
+}
+
+// A^-1 = solve(I) (PartialPivLU.h:197-201): the identity solved in place at d_x
+static int lu_inverse_into(gbs_lu* o, void* d_x, int64_t ldx)
+{
+  const int64_t n = o->n;
+  count_launch();
+  const int grid = (int)std::min<int64_t>((n * n + 255) / 256, 1 << 30);
+  if (o->dtype == GBS_F64) identity_kernel<double><<<grid, 256, 0, o->stream>>>((double*)d_x, ldx, n);
+  else identity_kernel<float><<<grid, 256, 0, o->stream>>>((float*)d_x, ldx, n);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return lu_solve_inplace(o, (int)n, d_x, ldx, 0);
+}
+
+extern "C" int gbs_lu_inverse(gbs_lu* o, void* x, int64_t ldx)
+{
+  GBS_TRY(lu_ready(o));
+  const int64_t n = o->n;
+  if (!x && n > 0) return GBS_INVALID_ARGUMENT;
+  if (ldx < std::max<int64_t>(1, n)) return GBS_INVALID_ARGUMENT;
+  if (n == 0) return GBS_SUCCESS;
+  const size_t es = esize(o->dtype);
+  GBS_TRY(o->rhs.reserve(es * (size_t)n * n));
+  GBS_TRY(lu_inverse_into(o, o->rhs.p, n));
+  GBS_TRY(solve_status(o->stream, o->sw));
+  GBS_TRY(download_matrix(o->stream, o->rhs.p, n, x, ldx, n, n, es));
+  return sync(o->stream);
+}
+
+extern "C" int gbs_lu_inverse_device(gbs_lu* o, void* d_x, int64_t ldx)
+{
+  GBS_TRY(lu_ready(o));
+  const int64_t n = o->n;
+  if (!d_x && n > 0) return GBS_INVALID_ARGUMENT;
+  if (ldx < std::max<int64_t>(1, n)) return GBS_INVALID_ARGUMENT;
+  if (n == 0) return GBS_SUCCESS;
+  return lu_inverse_into(o, d_x, ldx);
 }
 
 extern "C" int gbs_lu_rcond(gbs_lu* o, double* rcond)

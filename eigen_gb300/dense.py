@@ -214,6 +214,12 @@ class PartialPivLU(_Decomposition):
         L.check(L.lib().gbs_lu_determinant(self._h, C.byref(d)), "lu.determinant")
         return d.value
 
+    def inverse(self):
+        """PartialPivLU::inverse(): A^-1 = solve(I), on the host (numpy)."""
+        out = np.empty((self._n, self._n), dtype=_np_dtype(self._code), order="F")
+        L.check(L.lib().gbs_lu_inverse(self._h, out.ctypes.data_as(C.c_void_p), max(self._n, 1)), "lu.inverse")
+        return out
+
     def first_zero_pivot(self) -> int:
         return int(L.lib().gbs_lu_first_zero_pivot(self._h))
 

@@ -181,6 +181,10 @@ int gbs_lu_solve_device(gbs_lu* lu, int64_t nrhs, const void* d_b, int64_t ldb, 
 int gbs_lu_rcond(gbs_lu* lu, double* rcond);
 int gbs_lu_l1_norm(const gbs_lu* lu, double* l1);
 int gbs_lu_determinant(gbs_lu* lu, double* det);
+/* A^-1 = solve(I), PartialPivLU::inverse() (PartialPivLU.h:197-201): n x n,
+ * column-major, to host x (ld ldx) or device d_x (stream-ordered). */
+int gbs_lu_inverse(gbs_lu* lu, void* x, int64_t ldx);
+int gbs_lu_inverse_device(gbs_lu* lu, void* d_x, int64_t ldx);
 int gbs_lu_matrix(gbs_lu* lu, void* out, int64_t ld);
 int gbs_lu_transpositions(gbs_lu* lu, int* out);
 int gbs_lu_permutation(gbs_lu* lu, int* out);

@@ -320,3 +320,15 @@ def test_nonfinite_input_returns_without_hang():
     s[20, 20] = np.nan
     llt = LLT(s)
     assert llt.failed_column() == O.llt(s)[1]
+
+
+@pytest.mark.parametrize("n", [1, 7, 200, 1031])
+def test_lu_inverse_matches_oracle_solve_of_identity(n):
+    """PartialPivLU::inverse() is solve(I) (PartialPivLU.h:197-201)."""
+    a = O.gauss(500 + n, n, n)
+    lu = PartialPivLU(a)
+    inv = lu.inverse()
+    f, tr, _, _ = O.lu(a)
+    ref = O.lu_solve(f, tr, np.eye(n))
+    assert np.linalg.norm(inv - ref) <= 1e-12 * max(1.0, np.linalg.norm(ref))
+    assert np.linalg.norm(a @ inv - np.eye(n)) <= 1e-9 * n
