@@ -621,6 +621,11 @@ def run_batched(args):
         A, B = A0.clone(), B0.clone()
         info = torch.empty(len(sizes), dtype=torch.int32, device="cuda")
         piv = torch.empty(bs.b_elems, dtype=torch.int32, device="cuda")
+        dflt = []                                  # the plan's default variants, before autotuning
+        for _ in range(max(args.warmup, 3) + 3):
+            A.copy_(A0); B.copy_(B0)
+            dflt.append(_event_time(lambda: bs.solve(A, B, info, piv))[1])
+        dflt = min(dflt[-3:])
         cfg = bs.autotune(A.clone(), B.clone(), info, piv)
         times = []
         for _ in range(args.warmup + args.steps):
@@ -657,6 +662,7 @@ def run_batched(args):
         byts = float(np.sum(2 * sizes.astype(np.float64) ** 2 + 3 * sizes)) * np.dtype(dtype).itemsize
         out[name] = {"solves_per_s": len(sizes) / dt, "ms": 1e3 * dt, "tflops": flops / dt / 1e12,
                      "hbm_gbs": byts / dt / 1e9, "failures": failures, "autotuned": cfg,
+                     "default_variants_ms": 1e3 * dflt,
                      "per_matrix_plain_gpu_solves_per_s": per_matrix, "cpu_oracle_solves_per_s": cpu,
                      "cpu_cores": O.num_threads()}
     line = {"metric": METRIC, "value": out["f64"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,

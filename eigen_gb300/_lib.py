@@ -105,6 +105,8 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_batched_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "gbs_batched_autotune": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
     "gbs_batched_config": (c_int, [c_vp, c_ip, c_ip]),
+    "gbs_batched_buckets": (c_int, [c_vp, c_int, c_ip, c_ip]),
+    "gbs_batched_set_variant": (c_int, [c_vp, c_int, c_int, c_int]),
     # medium batches + router
     "gbs_mbatch_create": (c_int, [C.POINTER(c_vp), c_i64, c_vp]),
     "gbs_mbatch_destroy": (c_int, [c_vp]),

@@ -62,7 +62,22 @@ class BatchedSolver:
                                              int(persist)), "batched.autotune")
         return self.config()
 
+    def buckets(self):
+        """The plan's buckets: kind, size class, items, largest n, variant."""
+        cnt = C.c_int()
+        L.check(L.lib().gbs_batched_buckets(self._h, 0, C.byref(cnt), None), "batched.buckets")
+        d = np.zeros(7 * max(cnt.value, 1), dtype=np.int32)
+        L.check(L.lib().gbs_batched_buckets(self._h, cnt.value, C.byref(cnt),
+                                            d.ctypes.data_as(C.POINTER(C.c_int))),
+                "batched.buckets")
+        keys = ("kind", "n_lo", "n_hi", "items", "max_n", "lanes_per_system", "warps_per_cta")
+        return [dict(zip(keys, map(int, d[7 * i:7 * i + 7]))) for i in range(cnt.value)]
+
+    def set_variant(self, bucket, lanes_per_system, warps_per_cta=1):
+        L.check(L.lib().gbs_batched_set_variant(self._h, int(bucket), int(lanes_per_system), int(warps_per_cta)),
+                "batched.set_variant")
+
     def config(self):
         ws, wl = C.c_int(), C.c_int()
         L.lib().gbs_batched_config(self._h, C.byref(ws), C.byref(wl))
-        return {"warps_per_cta_n<=32": ws.value, "warps_per_cta_n<=64": wl.value}
+        return {"warps_per_cta_n<=32": ws.value, "warps_per_cta_n<=64": wl.value, "buckets": self.buckets()}

@@ -2,20 +2,22 @@
 // partial pivoting for general matrices), one right-hand side each.
 //
 // The reference has no batch API: its CPU path is one LLT / PartialPivLU per
-// matrix (LLT.h:305-328 for n < 32; PartialPivLU.h:365-496).  Here one
-// persistent launch per size bucket serves the whole batch:
-//   * the work list is sorted by cost (largest first) at plan time;
-//   * every warp takes the next matrix with one atomicAdd (no waits);
-//   * the matrix lives in the warp's own shared-memory slice, lanes own rows;
-//   * LLT follows the reference's left-looking column order (x = a_kk -
-//     ||l_k||^2, fail if x <= 0, column below scaled by 1/x after the dot
-//     products), so info() and the failing column match;
-//   * LU pivots on the first maximum of |a_ik| (warp-shuffle argmax), swaps
-//     whole rows, scales, rank-1 updates -- the reference's pivot sequence;
-//   * the solve (P, L, U or L, L^T) runs in the same warp, lane = row.
-// The two buckets (n <= 32, one row per lane; n <= 64, two rows per lane) run
-// as two kernel nodes of one CUDA graph; threads per CTA per bucket come from
-// the autotuner (batched_autotune), cached per (bucket, dtype, GPU).
+// matrix (LLT.h:305-328 for n < 32; PartialPivLU.h:365-496).  Here the plan
+// groups the items by (kind, size class), sorts each group by cost (largest
+// first) and gives every group one persistent launch; the launches are forked
+// onto side streams (one CUDA graph per call) so that their tails overlap.
+// Inside a launch, warps take the next items with one atomicAdd (no waits).
+// Each group runs one of two kernel families:
+//   * one warp per system (batched_kernel below): the matrix in the warp's
+//     shared-memory slice, lanes own rows (one or two per lane);
+//   * G lanes per system, G in {1, 2, 4, 8, 16} (batched_lane.cuh): 32 / G
+//     systems per warp, which keeps the FP64 units busy on small n.
+// Both follow the reference's arithmetic: LLT left-looking (x = a_kk -
+// ||l_k||^2, fail if x <= 0 with the failing column untouched), LU with the
+// first maximum of |a_ik| as pivot, whole-row interchanges, division by the
+// pivot, rank-1 updates -- the same pivots and failing columns.  The variant
+// per group comes from the autotuner (gbs_batched_autotune), cached per
+// (GPU, kind, size class, dtype).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -29,6 +31,7 @@
 #include <string>
 #include <vector>
 
+#include "batched_lane.cuh"
 #include "dense_driver.cuh"
 #include "gbs_common.cuh"
 #include "gbs_profile.cuh"
@@ -36,14 +39,7 @@
 namespace gbs {
 namespace {
 
-struct Item {
-  int64_t a_off;   // element offset of the matrix (column-major n x n, ld = n)
-  int64_t b_off;   // element offset of its right-hand side (n)
-  int n;
-  int kind;        // 0 = LLT, 1 = LU
-  int id;          // position in the caller's batch
-  int pad;
-};
+using Item = BatchItem;
 
 // b[k / 32] without a dynamic register index (which would go to local memory)
 template <typename T, int RPL>
@@ -58,9 +54,10 @@ __device__ __forceinline__ T pick(const T (&b)[RPL], int k)
 
 // MAXN: bucket bound (32 or 64); RPL: rows per lane = MAXN / 32.
 template <typename T, int MAXN>
-__global__ void batched_kernel(const Item* __restrict__ items, int count, T* __restrict__ A, T* __restrict__ Bv,
-                               int* __restrict__ info, int* __restrict__ piv, int* __restrict__ counter)
+__global__ void batched_kernel(const Item* __restrict__ items, int count, int maxn, T* __restrict__ A,
+                               T* __restrict__ Bv, int* __restrict__ info, int* __restrict__ piv, int* __restrict__ counter)
 {
+  (void)maxn;
   constexpr int RPL = MAXN / 32;
   constexpr int LD = MAXN + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -75,7 +72,8 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
     const int n = it.n;
     T* a = A + it.a_off;
     T* bv = Bv + it.b_off;
-    for (int e = lane; e < n * n; e += 32) S[(e / n) * LD + (e % n)] = a[e];   // S[col*LD + row]
+    for (int c = 0; c < n; ++c)                                   // S[col*LD + row], coalesced per column
+      for (int r = lane; r < n; r += 32) S[c * LD + r] = a[c * n + r];
     T b[RPL];
 #pragma unroll
     for (int q = 0; q < RPL; ++q) {
@@ -130,46 +128,41 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
         }
       }
       // write back the lower triangle (the strict upper part is the caller's)
-      for (int e = lane; e < n * n; e += 32) {
-        const int r = e % n, c = e / n;
-        if (r >= c) a[e] = S[c * LD + r];
-      }
+      for (int c = 0; c < n; ++c)
+        for (int r = c + lane; r < n; r += 32) a[c * n + r] = S[c * LD + r];
     } else {
       // ---------------- LU with partial pivoting (PartialPivLU.h:365-409)
+      using U = typename PivotKey<T>::U;
       int* pv = piv + it.b_off;
-      int nbt = 0;
       for (int k = 0; k < n; ++k) {
-        T bs = T(-2);
+        U bk = 0;                        // integer pivot keys: no FP64 compares
         int bi = 0x7fffffff;
 #pragma unroll
         for (int q = 0; q < RPL; ++q) {
           const int i = lane + 32 * q;
           if (i >= k && i < n) {
-            const T x = S[k * LD + i];
-            const T s = (i == k) ? ((x != x) ? T(INFINITY) : gbs_abs(x)) : pivot_score(x);
-            if (better(s, i, bs, bi)) { bs = s; bi = i; }
+            const U key = pivot_key(S[k * LD + i], i == k);
+            if (key > bk) { bk = key; bi = i; }
           }
         }
-        warp_argmax(bs, bi);
+        group_argmax<32>(bk, bi, 0xffffffffu);
         const int p = bi;
-        const T pivv = S[k * LD + p];
-        const bool nz = pivv != T(0);
-        __syncwarp();                    // every lane has read the pivot before rows move
+        const bool nz = bk != U(2);
+        __syncwarp();                    // every lane has finished the previous update
         if (lane == 0) pv[k] = p;
         if (nz) {
           if (p != k) {
             for (int c = lane; c < n; c += 32) {
               const T t = S[c * LD + k]; S[c * LD + k] = S[c * LD + p]; S[c * LD + p] = t;
             }
-            ++nbt;
             // the right-hand side row follows (P b, PartialPivLU.h:233)
-            const T bk = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
+            const T bk2 = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
             const T bp = __shfl_sync(0xffffffffu, pick(b, p), p % 32);
 #pragma unroll
             for (int q = 0; q < RPL; ++q) {
               const int i = lane + 32 * q;
               if (i == k) b[q] = bp;
-              if (i == p) b[q] = bk;
+              if (i == p) b[q] = bk2;
             }
           }
           __syncwarp();
@@ -183,18 +176,45 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
           status = k;
         }
         __syncwarp();
+        // trailing update, four columns at a time (loads of a block before its stores)
+        T l[RPL];
+        bool act[RPL];
 #pragma unroll
         for (int q = 0; q < RPL; ++q) {
           const int i = lane + 32 * q;
-          if (i > k && i < n) {
-            const T l = S[k * LD + i];
-            for (int j = k + 1; j < n; ++j) S[j * LD + i] = fma(-l, S[j * LD + k], S[j * LD + i]);
+          act[q] = i > k && i < n;
+          l[q] = act[q] ? S[k * LD + i] : T(0);
+        }
+        int j = k + 1;
+        for (; j + 4 <= n; j += 4) {
+          const T u0 = S[j * LD + k], u1 = S[(j + 1) * LD + k], u2 = S[(j + 2) * LD + k], u3 = S[(j + 3) * LD + k];
+#pragma unroll
+          for (int q = 0; q < RPL; ++q) {
+            if (act[q]) {
+              T* ar = S + j * LD + lane + 32 * q;
+              const T a0 = ar[0], a1 = ar[LD], a2 = ar[2 * LD], a3 = ar[3 * LD];
+              ar[0] = fma(-l[q], u0, a0);
+              ar[LD] = fma(-l[q], u1, a1);
+              ar[2 * LD] = fma(-l[q], u2, a2);
+              ar[3 * LD] = fma(-l[q], u3, a3);
+            }
           }
         }
-        __syncwarp();
+        for (; j < n; ++j) {
+          const T u = S[j * LD + k];
+#pragma unroll
+          for (int q = 0; q < RPL; ++q)
+            if (act[q]) S[j * LD + lane + 32 * q] = fma(-l[q], u, S[j * LD + lane + 32 * q]);
+        }
       }
-      (void)nbt;
-      // L y = P b (unit), U x = y
+      __syncwarp();
+      // L y = P b (unit), U x = y; the reciprocals of U's diagonal per row, in parallel
+      T rd[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        const int i = lane + 32 * q;
+        rd[q] = i < n ? T(1) / S[i * LD + i] : T(0);
+      }
       for (int k = 0; k < n; ++k) {
         const T yk = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
 #pragma unroll
@@ -204,8 +224,7 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
         }
       }
       for (int k = n - 1; k >= 0; --k) {
-        T xk = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
-        xk = xk / S[k * LD + k];
+        const T xk = __shfl_sync(0xffffffffu, pick(b, k), k % 32) * __shfl_sync(0xffffffffu, pick(rd, k), k % 32);
 #pragma unroll
         for (int q = 0; q < RPL; ++q) {
           const int i = lane + 32 * q;
@@ -213,7 +232,8 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
           if (i == k) b[q] = xk;
         }
       }
-      for (int e = lane; e < n * n; e += 32) a[e] = S[(e / n) * LD + (e % n)];
+      for (int c = 0; c < n; ++c)
+        for (int r = lane; r < n; r += 32) a[c * n + r] = S[c * LD + r];
     }
 #pragma unroll
     for (int q = 0; q < RPL; ++q) {
@@ -228,13 +248,63 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, T* __r
 template <typename T, int MAXN>
 size_t smem_per_warp() { return sizeof(T) * MAXN * (MAXN + 1); }
 
-// ------------------------------------------------------------------ autotuner
-// Candidate CTA shapes (warps per CTA); the best per (bucket, dtype, GPU) is
-// cached in a small JSON-lines file.
+// ------------------------------------------------------------------ variants
+// A size bucket runs one of: one warp per system (batched_kernel, lanes = 32,
+// warps per CTA from kWarpChoices) or G lanes per system (lu_group_kernel,
+// llt_lane_kernel; one warp per CTA).
 const int kWarpChoices[] = {1, 2, 4, 8};
 
+template <typename T>
+const void* kernel_for(int kind, int lanes, int maxn)
+{
+  if (lanes == 32) return maxn <= 32 ? (const void*)batched_kernel<T, 32> : (const void*)batched_kernel<T, 64>;
+  if (kind == 0) return lanes == 1 ? (const void*)llt_lane_kernel<T> : nullptr;
+  switch (lanes) {
+    case 1: return (const void*)lu_group_kernel<T, 1>;
+    case 2: return (const void*)lu_group_kernel<T, 2>;
+    case 4: return (const void*)lu_group_kernel<T, 4>;
+    case 8: return (const void*)lu_group_kernel<T, 8>;
+    case 16: return (const void*)lu_group_kernel<T, 16>;
+  }
+  return nullptr;
+}
+
+template <typename T>
+size_t smem_for(int kind, int lanes, int maxn, int warps)
+{
+  if (lanes == 32) return (maxn <= 32 ? smem_per_warp<T, 32>() : smem_per_warp<T, 64>()) * warps;
+  return kind == 0 ? llt_lane_smem<T>(maxn) : lu_group_smem<T>(maxn, lanes);
+}
+
+// size classes (upper bounds) and the variants tried for each
+const int kLltClasses[] = {8, 12, 16, 20, 24, 32, 64};
+const int kLuClasses[] = {8, 12, 16, 24, 32, 48, 64};
+
+std::vector<int> lane_choices(int kind, int hi)
+{
+  if (kind == 0) return hi <= 32 ? std::vector<int>{1, 32} : std::vector<int>{32};
+  if (hi <= 16) return {1, 2, 32};
+  if (hi <= 32) return {2, 4, 8, 32};
+  return {8, 16, 32};
+}
+
+// defaults (before autotuning) from per-bucket timings on GB300: one lane
+// per system for LLT up to n = 32, one warp per system for LU except
+// n = 33..48, where 16 lanes per system win
+int default_lanes(int kind, int hi)
+{
+  if (kind == 0) return hi <= 32 ? 1 : 32;
+  return hi == 48 ? 16 : 32;
+}
+
+// ------------------------------------------------------------------ autotuner
+// The best (lanes per system, warps per CTA) per (GPU, kind, size class,
+// dtype) is cached in a small JSON-lines file.
+struct TuneEntry {
+  int lanes, warps;
+};
 std::mutex g_tune_mu;
-std::map<std::string, int> g_tune;   // key -> warps per CTA
+std::map<std::string, TuneEntry> g_tune;
 bool g_tune_loaded = false;
 
 std::string cache_path()
@@ -252,36 +322,49 @@ void load_cache()
   std::ifstream f(cache_path());
   std::string line;
   while (std::getline(f, line)) {
-    auto k0 = line.find("\"key\": \""), w0 = line.find("\"warps\": ");
-    if (k0 == std::string::npos || w0 == std::string::npos) continue;
+    auto k0 = line.find("\"key\": \""), w0 = line.find("\"warps\": "), l0 = line.find("\"lanes\": ");
+    if (k0 == std::string::npos || w0 == std::string::npos || l0 == std::string::npos) continue;
     k0 += 8;
     auto k1 = line.find('"', k0);
-    g_tune[line.substr(k0, k1 - k0)] = atoi(line.c_str() + w0 + 9);
+    g_tune[line.substr(k0, k1 - k0)] = {atoi(line.c_str() + l0 + 9), atoi(line.c_str() + w0 + 9)};
   }
 }
 
-void store_cache(const std::string& key, int warps, double us)
+void store_cache(const std::string& key, TuneEntry e, double us)
 {
-  g_tune[key] = warps;
+  g_tune[key] = e;
   std::ofstream f(cache_path(), std::ios::app);
-  if (f) f << "{\"key\": \"" << key << "\", \"warps\": " << warps << ", \"us\": " << us << "}\n";
+  if (f) f << "{\"key\": \"" << key << "\", \"lanes\": " << e.lanes << ", \"warps\": " << e.warps << ", \"us\": " << us << "}\n";
 }
 
-std::string tune_key(int bucket, int dtype)
+std::string tune_key(int kind, int hi, int dtype)
 {
   cudaDeviceProp p;
   int dev = 0;
   cudaGetDevice(&dev);
   cudaGetDeviceProperties(&p, dev);
   std::ostringstream s;
-  s << p.name << "|sm" << p.major << p.minor << "|n<=" << bucket << "|" << (dtype == GBS_F64 ? "f64" : "f32");
+  s << p.name << "|sm" << p.major << p.minor << "|" << (kind ? "lu" : "llt") << "|n<=" << hi << "|"
+    << (dtype == GBS_F64 ? "f64" : "f32");
   return s.str();
 }
+
+constexpr int kSideStreams = 4;
 
 }  // namespace
 }  // namespace gbs
 
 using namespace gbs;
+
+struct BucketPlan {
+  int kind, lo, hi;      // item kind and size class lo..hi
+  int first, count;      // its range of the sorted work list
+  int maxn;              // largest n present
+  int lanes;             // lanes per system (32: one warp per system)
+  int warps;             // warps per CTA
+  int grid;
+  double cost;           // sum of n^3 (LU counted twice), for the launch order
+};
 
 struct gbs_batched {
   int dtype = GBS_F64;
@@ -289,11 +372,12 @@ struct gbs_batched {
   int64_t total_a = 0, total_b = 0;
   std::vector<int> sizes, kinds;
   std::vector<int64_t> a_off, b_off;
-  int nb[2] = {0, 0};            // items per bucket
-  int warps[2] = {4, 4};         // warps per CTA per bucket
-  int grid[2] = {0, 0};
+  std::vector<BucketPlan> buckets;
   DevBuf items, counters;
   cudaStream_t stream = nullptr;
+  cudaStream_t side[kSideStreams] = {};
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_join;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   void* g_a = nullptr;           // buffers the graph was captured with
@@ -303,63 +387,89 @@ struct gbs_batched {
   int use_graph = 1;
 };
 
-// grid for a bucket: co-resident CTAs of this shape (sets the smem limit
-// first); called outside any stream capture.
-template <typename T, int MAXN>
-static int bucket_grid(int count, int warps, int* grid)
+static void drop_graph(gbs_batched* p)
 {
-  *grid = 0;
-  if (count <= 0) return GBS_SUCCESS;
-  const size_t smem = smem_per_warp<T, MAXN>() * warps;
-  GBS_CUDA_TRY(cudaFuncSetAttribute(batched_kernel<T, MAXN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<T, MAXN>, 32 * warps, smem));
-  per_sm = std::max(per_sm, 1);
-  *grid = std::min<int>(per_sm * device_sm_count(), (count + warps - 1) / warps);
-  return GBS_SUCCESS;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
 }
 
-template <typename T, int MAXN>
-static int launch_bucket(cudaStream_t s, const Item* items, int count, int warps, int grid, T* A, T* B, int* info,
-                         int* piv, int* counter)
+// grid of a bucket: co-resident CTAs of its variant (raises the kernel's
+// shared-memory limit first); called outside any stream capture.
+template <typename T>
+static int bucket_grid(BucketPlan& b)
 {
-  if (count <= 0) return GBS_SUCCESS;
-  const size_t smem = smem_per_warp<T, MAXN>() * warps;
-  count_launch();
-  batched_kernel<T, MAXN><<<grid, 32 * warps, smem, s>>>(items, count, A, B, info, piv, counter);
-  GBS_CUDA_TRY(cudaGetLastError());
+  b.grid = 0;
+  if (b.count <= 0) return GBS_SUCCESS;
+  const void* fn = kernel_for<T>(b.kind, b.lanes, b.maxn);
+  if (!fn) return GBS_INVALID_ARGUMENT;
+  const size_t smem = smem_for<T>(b.kind, b.lanes, b.maxn, b.warps);
+  int optin = 0, dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  GBS_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)optin) return GBS_INVALID_ARGUMENT;
+  // the limit, not this bucket's size: several buckets may share the kernel
+  GBS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  int per_sm = 0;
+  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * b.warps, smem));
+  per_sm = std::max(per_sm, 1);
+  const int per_cta = b.lanes == 32 ? b.warps : 32 / b.lanes;    // systems a CTA takes at once
+  b.grid = std::min<int>(per_sm * device_sm_count(), (b.count + per_cta - 1) / per_cta);
   return GBS_SUCCESS;
 }
 
 static int prepare(gbs_batched* p)
 {
-  if (p->dtype == GBS_F64) {
-    GBS_TRY((bucket_grid<double, 32>(p->nb[0], p->warps[0], &p->grid[0])));
-    GBS_TRY((bucket_grid<double, 64>(p->nb[1], p->warps[1], &p->grid[1])));
-  } else {
-    GBS_TRY((bucket_grid<float, 32>(p->nb[0], p->warps[0], &p->grid[0])));
-    GBS_TRY((bucket_grid<float, 64>(p->nb[1], p->warps[1], &p->grid[1])));
+  for (BucketPlan& b : p->buckets) GBS_TRY(p->dtype == GBS_F64 ? bucket_grid<double>(b) : bucket_grid<float>(b));
+  return GBS_SUCCESS;
+}
+
+template <typename T>
+static int launch_bucket(const BucketPlan& b, cudaStream_t s, const Item* items, void* A, void* B, int* info,
+                         int* piv, int* counter)
+{
+  if (b.count <= 0) return GBS_SUCCESS;
+  const Item* it = items + b.first;
+  int count = b.count, maxn = b.maxn;
+  T* a = (T*)A;
+  T* bb = (T*)B;
+  void* args[] = {(void*)&it, (void*)&count, (void*)&maxn, (void*)&a, (void*)&bb, (void*)&info, (void*)&piv, (void*)&counter};
+  count_launch();
+  GBS_CUDA_TRY(cudaLaunchKernel(kernel_for<T>(b.kind, b.lanes, b.maxn), dim3(b.grid), dim3(32 * b.warps), args,
+                                smem_for<T>(b.kind, b.lanes, b.maxn, b.warps), s));
+  return GBS_SUCCESS;
+}
+
+// only >= 0: that bucket alone (autotuning); else every bucket, forked onto
+// side streams so that the buckets' tails overlap, joined back into s.
+static int enqueue(gbs_batched* p, cudaStream_t s, void* d_a, void* d_b, int* d_info, int* d_piv, int only = -1)
+{
+  const int nb = (int)p->buckets.size();
+  GBS_CUDA_TRY(cudaMemsetAsync(p->counters.p, 0, sizeof(int) * std::max(nb, 1), s));
+  const Item* it = p->items.as<Item>();
+  int* ctr = p->counters.as<int>();
+  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
+  auto launch = [&](int b, cudaStream_t st) {
+    return p->dtype == GBS_F64 ? launch_bucket<double>(p->buckets[b], st, it, d_a, d_b, d_info, d_piv, ctr + b)
+                               : launch_bucket<float>(p->buckets[b], st, it, d_a, d_b, d_info, d_piv, ctr + b);
+  };
+  if (only >= 0) return launch(only, s);
+  if (nb == 1) return launch(0, s);
+  GBS_CUDA_TRY(cudaEventRecord(p->ev_fork, s));
+  for (int b = 0; b < nb; ++b) {
+    cudaStream_t st = p->side[b % kSideStreams];
+    if (b < kSideStreams) GBS_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_fork, 0));
+    GBS_TRY(launch(b, st));
+  }
+  for (int k = 0; k < std::min(nb, kSideStreams); ++k) {
+    GBS_CUDA_TRY(cudaEventRecord(p->ev_join[k], p->side[k]));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, p->ev_join[k], 0));
   }
   return GBS_SUCCESS;
 }
 
-static int enqueue(gbs_batched* p, cudaStream_t s, void* d_a, void* d_b, int* d_info, int* d_piv)
-{
-  GBS_CUDA_TRY(cudaMemsetAsync(p->counters.p, 0, 2 * sizeof(int), s));
-  const Item* it = p->items.as<Item>();
-  int* ctr = p->counters.as<int>();
-  PhaseScope ps(s, PH_BATCHED, 0.0, 0.0);
-  if (p->dtype == GBS_F64) {
-    GBS_TRY((launch_bucket<double, 32>(s, it, p->nb[0], p->warps[0], p->grid[0], (double*)d_a, (double*)d_b, d_info, d_piv, ctr)));
-    GBS_TRY((launch_bucket<double, 64>(s, it + p->nb[0], p->nb[1], p->warps[1], p->grid[1], (double*)d_a, (double*)d_b, d_info,
-                                      d_piv, ctr + 1)));
-  } else {
-    GBS_TRY((launch_bucket<float, 32>(s, it, p->nb[0], p->warps[0], p->grid[0], (float*)d_a, (float*)d_b, d_info, d_piv, ctr)));
-    GBS_TRY((launch_bucket<float, 64>(s, it + p->nb[0], p->nb[1], p->warps[1], p->grid[1], (float*)d_a, (float*)d_b, d_info,
-                                     d_piv, ctr + 1)));
-  }
-  return GBS_SUCCESS;
-}
+extern "C" int gbs_batched_destroy(gbs_batched* p);
 
 extern "C" int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, const int* sizes, const int* kinds,
                                   int use_graph)
@@ -391,15 +501,23 @@ extern "C" int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, c
   }
   p->total_a = ao;
   p->total_b = bo;
-  // work list: bucket by size, each bucket sorted by cost (largest first)
+  // size class of an item: index into kLltClasses / kLuClasses
+  auto cls = [&](int64_t i) {
+    const int* c = kinds[i] ? kLuClasses : kLltClasses;
+    int k = 0;
+    while (sizes[i] > c[k]) ++k;
+    return k;
+  };
+  // work list: grouped by (kind, size class), each group sorted by cost
+  // (largest first); warps take consecutive items, so a warp's systems have
+  // nearly equal sizes
   std::vector<Item> items((size_t)count);
   std::vector<int64_t> order((size_t)count);
   std::iota(order.begin(), order.end(), 0);
-  auto cost = [&](int64_t i) { return (double)sizes[i] * sizes[i] * sizes[i] * (kinds[i] ? 2.0 : 1.0); };
   std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
-    const int bx = sizes[x] > 32, by = sizes[y] > 32;
-    if (bx != by) return bx < by;
-    return cost(x) > cost(y);
+    const int gx = kinds[x] * 16 + cls(x), gy = kinds[y] * 16 + cls(y);
+    if (gx != gy) return gx < gy;
+    return sizes[x] > sizes[y];
   });
   for (int64_t k = 0; k < count; ++k) {
     const int64_t i = order[(size_t)k];
@@ -410,30 +528,56 @@ extern "C" int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, c
     it.kind = kinds[i];
     it.id = (int)i;
     it.pad = 0;
-    p->nb[sizes[i] > 32]++;
+    const int c = cls(i);
+    const int* cl = kinds[i] ? kLuClasses : kLltClasses;
+    if (p->buckets.empty() || p->buckets.back().kind != kinds[i] || p->buckets.back().hi != cl[c]) {
+      BucketPlan b{};
+      b.kind = kinds[i];
+      b.lo = c ? cl[c - 1] + 1 : 1;
+      b.hi = cl[c];
+      b.first = (int)k;
+      b.maxn = sizes[i];
+      b.lanes = default_lanes(b.kind, b.hi);
+      b.warps = b.lanes == 32 ? 4 : 1;
+      p->buckets.push_back(b);
+    }
+    BucketPlan& b = p->buckets.back();
+    b.count++;
+    b.cost += (double)sizes[i] * sizes[i] * sizes[i] * (kinds[i] ? 2.0 : 1.0);
   }
+  const int nb = (int)p->buckets.size();
   int rc;
   if ((rc = p->items.reserve(sizeof(Item) * (size_t)std::max<int64_t>(count, 1))) != GBS_SUCCESS ||
-      (rc = p->counters.reserve(2 * sizeof(int))) != GBS_SUCCESS) {
+      (rc = p->counters.reserve(sizeof(int) * (size_t)std::max(nb, 1))) != GBS_SUCCESS) {
     delete p;
     return rc;
   }
-  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamDefault) != cudaSuccess) {
-    delete p;
-    return GBS_CUDA_ERROR;
+  bool ok = cudaStreamCreateWithFlags(&p->stream, cudaStreamDefault) == cudaSuccess &&
+            cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; ok && k < kSideStreams; ++k) {
+    cudaEvent_t e = nullptr;
+    ok = cudaStreamCreateWithFlags(&p->side[k], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    p->ev_join.push_back(e);
   }
-  if (count > 0 && cudaMemcpy(p->items.p, items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
-    delete p;
+  if (!ok || (count > 0 && cudaMemcpy(p->items.p, items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice) != cudaSuccess)) {
+    gbs_batched_destroy(p);
     return GBS_CUDA_ERROR;
   }
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     load_cache();
-    for (int b = 0; b < 2; ++b) {
-      auto f = g_tune.find(tune_key(b ? 64 : 32, dtype));
-      if (f != g_tune.end()) p->warps[b] = f->second;
+    for (BucketPlan& b : p->buckets) {
+      auto f = g_tune.find(tune_key(b.kind, b.hi, dtype));
+      if (f == g_tune.end()) continue;
+      const std::vector<int> ch = lane_choices(b.kind, b.hi);
+      if (std::find(ch.begin(), ch.end(), f->second.lanes) == ch.end()) continue;
+      b.lanes = f->second.lanes;
+      b.warps = b.lanes == 32 ? f->second.warps : 1;
     }
   }
+  // largest total work first: its tail overlaps the smaller buckets
+  std::stable_sort(p->buckets.begin(), p->buckets.end(), [](const BucketPlan& x, const BucketPlan& y) { return x.cost > y.cost; });
   if ((rc = prepare(p)) != GBS_SUCCESS) {
     gbs_batched_destroy(p);
     return rc;
@@ -446,8 +590,14 @@ extern "C" int gbs_batched_destroy(gbs_batched* p)
 {
   if (!p) return GBS_SUCCESS;
   if (p->stream) cudaStreamSynchronize(p->stream);
-  if (p->exec) cudaGraphExecDestroy(p->exec);
-  if (p->graph) cudaGraphDestroy(p->graph);
+  for (int k = 0; k < kSideStreams; ++k)
+    if (p->side[k]) cudaStreamSynchronize(p->side[k]);
+  drop_graph(p);
+  for (cudaEvent_t e : p->ev_join)
+    if (e) cudaEventDestroy(e);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  for (int k = 0; k < kSideStreams; ++k)
+    if (p->side[k]) cudaStreamDestroy(p->side[k]);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
   return GBS_SUCCESS;
@@ -470,14 +620,9 @@ extern "C" int gbs_batched_solve(gbs_batched* p, void* d_a, void* d_b, int* d_in
   if (p->count == 0) return GBS_SUCCESS;
   cudaStream_t s = (cudaStream_t)stream;     // NULL: the legacy default stream
   if (!p->use_graph) return enqueue(p, s, d_a, d_b, d_info, d_piv);
-  if (p->exec && (p->g_a != d_a || p->g_b != d_b || p->g_info != d_info || p->g_piv != d_piv)) {
-    cudaGraphExecDestroy(p->exec);
-    cudaGraphDestroy(p->graph);
-    p->exec = nullptr;
-    p->graph = nullptr;
-  }
+  if (p->exec && (p->g_a != d_a || p->g_b != d_b || p->g_info != d_info || p->g_piv != d_piv)) drop_graph(p);
   if (!p->exec) {
-    // capture on the plan's own stream (counter reset + both bucket kernels)
+    // capture on the plan's own stream (counter reset + the bucket kernels)
     GBS_CUDA_TRY(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     int rc = enqueue(p, p->stream, d_a, d_b, d_info, d_piv);
     cudaGraph_t g = nullptr;
@@ -496,63 +641,130 @@ extern "C" int gbs_batched_solve(gbs_batched* p, void* d_a, void* d_b, int* d_in
   return GBS_SUCCESS;
 }
 
-// Times each candidate CTA shape per bucket on the caller's batch (the data
-// are re-factored, so pass scratch copies) and keeps the fastest.
+// Coordinate descent over the buckets' variants (lanes per system, and warps
+// per CTA for one warp per system) on the whole concurrent batch: each bucket
+// in turn tries every allowed variant and keeps one that lowers the batch's
+// time by more than 1 %.  Every timed run starts from the caller's input
+// (kept in a scratch copy), and the buffers hold that input again on return.
 extern "C" int gbs_batched_autotune(gbs_batched* p, void* d_a, void* d_b, int* d_info, int* d_piv, int persist)
 {
-  if (!p || p->count == 0) return GBS_INVALID_ARGUMENT;
+  if (!p || p->count == 0 || !d_a || !d_b || !d_info || !d_piv) return GBS_INVALID_ARGUMENT;
   cudaStream_t s = p->stream;
+  const size_t esz = p->dtype == GBS_F64 ? 8 : 4;
+  const size_t abytes = (size_t)p->total_a * esz, bbytes = (size_t)p->total_b * esz;
+  DevBuf a0, b0;
+  GBS_TRY(a0.reserve(abytes));
+  GBS_TRY(b0.reserve(bbytes));
+  GBS_CUDA_TRY(cudaMemcpyAsync(a0.p, d_a, abytes, cudaMemcpyDeviceToDevice, s));
+  GBS_CUDA_TRY(cudaMemcpyAsync(b0.p, d_b, bbytes, cudaMemcpyDeviceToDevice, s));
   cudaEvent_t e0, e1;
   GBS_CUDA_TRY(cudaEventCreate(&e0));
   GBS_CUDA_TRY(cudaEventCreate(&e1));
-  int chosen[2] = {p->warps[0], p->warps[1]};
-  for (int b = 0; b < 2; ++b) {
-    if (p->nb[b] == 0) continue;
-    double best = 1e30;
-    int best_w = chosen[b];
-    for (int w : kWarpChoices) {
-      p->warps[0] = b == 0 ? w : chosen[0];
-      p->warps[1] = b == 1 ? w : chosen[1];
-      const size_t smem = (b == 0 ? (p->dtype == GBS_F64 ? smem_per_warp<double, 32>() : smem_per_warp<float, 32>())
-                                  : (p->dtype == GBS_F64 ? smem_per_warp<double, 64>() : smem_per_warp<float, 64>())) *
-                          w;
-      if (smem > 200 * 1024) continue;
-      GBS_TRY(prepare(p));
-      float ms = 0, tot = 0;
-      for (int rep = 0; rep < 3; ++rep) {
-        GBS_CUDA_TRY(cudaEventRecord(e0, s));
-        GBS_TRY(enqueue(p, s, d_a, d_b, d_info, d_piv));
-        GBS_CUDA_TRY(cudaEventRecord(e1, s));
-        GBS_CUDA_TRY(cudaEventSynchronize(e1));
-        GBS_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep) tot += ms;
-      }
-      if (tot < best) { best = tot; best_w = w; }
+  int rc = GBS_SUCCESS;
+  auto restore = [&]() {
+    if (rc == GBS_SUCCESS && (cudaMemcpyAsync(d_a, a0.p, abytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+                              cudaMemcpyAsync(d_b, b0.p, bbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess))
+      rc = GBS_CUDA_ERROR;
+  };
+  // best of `reps` runs of the whole batch, in ms
+  auto time_batch = [&](int reps) {
+    float best = 1e30f, ms = 0;
+    for (int r = 0; r < reps && rc == GBS_SUCCESS; ++r) {
+      restore();
+      if (rc == GBS_SUCCESS && cudaEventRecord(e0, s) != cudaSuccess) rc = GBS_CUDA_ERROR;
+      if (rc == GBS_SUCCESS) rc = enqueue(p, s, d_a, d_b, d_info, d_piv);
+      if (rc == GBS_SUCCESS && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = GBS_CUDA_ERROR;
+      best = std::min(best, ms);
     }
-    chosen[b] = best_w;
-    if (persist) {
+    return best;
+  };
+  time_batch(1);                                     // warm-up
+  float best = time_batch(3);
+  for (int bi = 0; bi < (int)p->buckets.size() && rc == GBS_SUCCESS; ++bi) {
+    BucketPlan& b = p->buckets[bi];
+    BucketPlan keep = b;
+    for (int lanes : lane_choices(b.kind, b.hi)) {
+      for (int w : kWarpChoices) {
+        if ((lanes != 32 && w != 1) || (lanes == keep.lanes && w == keep.warps)) continue;
+        b = keep;
+        b.lanes = lanes;
+        b.warps = w;
+        if ((p->dtype == GBS_F64 ? bucket_grid<double>(b) : bucket_grid<float>(b)) != GBS_SUCCESS) {
+          cudaGetLastError();
+          continue;                                  // does not fit
+        }
+        const float t = time_batch(3);
+        if (rc == GBS_SUCCESS && t < 0.99f * best) {
+          best = t;
+          keep = b;
+        }
+      }
+    }
+    b = keep;
+    if (rc == GBS_SUCCESS && persist) {
       std::lock_guard<std::mutex> lk(g_tune_mu);
-      store_cache(tune_key(b ? 64 : 32, p->dtype), best_w, best * 500.0);
+      store_cache(tune_key(b.kind, b.hi, p->dtype), {b.lanes, b.warps}, best * 1e3);
     }
   }
-  p->warps[0] = chosen[0];
-  p->warps[1] = chosen[1];
-  GBS_TRY(prepare(p));
+  restore();
+  if (rc == GBS_SUCCESS && cudaStreamSynchronize(s) != cudaSuccess) rc = GBS_CUDA_ERROR;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (p->exec) {
-    cudaGraphExecDestroy(p->exec);
-    cudaGraphDestroy(p->graph);
-    p->exec = nullptr;
-    p->graph = nullptr;
+  GBS_TRY(rc);
+  GBS_TRY(prepare(p));
+  drop_graph(p);
+  return GBS_SUCCESS;
+}
+
+// Warps per CTA of the first bucket with n <= 32 and of the first with n > 32.
+extern "C" int gbs_batched_config(const gbs_batched* p, int* warps_small, int* warps_large)
+{
+  if (!p) return GBS_INVALID_ARGUMENT;
+  int ws = 4, wl = 4;
+  bool fs = false, fl = false;
+  for (const BucketPlan& b : p->buckets) {
+    if (b.hi <= 32 && !fs) { ws = b.warps; fs = true; }
+    if (b.hi > 32 && !fl) { wl = b.warps; fl = true; }
+  }
+  if (warps_small) *warps_small = ws;
+  if (warps_large) *warps_large = wl;
+  return GBS_SUCCESS;
+}
+
+// The plan's buckets, 7 ints each: kind, smallest and largest size of the
+// class, items, largest size present, lanes per system, warps per CTA.
+extern "C" int gbs_batched_buckets(const gbs_batched* p, int capacity, int* count, int* desc)
+{
+  if (!p || !count || capacity < 0 || (capacity > 0 && !desc)) return GBS_INVALID_ARGUMENT;
+  *count = (int)p->buckets.size();
+  for (int i = 0; i < std::min(capacity, *count); ++i) {
+    const BucketPlan& b = p->buckets[i];
+    const int v[7] = {b.kind, b.lo, b.hi, b.count, b.maxn, b.lanes, b.warps};
+    std::copy(v, v + 7, desc + 7 * i);
   }
   return GBS_SUCCESS;
 }
 
-extern "C" int gbs_batched_config(const gbs_batched* p, int* warps_small, int* warps_large)
+// Sets the variant of bucket i (as listed by gbs_batched_buckets).
+extern "C" int gbs_batched_set_variant(gbs_batched* p, int bucket, int lanes, int warps)
 {
-  if (!p) return GBS_INVALID_ARGUMENT;
-  if (warps_small) *warps_small = p->warps[0];
-  if (warps_large) *warps_large = p->warps[1];
+  if (!p || bucket < 0 || bucket >= (int)p->buckets.size()) return GBS_INVALID_ARGUMENT;
+  BucketPlan& b = p->buckets[bucket];
+  const std::vector<int> ch = lane_choices(b.kind, b.hi);
+  if (std::find(ch.begin(), ch.end(), lanes) == ch.end()) return GBS_INVALID_ARGUMENT;
+  if (lanes == 32 ? std::find(std::begin(kWarpChoices), std::end(kWarpChoices), warps) == std::end(kWarpChoices)
+                  : warps != 1)
+    return GBS_INVALID_ARGUMENT;
+  const BucketPlan keep = b;
+  b.lanes = lanes;
+  b.warps = warps;
+  const int rc = p->dtype == GBS_F64 ? bucket_grid<double>(b) : bucket_grid<float>(b);
+  if (rc != GBS_SUCCESS) {
+    b = keep;
+    return rc;
+  }
+  drop_graph(p);
   return GBS_SUCCESS;
 }

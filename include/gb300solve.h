@@ -286,7 +286,10 @@ int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const double* b, 
  * the right-hand sides with the solutions, writes info[i] (-1 = success,
  * else the failing column (LLT) or first exactly-zero pivot (LU)) and, for LU
  * items, the 0-based transpositions at the item's right-hand-side offset of
- * d_piv.  With use_graph != 0 the launch is a CUDA graph replayed per call
+ * d_piv.  A failed LLT item (info >= 0) keeps its right-hand side; its
+ * columns left of the failing one hold L, the rest is unspecified (the
+ * reference's blocked LLT, n >= 32, leaves the failing block partly updated).
+ * With use_graph != 0 the launch is a CUDA graph replayed per call
  * (re-captured when the buffer pointers change). */
 typedef struct gbs_batched gbs_batched;
 int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, const int* sizes, const int* kinds,
@@ -296,13 +299,28 @@ int64_t gbs_batched_matrix_elements(const gbs_batched* plan);
 int64_t gbs_batched_rhs_elements(const gbs_batched* plan);
 int gbs_batched_offsets(const gbs_batched* plan, int64_t* a_offsets, int64_t* b_offsets);
 int gbs_batched_solve(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, void* stream);
-/* Times each candidate CTA shape (warps per CTA) per size bucket on the given
- * buffers (they are factored repeatedly: pass scratch copies), keeps the
- * fastest and, if persist != 0, appends it to the autotune cache
- * ($GBS_AUTOTUNE_CACHE, default ~/.gb300solve_autotune.jsonl), keyed by
- * (GPU, bucket, dtype). */
+/* The plan groups the items into buckets by kind and size class (LLT: n <= 8,
+ * 12, 16, 20, 24, 32, 64; LU: n <= 8, 12, 16, 24, 32, 48, 64).  Each bucket
+ * runs one variant: G lanes per system (G in {1, 2, 4, 8, 16}; 32 / G systems
+ * per warp, one warp per CTA) or one warp per system (lanes = 32, 1-8 warps
+ * per CTA); the buckets run concurrently.  gbs_batched_autotune searches the
+ * variants bucket by bucket (coordinate descent), timing the whole batch on
+ * the given buffers, each run from the buffers' input (kept in a scratch
+ * copy; the buffers hold it again on return); a variant is kept when it
+ * lowers the batch's time by more than 1 %.  With persist != 0 the choices
+ * are appended to the autotune cache ($GBS_AUTOTUNE_CACHE, default
+ * ~/.gb300solve_autotune.jsonl), keyed by (GPU, kind, size class, dtype);
+ * later plans start from the cached choice. */
 int gbs_batched_autotune(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, int persist);
+/* warps per CTA of the first bucket with n <= 32 and the first with n > 32 */
 int gbs_batched_config(const gbs_batched* plan, int* warps_small, int* warps_large);
+/* *count = number of buckets; desc gets min(capacity, *count) records of 7
+ * ints: kind, smallest and largest n of the class, items, largest n present,
+ * lanes per system, warps per CTA. */
+int gbs_batched_buckets(const gbs_batched* plan, int capacity, int* count, int* desc);
+/* Forces bucket i's variant (GBS_INVALID_ARGUMENT if it is not allowed for
+ * the bucket or does not fit in shared memory). */
+int gbs_batched_set_variant(gbs_batched* plan, int bucket, int lanes_per_system, int warps_per_cta);
 
 /* ------------------------------------------------------------------ medium batches + precision router
  * Batches of general systems with n in [1, 512], one CTA per matrix, packed

@@ -13,18 +13,18 @@ from eigen_gb300.batched import BatchedSolver
 pytestmark = pytest.mark.gpu
 
 
-def make_batch(count_spd, count_gen, seed, bad=True):
+def make_batch(count_spd, count_gen, seed, bad=True, spd_sizes=(3, 25), gen_sizes=(4, 65)):
     rng = np.random.default_rng(seed)
     sizes, kinds, mats, rhs = [], [], [], []
     for i in range(count_spd):
-        n = int(rng.integers(3, 25))
+        n = int(rng.integers(*spd_sizes))
         g = O.gauss(seed * 100000 + i, n, n)
         a = np.asfortranarray(g @ g.T + 0.1 * np.eye(n))
         if bad and i % 97 == 5:
             a[n // 2, n // 2] = -1.0          # not SPD: fails at column n // 2 (or earlier)
         sizes.append(n); kinds.append(0); mats.append(a); rhs.append(O.gauss(seed * 7 + i, n, 1)[:, 0])
     for i in range(count_gen):
-        n = int(rng.integers(4, 65))
+        n = int(rng.integers(*gen_sizes))
         a = O.gauss(seed * 200000 + i, n, n)
         if bad and i % 53 == 7:
             a[:, n // 3] = 0.0                # exactly singular
@@ -46,30 +46,82 @@ def run_batch(dtype, sizes, kinds, mats, rhs, use_graph=True, repeat=1):
     return bs, d_a.cpu().numpy(), d_b.cpu().numpy(), d_info.cpu().numpy(), d_piv.cpu().numpy()
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
-def test_batched_matches_oracle_item_by_item(dtype):
-    sizes, kinds, mats, rhs = make_batch(600, 300, seed=3)
-    bs, fa, fb, info, piv = run_batch(dtype, sizes, kinds, mats, rhs, repeat=2)
+def check_items(dtype, bs, sizes, kinds, mats, rhs, fa, fb, info, piv):
     ftol = 1e-12 if dtype == np.float64 else 2e-5
     for i, (n, k) in enumerate(zip(sizes, kinds)):
         a = np.asfortranarray(mats[i].astype(dtype))
         f, x = bs.unpack(fa, fb, i)
         if k == 0:
             fo, io = O.llt(a)
-            assert info[i] == io, (i, info[i], io)
+            assert info[i] == io, (i, n, info[i], io)
             assert np.array_equal(np.triu(f, 1), np.triu(a, 1))
-            assert np.linalg.norm(np.tril(f) - np.tril(fo)) <= ftol * np.linalg.norm(np.tril(fo)) * 10
+            # a failed factorization: from n = 32 on the reference's LLT is blocked (LLT.h:331-360,
+            # 8-column blocks for n < 128) and stops inside the failing block before its panel solve;
+            # compare the finished columns left of that block and the block's own rows
+            fl, fol = np.tril(f), np.tril(fo)
+            if io >= 0 and n >= 32:
+                k0 = io // 8 * 8
+                fl = np.concatenate([fl[:, :k0].ravel(), fl[k0:k0 + 8, k0:io].ravel()])
+                fol = np.concatenate([fol[:, :k0].ravel(), fol[k0:k0 + 8, k0:io].ravel()])
+            assert np.linalg.norm(fl - fol) <= ftol * np.linalg.norm(fol) * 10, (i, n)
             if io < 0:
                 xo = O.llt_solve(fo, rhs[i].astype(dtype))
-                assert np.linalg.norm(x - xo) <= 1e3 * ftol * np.linalg.norm(xo)
+                assert np.linalg.norm(x - xo) <= 1e3 * ftol * np.linalg.norm(xo), (i, n)
+            else:
+                assert np.array_equal(x, rhs[i].astype(dtype))      # a failed item keeps its right-hand side
         else:
             fo, tro, _, fz = O.lu(a)
-            assert info[i] == fz, (i, info[i], fz)
+            assert info[i] == fz, (i, n, info[i], fz)
             tr = piv[bs.b_off[i]:bs.b_off[i] + n]
-            assert np.array_equal(tr, tro), (i, tr, tro)
-            assert np.linalg.norm(f - fo) <= ftol * np.linalg.norm(fo) * 10
+            assert np.array_equal(tr, tro), (i, n, tr, tro)
+            assert np.linalg.norm(f - fo) <= ftol * np.linalg.norm(fo) * 10, (i, n)
             if fz < 0 and dtype == np.float64:
-                assert O.backward_error(mats[i], x.reshape(-1, 1), rhs[i].reshape(-1, 1)) < 1e-14
+                assert O.backward_error(mats[i], x.reshape(-1, 1), rhs[i].reshape(-1, 1)) < 1e-14, (i, n)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_batched_matches_oracle_item_by_item(dtype):
+    sizes, kinds, mats, rhs = make_batch(600, 300, seed=3)
+    bs, fa, fb, info, piv = run_batch(dtype, sizes, kinds, mats, rhs, repeat=2)
+    check_items(dtype, bs, sizes, kinds, mats, rhs, fa, fb, info, piv)
+
+
+LANE_CHOICES = (1, 2, 4, 8, 16, 32)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_batched_every_variant_matches_oracle(dtype):
+    """Every bucket (LLT and LU, n = 1..64) under each variant it allows:
+    G lanes per system or one warp per system."""
+    torch = pytest.importorskip("torch")
+    sizes, kinds, mats, rhs = make_batch(500, 400, seed=21, spd_sizes=(1, 65), gen_sizes=(1, 65))
+    bs = BatchedSolver(sizes, kinds, dtype=dtype)
+    buckets = bs.buckets()
+    assert sum(b["items"] for b in buckets) == len(sizes)
+    allowed = []
+    for i, b in enumerate(buckets):
+        ok = []
+        for lanes in LANE_CHOICES:
+            try:
+                bs.set_variant(i, lanes, 4 if lanes == 32 else 1)
+                ok.append(lanes)
+            except Exception:
+                pass
+        assert ok and 32 in ok, (b, ok)
+        allowed.append(ok)
+    a, b = bs.pack(mats, rhs)
+    for v in range(max(len(ok) for ok in allowed)):
+        for i, ok in enumerate(allowed):
+            lanes = ok[v % len(ok)]
+            bs.set_variant(i, lanes, 4 if lanes == 32 else 1)
+        d_a = torch.from_numpy(a.copy()).cuda()
+        d_b = torch.from_numpy(b.copy()).cuda()
+        d_info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+        d_piv = torch.zeros(max(bs.b_elems, 1), dtype=torch.int32, device="cuda")
+        bs.solve(d_a, d_b, d_info, d_piv)
+        torch.cuda.synchronize()
+        check_items(dtype, bs, sizes, kinds, mats, rhs, d_a.cpu().numpy(), d_b.cpu().numpy(), d_info.cpu().numpy(),
+                    d_piv.cpu().numpy())
 
 
 def test_batched_without_graph_equals_with_graph():
@@ -90,6 +142,7 @@ def test_batched_autotune_keeps_results():
                   torch.zeros(bs.b_elems, dtype=torch.int32, device="cuda"))
     cfg = bs.autotune(*mk(), persist=False)
     assert cfg["warps_per_cta_n<=32"] in (1, 2, 4, 8) and cfg["warps_per_cta_n<=64"] in (1, 2, 4, 8)
+    assert all(b["lanes_per_system"] in (1, 2, 4, 8, 16, 32) for b in cfg["buckets"])
     d_a, d_b, d_info, d_piv = mk()
     bs.solve(d_a, d_b, d_info, d_piv)
     torch.cuda.synchronize()
