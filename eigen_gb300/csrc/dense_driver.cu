@@ -189,8 +189,16 @@ static int gemm_sub(cudaStream_t s, int phase, int M, int N, int K, const T* A, 
   const double flops = (lower ? 1.0 : 2.0) * M * (double)N * K + (lower ? (double)M * K : 0.0);
   const double bytes = sizeof(T) * ((double)M * K + (double)K * N + (lower ? 1.0 : 2.0) * M * (double)N);
   PhaseScope ps(s, phase, flops, bytes);
-  gemm_sub_kernel<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(
-      M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower, stop_flag);
+  if ((int64_t)grid.x * grid.y < device_sm_count()) {
+    // fewer 64 x 64 tiles than SMs: 32 x 32 tiles put the update on up to
+    // four times as many SMs (an SM's FP64 rate, not bandwidth, bounds it)
+    dim3 g2(ceil_div(N, 32), ceil_div(M, 32));
+    gemm_sub_kernel<T, 32, 32, BK, 2, 2><<<g2, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower,
+                                                           stop_flag);
+  } else {
+    gemm_sub_kernel<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(
+        M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower, stop_flag);
+  }
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }
@@ -385,8 +393,9 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
   if (!attr_set) {
     size_t diag = sizeof(T) * max_bs * (max_bs + 1);
     GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag));
-    size_t trs = sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 64);
-    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trs));
+    size_t trs = sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 32 + max_bs);
+    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_blocked_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)trs));
     attr_set = true;
   }
   if (n < 32) {
@@ -413,8 +422,8 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
       T* A21 = Akk + b;
       {
       PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, sizeof(T) * 2.0 * rs * b);
-      trsm_rlt_kernel<T, 64><<<ceil_div(rs, 64), 64, sizeof(T) * (b * (b + 1) + b * 64), s>>>(Akk, lda, b, A21, lda,
-                                                                                             rs, dSt);
+      trsm_rlt_blocked_kernel<T, 32><<<ceil_div(rs, 32), 256, sizeof(T) * (b * (b + 1) + b * 32 + b), s>>>(
+          Akk, lda, b, A21, lda, rs, dSt);
       GBS_CUDA_TRY(cudaGetLastError());
       }
       T* A22 = A21 + (int64_t)b * lda;

@@ -15,6 +15,8 @@
 //   norm kernels         ||A||_1 (PartialPivLU.h:522, LLT.h:434-445)
 #pragma once
 
+#include <type_traits>
+
 #include <math.h>
 
 #include "gbs_common.cuh"
@@ -314,13 +316,35 @@ gemm_sub_kernel(int M, int N, int K, const T* __restrict__ A, int64_t a_rs, int6
 // --------------------------------------------------------------------- LLT diag
 // Cholesky of the bs x bs diagonal block in shared memory, the reference's
 // unblocked algorithm (LLT.h:305-328: x = a_kk - ||l_k||^2, fail if x <= 0,
-// x = sqrt(x), column divided by x) in right-looking order: after column k is
-// final its rank-1 update goes to the whole trailing triangle at once, so each
-// column costs three barriers and (bs - k)^2 / 2 independent FMAs spread over
-// the CTA.  On failure writes k0 + k into st->info and writes back only the
-// columns already final (the trailing columns in global memory were never
-// touched, as the reference's early return leaves them).  Only the lower
-// triangle is read or written.  Dynamic smem: bs*(bs+1)*sizeof(T).
+// x = sqrt(x), column divided by x) in right-looking order with a one-column
+// look-ahead: while warps 1.. apply column k to the trailing columns k+2..,
+// warp 0 applies it to column k+1 alone, then checks, square-roots and scales
+// column k+1, so one barrier per column separates the steps and the square
+// root overlaps the bulk of the update.  Every element sees the same FMAs in
+// the same order as in a plain right-looking sweep.  In FP64 the column is
+// scaled by the reciprocal square root (within an ulp of the reference's
+// division, one long-latency sequence instead of two); FP32 divides by the
+// square root as the reference does.  On failure writes k0 + k into st->info
+// and writes back only the columns already final (the trailing columns in
+// global memory were never touched, as the reference's early return leaves
+// them).  Only the lower triangle is read or written.
+// Dynamic smem: bs*(bs+1)*sizeof(T); 256 threads, bs <= 128.
+template <typename T>
+__device__ __forceinline__ bool llt_diag_column(T* s, int ld, int bs, int k, int lane)
+{
+  const T d = s[k * ld + k];
+  if (!(d > T(0)) && !(d != d)) return false;         // x <= 0 (a NaN does not fail, as in the reference)
+  if constexpr (std::is_same<T, double>::value) {
+    const T r = rsqrt(d);
+    for (int i = k + 1 + lane; i < bs; i += 32) s[k * ld + i] *= r;
+  } else {
+    const T x = sqrt(d);
+    for (int i = k + 1 + lane; i < bs; i += 32) s[k * ld + i] = s[k * ld + i] / x;
+  }
+  if (lane == 0) s[k * ld + k] = sqrt(d);
+  return true;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* st)
@@ -329,40 +353,49 @@ potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = (T*)smem_raw;
   const int ld = bs + 1;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  __shared__ int s_fail;
   for (int e = tid; e < bs * bs; e += nt) {
     const int i = e % bs, j = e / bs;
     if (i >= j) s[j * ld + i] = a[(int64_t)j * lda + i];
   }
+  if (tid == 0) s_fail = -1;
   __syncthreads();
-  __shared__ T s_x;
-  __shared__ int s_fail;
+  if (warp == 0 && !llt_diag_column(s, ld, bs, 0, lane) && lane == 0) s_fail = 0;
+  __syncthreads();
+  const int t = tid - 32, nw = nt - 32;                 // threads of warps 1..: four per row
+  const int rsub = t % (nw / 4), csub = t / (nw / 4), rstep = nw / 4;
   for (int k = 0; k < bs; ++k) {
-    if (tid == 0) {
-      const T x = s[k * ld + k];
-      const int fail = !(x > T(0)) && !(x != x) ? 1 : 0;   // x <= 0 (a NaN does not fail, as in the reference)
-      s_fail = fail;
-      const T r = fail ? x : sqrt(x);
-      s_x = r;
-      if (!fail) s[k * ld + k] = r;
-    }
-    __syncthreads();
-    if (s_fail) {
-      if (tid == 0) st->info = k0 + k;
-      for (int e = tid; e < bs * k; e += nt) {
+    const int f = s_fail;
+    if (f >= 0) {                                       // column f failed; columns < f are final
+      if (tid == 0) st->info = k0 + f;
+      for (int e = tid; e < bs * f; e += nt) {
         const int i = e % bs, j = e / bs;
         if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
       }
       return;
     }
-    const T x = s_x;
-    for (int i = k + 1 + tid; i < bs; i += nt) s[k * ld + i] = s[k * ld + i] / x;
-    __syncthreads();
-    {
-      const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;   // warp per column, lanes down the rows
-      for (int j = k + 1 + w; j < bs; j += nw) {
-        const T ljk = s[k * ld + j];
-        for (int i = j + lane; i < bs; i += 32) s[j * ld + i] = fma(-s[k * ld + i], ljk, s[j * ld + i]);
+    if (k + 1 >= bs) break;
+    if (warp == 0) {
+      // column k+1: a_{i,k+1} -= l_ik l_{k+1,k}, then its own step
+      const T lj = s[k * ld + k + 1];
+      for (int i = k + 1 + lane; i < bs; i += 32) s[(k + 1) * ld + i] = fma(-s[k * ld + i], lj, s[(k + 1) * ld + i]);
+      __syncwarp();
+      if (!llt_diag_column(s, ld, bs, k + 1, lane) && lane == 0) s_fail = k + 1;
+    } else {
+      // columns k+2..: a_ij -= l_ik l_jk for k+2 <= j <= i
+      for (int i = k + 2 + rsub; i < bs; i += rstep) {
+        const T lik = s[k * ld + i];
+        int j = k + 2 + csub;
+        for (; j + 12 <= i; j += 16) {
+          const T l0 = s[k * ld + j], l1 = s[k * ld + j + 4], l2 = s[k * ld + j + 8], l3 = s[k * ld + j + 12];
+          const T a0 = s[j * ld + i], a1 = s[(j + 4) * ld + i], a2 = s[(j + 8) * ld + i], a3 = s[(j + 12) * ld + i];
+          s[j * ld + i] = fma(-lik, l0, a0);
+          s[(j + 4) * ld + i] = fma(-lik, l1, a1);
+          s[(j + 8) * ld + i] = fma(-lik, l2, a2);
+          s[(j + 12) * ld + i] = fma(-lik, l3, a3);
+        }
+        for (; j <= i; j += 4) s[j * ld + i] = fma(-lik, s[k * ld + j], s[j * ld + i]);
       }
     }
     __syncthreads();
@@ -375,7 +408,10 @@ potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* 
 
 // --------------------------------------------------------------------- LLT TRSM
 // X(m x bs) <- X L^{-T}, L lower bs x bs.  One thread per row of X; the CTA's
-// rows and L live in shared memory.  Dynamic smem: (bs*(bs+1) + bs*RT)*sizeof(T).
+// rows and L live in shared memory; in FP64 the reciprocals of L's diagonal
+// are taken once per CTA, so a column step is a dot product and a multiply
+// (FP32 divides, as the reference does).
+// Dynamic smem: (bs*(bs+1) + bs*RT + bs)*sizeof(T).
 template <typename T, int RT>
 __global__ void __launch_bounds__(RT)
 trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X, int64_t ldx, int m,
@@ -385,11 +421,13 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sL = (T*)smem_raw;              // sL[j*(bs+1) + l] = L(j,l)
   T* sX = sL + bs * (bs + 1);        // sX[c*RT + t]
+  T* sR = sX + bs * RT;              // sR[j] = 1 / L(j,j)
   const int ldL = bs + 1;
   for (int e = threadIdx.x; e < bs * bs; e += RT) {
     int j = e % bs, l = e / bs;
     if (j >= l) sL[j * ldL + l] = L[(int64_t)l * ldl + j];
   }
+  for (int j = threadIdx.x; j < bs; j += RT) sR[j] = std::is_same<T, double>::value ? T(1) / L[(int64_t)j * ldl + j] : L[(int64_t)j * ldl + j];
   const int r0 = blockIdx.x * RT;
   for (int e = threadIdx.x; e < bs * RT; e += RT) {
     int t = e % RT, c = e / RT;
@@ -408,13 +446,89 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
       s3 = fma(-sX[(l + 3) * RT + t], sL[j * ldL + l + 3], s3);
     }
     for (; l < j; ++l) s0 = fma(-sX[l * RT + t], sL[j * ldL + l], s0);
-    sX[j * RT + t] = ((s0 + s1) + (s2 + s3)) / sL[j * ldL + j];
+    const T sj = (s0 + s1) + (s2 + s3);
+    if constexpr (std::is_same<T, double>::value) sX[j * RT + t] = sj * sR[j];   // FP64: no division on the chain
+    else sX[j * RT + t] = sj / sR[j];
   }
   __syncthreads();
   for (int e = threadIdx.x; e < bs * RT; e += RT) {
     int tt = e % RT, c = e / RT;
     int r = r0 + tt;
     if (r < m) X[(int64_t)c * ldx + r] = sX[c * RT + tt];
+  }
+}
+
+// X(m x bs) <- X L^{-T} in 16-column blocks, for latency: per block, every
+// (row, column) pair first subtracts the finished columns' contribution (a
+// dot product, all pairs in parallel), then one thread per row finishes the
+// block right-looking in registers (a multiply and one FMA per column on the
+// dependent chain).  RT rows per CTA, 256 threads, bs <= 128, bs % 16 == 0
+// or the last block narrower.  FP64 multiplies by the reciprocals of L's
+// diagonal, FP32 divides.  Dynamic smem: (bs*(bs+1) + bs*RT + bs)*sizeof(T).
+template <typename T, int RT>
+__global__ void __launch_bounds__(256)
+trsm_rlt_blocked_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X, int64_t ldx, int m,
+                        const DeviceStatus* st)
+{
+  constexpr int W = 16;
+  constexpr bool kRecip = std::is_same<T, double>::value;
+  if (st && ld_volatile_i32(&st->info) >= 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sL = (T*)smem_raw;              // sL[j*(bs+1) + l] = L(j,l)
+  T* sX = sL + bs * (bs + 1);        // sX[c*RT + t]
+  T* sR = sX + bs * RT;              // FP64: 1 / L(j,j); FP32: L(j,j)
+  const int ldL = bs + 1, tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < bs * bs; e += nt) {
+    const int j = e % bs, l = e / bs;
+    if (j >= l) sL[j * ldL + l] = L[(int64_t)l * ldl + j];
+  }
+  for (int j = tid; j < bs; j += nt) sR[j] = kRecip ? T(1) / L[(int64_t)j * ldl + j] : L[(int64_t)j * ldl + j];
+  const int r0 = blockIdx.x * RT;
+  for (int e = tid; e < bs * RT; e += nt) {
+    const int t = e % RT, c = e / RT;
+    const int r = r0 + t;
+    sX[c * RT + t] = r < m ? X[(int64_t)c * ldx + r] : T(0);
+  }
+  __syncthreads();
+  for (int jb = 0; jb < bs; jb += W) {
+    const int wb = min(W, bs - jb);
+    if (jb > 0) {
+      for (int e = tid; e < RT * wb; e += nt) {       // x_rc -= sum_{l < jb} x_rl L(c,l)
+        const int t = e % RT, c = jb + e / RT;
+        T s0 = sX[c * RT + t], s1 = T(0), s2 = T(0), s3 = T(0);
+        for (int l = 0; l < jb; l += 4) {
+          s0 = fma(-sX[l * RT + t], sL[c * ldL + l], s0);
+          s1 = fma(-sX[(l + 1) * RT + t], sL[c * ldL + l + 1], s1);
+          s2 = fma(-sX[(l + 2) * RT + t], sL[c * ldL + l + 2], s2);
+          s3 = fma(-sX[(l + 3) * RT + t], sL[c * ldL + l + 3], s3);
+        }
+        sX[c * RT + t] = (s0 + s1) + (s2 + s3);
+      }
+      __syncthreads();
+    }
+    if (tid < RT) {                                   // the block's own columns, right-looking
+      T x[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) x[c] = c < wb ? sX[(jb + c) * RT + tid] : T(0);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        if (c < wb) {
+          x[c] = kRecip ? x[c] * sR[jb + c] : x[c] / sR[jb + c];
+#pragma unroll
+          for (int c2 = c + 1; c2 < W; ++c2)
+            if (c2 < wb) x[c2] = fma(-x[c], sL[(jb + c2) * ldL + jb + c], x[c2]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < W; ++c)
+        if (c < wb) sX[(jb + c) * RT + tid] = x[c];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < bs * RT; e += nt) {
+    const int t = e % RT, c = e / RT;
+    const int r = r0 + t;
+    if (r < m) X[(int64_t)c * ldx + r] = sX[c * RT + t];
   }
 }
 
@@ -593,15 +707,22 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
     }
     __syncthreads();
     if (warp < nrhs) {
-      T yl[PER];
+      // FP64: reciprocals of the diagonal, taken off the substitution's chain
+      // (within an ulp of the division); FP32 divides
+      constexpr bool kRecip = std::is_same<T, double>::value;
+      T yl[PER], rd[PER];
 #pragma unroll
-      for (int p = 0; p < PER; ++p) yl[p] = sY[lane + 32 * p][warp];
+      for (int p = 0; p < PER; ++p) {
+        yl[p] = sY[lane + 32 * p][warp];
+        rd[p] = (unit || lane + 32 * p >= ni) ? T(1) : kRecip ? T(1) / sD[lane + 32 * p][lane + 32 * p]
+                                                                : sD[lane + 32 * p][lane + 32 * p];
+      }
       if (forward) {
 #pragma unroll
         for (int r = 0; r < NB; ++r) {
           if (r < ni) {
-            T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
-            if (!unit) xr = xr / sD[r][r];
+            const T yr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32), dr = __shfl_sync(0xffffffffu, rd[r / 32], r % 32);
+            const T xr = kRecip ? yr * dr : yr / dr;
 #pragma unroll
             for (int p = 0; p < PER; ++p) {
               const int row = lane + 32 * p;
@@ -614,8 +735,8 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
 #pragma unroll
         for (int r = NB - 1; r >= 0; --r) {
           if (r < ni) {
-            T xr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32);
-            if (!unit) xr = xr / sD[r][r];
+            const T yr = __shfl_sync(0xffffffffu, yl[r / 32], r % 32), dr = __shfl_sync(0xffffffffu, rd[r / 32], r % 32);
+            const T xr = kRecip ? yr * dr : yr / dr;
 #pragma unroll
             for (int p = 0; p < PER; ++p) {
               const int row = lane + 32 * p;

@@ -490,7 +490,7 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
     GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(sizeof(float) * max_bs * (max_bs + 1))));
     GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64))));
+                                      (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64 + max_bs))));
     attr = true;
   }
   int bs = n < 32 ? n : std::min(std::max((n / 8 / 16) * 16, 8), max_bs);
@@ -515,7 +515,7 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
         GBS_TRY(tc_gemm_sub(s, kind, rs, b, b, A21, 1, lda, minv.as<float>(), kMixedNB, 1, A21, lda, 0, st, tcw));
       } else {
         PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, 8.0 * rs * b);
-        trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64), s>>>(Akk, lda, b, A21,
+        trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64 + b), s>>>(Akk, lda, b, A21,
                                                                                                    lda, rs, st);
         GBS_CUDA_TRY(cudaGetLastError());
       }
