@@ -91,13 +91,14 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, int ma
         T x = S[k * LD + k] - p;
         if (x <= T(0)) { status = k; break; }
         x = sqrt(x);
+        const T rx = T(1) / x;           // one reciprocal per column: an FP64 division costs ~10 FMAs
 #pragma unroll
         for (int q = 0; q < RPL; ++q) {
           const int i = lane + 32 * q;
           if (i > k && i < n) {
             T s = T(0);
             for (int j = 0; j < k; ++j) s = fma(S[j * LD + i], S[j * LD + k], s);
-            S[k * LD + i] = (S[k * LD + i] - s) / x;
+            S[k * LD + i] = (S[k * LD + i] - s) * rx;
           }
         }
         __syncwarp();
@@ -105,10 +106,15 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, int ma
         __syncwarp();
       }
       if (status < 0) {
-        // L y = b, then L^T x = y (lane = row)
+        // L y = b, then L^T x = y (lane = row); reciprocals of the diagonal per row, in parallel
+        T rd[RPL];
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+          const int i = lane + 32 * q;
+          rd[q] = i < n ? T(1) / S[i * LD + i] : T(0);
+        }
         for (int k = 0; k < n; ++k) {
-          T yk = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
-          yk = yk / S[k * LD + k];
+          const T yk = __shfl_sync(0xffffffffu, pick(b, k), k % 32) * __shfl_sync(0xffffffffu, pick(rd, k), k % 32);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) {
             const int i = lane + 32 * q;
@@ -117,8 +123,7 @@ __global__ void batched_kernel(const Item* __restrict__ items, int count, int ma
           }
         }
         for (int k = n - 1; k >= 0; --k) {
-          T xk = __shfl_sync(0xffffffffu, pick(b, k), k % 32);
-          xk = xk / S[k * LD + k];
+          const T xk = __shfl_sync(0xffffffffu, pick(b, k), k % 32) * __shfl_sync(0xffffffffu, pick(rd, k), k % 32);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) {
             const int i = lane + 32 * q;
