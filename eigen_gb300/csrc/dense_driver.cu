@@ -391,7 +391,7 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
   static bool attr_set = false;
   const int max_bs = 128;
   if (!attr_set) {
-    size_t diag = sizeof(T) * max_bs * (max_bs + 1);
+    size_t diag = potrf_diag_smem<T>(max_bs);
     GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag));
     size_t trs = sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 32 + max_bs);
     GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_blocked_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -400,7 +400,7 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
   }
   if (n < 32) {
     PhaseScope ps(s, PH_POTRF_DIAG, (double)n * n * n / 3.0, sizeof(T) * (double)n * n);
-    potrf_diag_kernel<T><<<1, 256, sizeof(T) * n * (n + 1), s>>>(dA, lda, n, 0, dSt);
+    potrf_diag_kernel<T><<<1, 256, potrf_diag_smem<T>(n), s>>>(dA, lda, n, 0, dSt);
     GBS_CUDA_TRY(cudaGetLastError());
     return GBS_SUCCESS;
   }
@@ -415,7 +415,7 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
     T* Akk = dA + (int64_t)k * lda + k;
     {
       PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, sizeof(T) * (double)b * b);
-      potrf_diag_kernel<T><<<1, 256, sizeof(T) * b * (b + 1), s>>>(Akk, lda, b, k, dSt);
+      potrf_diag_kernel<T><<<1, 256, potrf_diag_smem<T>(b), s>>>(Akk, lda, b, k, dSt);
       GBS_CUDA_TRY(cudaGetLastError());
     }
     if (rs > 0) {

@@ -317,31 +317,46 @@ gemm_sub_kernel(int M, int N, int K, const T* __restrict__ A, int64_t a_rs, int6
 // Cholesky of the bs x bs diagonal block in shared memory, the reference's
 // unblocked algorithm (LLT.h:305-328: x = a_kk - ||l_k||^2, fail if x <= 0,
 // x = sqrt(x), column divided by x) in right-looking order with a one-column
-// look-ahead: while warps 1.. apply column k to the trailing columns k+2..,
+// look-ahead: while six warps apply column k to the trailing columns k+2..,
 // warp 0 applies it to column k+1 alone, then checks, square-roots and scales
 // column k+1, so one barrier per column separates the steps and the square
-// root overlaps the bulk of the update.  Every element sees the same FMAs in
-// the same order as in a plain right-looking sweep.  In FP64 the column is
+// root overlaps the bulk of the update.  The bulk is dealt out evenly: the
+// trailing triangle is a suffix of the packed column-major order, and a
+// table gives each packed element's (row, column), so every FP64 warp
+// instruction (64 cycles on GB300 whatever the active lanes) carries 32
+// elements.  Every element sees the same FMAs in the same order as in a
+// plain right-looking sweep.  In FP64 the column is
 // scaled by the reciprocal square root (within an ulp of the reference's
 // division, one long-latency sequence instead of two); FP32 divides by the
 // square root as the reference does.  On failure writes k0 + k into st->info
 // and writes back only the columns already final (the trailing columns in
 // global memory were never touched, as the reference's early return leaves
 // them).  Only the lower triangle is read or written.
-// Dynamic smem: bs*(bs+1)*sizeof(T); 256 threads, bs <= 128.
+// Dynamic smem: potrf_diag_smem<T>(bs) (the block and the element table);
+// 256 threads, bs <= 128.
 template <typename T>
-__device__ __forceinline__ bool llt_diag_column(T* s, int ld, int bs, int k, int lane)
+__host__ __device__ constexpr size_t potrf_diag_smem(int bs)
+{
+  return sizeof(T) * (size_t)bs * (bs + 1) + sizeof(unsigned short) * (size_t)(bs * (bs + 1) / 2);
+}
+
+// Column k's own step (warp 0): check, then scale.  FP64 keeps x_kk in sd[k]
+// and takes the diagonal's square roots at the end, all at once (a 730-cycle
+// sqrt per column would sit on warp 0's chain); FP32 writes sqrt(x_kk).
+template <typename T>
+__device__ __forceinline__ bool llt_diag_column(T* s, T* sd, int ld, int bs, int k, int lane)
 {
   const T d = s[k * ld + k];
   if (!(d > T(0)) && !(d != d)) return false;         // x <= 0 (a NaN does not fail, as in the reference)
   if constexpr (std::is_same<T, double>::value) {
     const T r = rsqrt(d);
     for (int i = k + 1 + lane; i < bs; i += 32) s[k * ld + i] *= r;
+    if (lane == 0) sd[k] = d;
   } else {
     const T x = sqrt(d);
     for (int i = k + 1 + lane; i < bs; i += 32) s[k * ld + i] = s[k * ld + i] / x;
+    if (lane == 0) s[k * ld + k] = x;
   }
-  if (lane == 0) s[k * ld + k] = sqrt(d);
   return true;
 }
 
@@ -355,19 +370,38 @@ potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* 
   const int ld = bs + 1;
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   __shared__ int s_fail;
+  __shared__ T sd[128];                                 // FP64: x_kk, square-rooted at the end
+  // tab[e] = (i << 8) | j for the e-th element (i >= j) of the packed
+  // column-major lower triangle: the trailing triangle of step k (j >= k+2)
+  // is the suffix from pstart(k+2), so the update deals it out evenly
+  const int tot = bs * (bs + 1) / 2;
+  unsigned short* tab = (unsigned short*)(s + bs * ld);
+  auto pstart = [bs](int j) { return j * bs - j * (j - 1) / 2; };
   for (int e = tid; e < bs * bs; e += nt) {
     const int i = e % bs, j = e / bs;
     if (i >= j) s[j * ld + i] = a[(int64_t)j * lda + i];
   }
+  for (int j = warp; j < bs; j += nt / 32)
+    for (int i = j + lane; i < bs; i += 32) tab[pstart(j) + i - j] = (unsigned short)((i << 8) | j);
   if (tid == 0) s_fail = -1;
   __syncthreads();
-  if (warp == 0 && !llt_diag_column(s, ld, bs, 0, lane) && lane == 0) s_fail = 0;
+  if (warp == 0 && !llt_diag_column(s, sd, ld, bs, 0, lane) && lane == 0) s_fail = 0;
   __syncthreads();
-  const int t = tid - 32, nw = nt - 32;                 // threads of warps 1..: four per row
-  const int rsub = t % (nw / 4), csub = t / (nw / 4), rstep = nw / 4;
+  // the trailing update runs on warps 1-3 and 5-7: warp 4 would share warp 0's
+  // FP64 unit (sub-partition 0) and slow its chain
+  const int bw = warp < 4 ? warp - 1 : warp - 2;        // 0..5 for warps 1-3, 5-7
+  const int t = bw * 32 + lane, nw = 192;
+  auto finish_diag = [&](int upto) {                    // FP64: l_kk = sqrt(x_kk) for k < upto
+    if constexpr (std::is_same<T, double>::value) {
+      __syncthreads();
+      for (int k = tid; k < upto; k += nt) s[k * ld + k] = sqrt(sd[k]);
+      __syncthreads();
+    }
+  };
   for (int k = 0; k < bs; ++k) {
     const int f = s_fail;
     if (f >= 0) {                                       // column f failed; columns < f are final
+      finish_diag(f);
       if (tid == 0) st->info = k0 + f;
       for (int e = tid; e < bs * f; e += nt) {
         const int i = e % bs, j = e / bs;
@@ -381,25 +415,27 @@ potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* 
       const T lj = s[k * ld + k + 1];
       for (int i = k + 1 + lane; i < bs; i += 32) s[(k + 1) * ld + i] = fma(-s[k * ld + i], lj, s[(k + 1) * ld + i]);
       __syncwarp();
-      if (!llt_diag_column(s, ld, bs, k + 1, lane) && lane == 0) s_fail = k + 1;
-    } else {
-      // columns k+2..: a_ij -= l_ik l_jk for k+2 <= j <= i
-      for (int i = k + 2 + rsub; i < bs; i += rstep) {
-        const T lik = s[k * ld + i];
-        int j = k + 2 + csub;
-        for (; j + 12 <= i; j += 16) {
-          const T l0 = s[k * ld + j], l1 = s[k * ld + j + 4], l2 = s[k * ld + j + 8], l3 = s[k * ld + j + 12];
-          const T a0 = s[j * ld + i], a1 = s[(j + 4) * ld + i], a2 = s[(j + 8) * ld + i], a3 = s[(j + 12) * ld + i];
-          s[j * ld + i] = fma(-lik, l0, a0);
-          s[(j + 4) * ld + i] = fma(-lik, l1, a1);
-          s[(j + 8) * ld + i] = fma(-lik, l2, a2);
-          s[(j + 12) * ld + i] = fma(-lik, l3, a3);
-        }
-        for (; j <= i; j += 4) s[j * ld + i] = fma(-lik, s[k * ld + j], s[j * ld + i]);
+      if (!llt_diag_column(s, sd, ld, bs, k + 1, lane) && lane == 0) s_fail = k + 1;
+    } else if (warp != 4) {
+      // columns k+2..: a_ij -= l_ik l_jk for k+2 <= j <= i, two elements per thread at a time
+      int e = pstart(k + 2) + t;
+      for (; e + nw < tot; e += 2 * nw) {
+        const unsigned v0 = tab[e], v1 = tab[e + nw];
+        const int i0 = v0 >> 8, j0 = v0 & 255, i1 = v1 >> 8, j1 = v1 & 255;
+        const T a0 = s[j0 * ld + i0], a1 = s[j1 * ld + i1];
+        const T p0 = s[k * ld + i0], q0 = s[k * ld + j0], p1 = s[k * ld + i1], q1 = s[k * ld + j1];
+        s[j0 * ld + i0] = fma(-p0, q0, a0);
+        s[j1 * ld + i1] = fma(-p1, q1, a1);
+      }
+      if (e < tot) {
+        const unsigned v0 = tab[e];
+        const int i0 = v0 >> 8, j0 = v0 & 255;
+        s[j0 * ld + i0] = fma(-s[k * ld + i0], s[k * ld + j0], s[j0 * ld + i0]);
       }
     }
     __syncthreads();
   }
+  finish_diag(bs);
   for (int e = tid; e < bs * bs; e += nt) {
     const int i = e % bs, j = e / bs;
     if (i >= j) a[(int64_t)j * lda + i] = s[j * ld + i];
@@ -460,10 +496,10 @@ trsm_rlt_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X,
 
 // X(m x bs) <- X L^{-T} in 16-column blocks, for latency: per block, every
 // (row, column) pair first subtracts the finished columns' contribution (a
-// dot product, all pairs in parallel), then one thread per row finishes the
-// block right-looking in registers (a multiply and one FMA per column on the
-// dependent chain).  RT rows per CTA, 256 threads, bs <= 128, bs % 16 == 0
-// or the last block narrower.  FP64 multiplies by the reciprocals of L's
+// dot product, all pairs in parallel), then the block is finished
+// right-looking with its 16 columns spread over the 8 warps (a multiply, a
+// barrier and one FMA per step on the dependent chain).  RT <= 32 rows per
+// CTA, 256 threads, bs <= 128, the last block may be narrower.  FP64 multiplies by the reciprocals of L's
 // diagonal, FP32 divides.  Dynamic smem: (bs*(bs+1) + bs*RT + bs)*sizeof(T).
 template <typename T, int RT>
 __global__ void __launch_bounds__(256)
@@ -506,22 +542,30 @@ trsm_rlt_blocked_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restr
       }
       __syncthreads();
     }
-    if (tid < RT) {                                   // the block's own columns, right-looking
-      T x[W];
-#pragma unroll
-      for (int c = 0; c < W; ++c) x[c] = c < wb ? sX[(jb + c) * RT + tid] : T(0);
-#pragma unroll
-      for (int c = 0; c < W; ++c) {
-        if (c < wb) {
-          x[c] = kRecip ? x[c] * sR[jb + c] : x[c] / sR[jb + c];
-#pragma unroll
-          for (int c2 = c + 1; c2 < W; ++c2)
-            if (c2 < wb) x[c2] = fma(-x[c], sL[(jb + c2) * ldL + jb + c], x[c2]);
+    // the block's own columns, right-looking: warp w owns columns jb+w and
+    // jb+w+8 (lane = row); a step is the owner's multiply, a barrier, and
+    // one FMA per later column, so no warp issues the block's FMAs alone
+    {
+      const int w = tid >> 5, ln = tid & 31;
+      const int ca = w, cb = w + 8;                    // owned columns within the block
+      T xa = T(0), xb = T(0);
+      if (ln < RT) {
+        if (ca < wb) xa = sX[(jb + ca) * RT + ln];
+        if (cb < wb) xb = sX[(jb + cb) * RT + ln];
+      }
+      for (int c = 0; c < wb; ++c) {
+        if (ln < RT && (c == ca || c == cb)) {         // the owner finishes column c
+          T& xc = c == ca ? xa : xb;
+          xc = kRecip ? xc * sR[jb + c] : xc / sR[jb + c];
+          sX[(jb + c) * RT + ln] = xc;
+        }
+        __syncthreads();
+        if (ln < RT) {
+          const T xc = sX[(jb + c) * RT + ln];
+          if (ca > c && ca < wb) xa = fma(-xc, sL[(jb + ca) * ldL + jb + c], xa);
+          if (cb > c && cb < wb) xb = fma(-xc, sL[(jb + cb) * ldL + jb + c], xb);
         }
       }
-#pragma unroll
-      for (int c = 0; c < W; ++c)
-        if (c < wb) sX[(jb + c) * RT + tid] = x[c];
     }
     __syncthreads();
   }

@@ -488,7 +488,7 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
   const int max_bs = 128;
   if (!attr) {
     GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(float) * max_bs * (max_bs + 1))));
+                                      (int)potrf_diag_smem<float>(max_bs)));
     GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64 + max_bs))));
     attr = true;
@@ -500,7 +500,7 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
     float* Akk = As + (int64_t)k * lda + k;
     {
       PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
-      potrf_diag_kernel<float><<<1, 256, sizeof(float) * b * (b + 1), s>>>(Akk, lda, b, k, st);
+      potrf_diag_kernel<float><<<1, 256, potrf_diag_smem<float>(b), s>>>(Akk, lda, b, k, st);
       GBS_CUDA_TRY(cudaGetLastError());
     }
     if (rs > 0) {
