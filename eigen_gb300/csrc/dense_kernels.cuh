@@ -9,7 +9,8 @@
 //   gemm_sub_kernel      C -= op(A) op(B), optional lower-triangle-only mode for
 //                        SYRK (PartialPivLU.h:492, LLT.h:357)
 //   potrf_diag_kernel    Cholesky of one diagonal block (LLT.h:305-328), right-looking in smem
-//   trsm_rlt_kernel      A21 <- A21 L11^{-T} (LLT.h:356)
+//   trsm_rlt_kernel      A21 <- A21 L11^{-T} (LLT.h:356); trsm_rlt_blocked_kernel
+//                        the same in 16-column blocks (the plain path's latency)
 //   trsm_persistent_kernel  whole triangular solve in one launch (LLT.h:499-505,
 //                        PartialPivLU.h:224-271, TriangularSolverMatrix.h)
 //   norm kernels         ||A||_1 (PartialPivLU.h:522, LLT.h:434-445)
@@ -709,7 +710,8 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
         sX[kk][c] = (col < n && c < nrhs) ? __ldcg(&B[(int64_t)c * ldb + col]) : T(0);
       }
       __syncthreads();
-      for (int k0 = 0; k0 < K; k0 += NB) {   // one partial sum per tile: rounding grows with NB, not with n
+      for (int k0 = 0; k0 < K && ag < nrhs; k0 += NB) {   // one partial sum per tile: rounding grows with NB, not with n
+        // (groups beyond nrhs skip: an FP64 instruction costs its unit 64 cycles even on zero columns)
         T part[CPT];
 #pragma unroll
         for (int q = 0; q < CPT; ++q) part[q] = T(0);
@@ -734,7 +736,7 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
 #pragma unroll
       for (int q = 0; q < CPT; ++q) out[q] = T(0);
 #pragma unroll 8
-      for (int k = 0; k < NB; ++k) {
+      for (int k = 0; k < NB && ag < nrhs; ++k) {
         const T dv = sD[ar][k];
 #pragma unroll
         for (int q = 0; q < CPT; ++q) out[q] = fma(dv, sY[k][ag + q * G], out[q]);
