@@ -665,12 +665,21 @@ def run_batched(args):
                      "default_variants_ms": 1e3 * dflt,
                      "per_matrix_plain_gpu_solves_per_s": per_matrix, "cpu_oracle_solves_per_s": cpu,
                      "cpu_cores": O.num_threads()}
+    fp64_peak = gemm_peak(torch.float64)
+    tf = out["f64"]["tflops"]
     line = {"metric": METRIC, "value": out["f64"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["f64"]["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: SPD G G^T + 0.1 I (n 3..24), general iid N(0,1) (n 4..64), seeded",
             "config": {"workload": "batched: 100,000 LLT + 20,000 PartialPivLU, 1 RHS each, one CUDA-graph launch",
-                       "count": int(len(sizes))}, "batched": out}
+                       "count": int(len(sizes))},
+            "gpu_launches": len(out["f64"]["autotuned"]["buckets"]),
+            "roofline": {"bound": "fp64", "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tf / fp64_peak,
+                         "traffic": None,
+                         "peak_source": "cuBLAS DGEMM measured in this run (MEASURED_PEAKS.json lists no FP64 unit)",
+                         "note": "algorithmic flops per item: n^3/3 + 2n^2 (LLT), 2n^3/3 + 2n^2 (LU); one kernel "
+                                 "per size group, all in one graph"},
+            "batched": out}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -543,7 +543,7 @@ extern "C" int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, c
       b.first = (int)k;
       b.maxn = sizes[i];
       b.lanes = default_lanes(b.kind, b.hi);
-      b.warps = b.lanes == 32 ? 4 : 1;
+      b.warps = 1;                       // one-warp CTAs pack best (33 KB each for n <= 64)
       p->buckets.push_back(b);
     }
     BucketPlan& b = p->buckets.back();
