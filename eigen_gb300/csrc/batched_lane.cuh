@@ -1,20 +1,20 @@
 // Small-system kernels with G lanes per system (G in {1, 2, 4, 8, 16}): a
 // warp factors and solves 32 / G systems at once.
 //
-// On GB300 an FP64 warp instruction occupies the SM's FP64 units for 16
-// clocks whatever the number of active lanes, so the cost of a small
-// factorization is its count of FP64 warp instructions.  With one warp per
-// system (batched_kernel), every per-column step (square root, division,
-// pivot reduction) is a full warp instruction serving one system, and lanes
-// beyond n idle; with G lanes per system the same instruction serves 32 / G
-// systems and the trailing updates keep almost every lane busy.
+// On GB300 an FP64 warp instruction holds its sub-partition's FP64 unit for
+// 64 cycles whatever the number of active lanes (about 19 cycles per warp
+// instruction for the SM once all four sub-partitions issue), so the cost of
+// a small factorization is its count of FP64 warp instructions.  With one
+// warp per system (batched_kernel), every per-column step (square root,
+// division, pivot reduction) is a full warp instruction serving one system,
+// and lanes beyond n idle; with G lanes per system the same instruction
+// serves 32 / G systems and the trailing updates keep almost every lane busy.
 //
 // Layout: each warp has its own shared-memory slice; the element (r, c) of
 // the warp's system s sits at ((c * R + r / G) * kLS + s * G + r % G), R =
 // ceil(maxn / G) rows per lane, so lane s * G + g owns rows g, g + G, ...
 // Accesses of one (row slot, column) by all lanes are consecutive (no bank
-// conflicts); the stride kLS = 33 spreads the coalesced global loads (lanes
-// walk rows of one column) over the banks.
+// conflicts).  Each lane loads and stores its own rows.
 //
 // Arithmetic follows the reference's unblocked algorithms:
 //  * LU: unblocked_lu (PartialPivLU.h:365-409): first maximum of |a_ik|

@@ -189,12 +189,24 @@ static int gemm_sub(cudaStream_t s, int phase, int M, int N, int K, const T* A, 
   const double flops = (lower ? 1.0 : 2.0) * M * (double)N * K + (lower ? (double)M * K : 0.0);
   const double bytes = sizeof(T) * ((double)M * K + (double)K * N + (lower ? 1.0 : 2.0) * M * (double)N);
   PhaseScope ps(s, phase, flops, bytes);
-  if ((int64_t)grid.x * grid.y < device_sm_count()) {
-    // fewer 64 x 64 tiles than SMs: 32 x 32 tiles put the update on up to
-    // four times as many SMs (an SM's FP64 rate, not bandwidth, bounds it)
-    dim3 g2(ceil_div(N, 32), ceil_div(M, 32));
-    gemm_sub_kernel<T, 32, 32, BK, 2, 2><<<g2, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower,
-                                                           stop_flag);
+  const int64_t sms = device_sm_count();
+  if ((int64_t)grid.x * grid.y < sms) {
+    // fewer 64 x 64 tiles than SMs: smaller tiles spread the update over more
+    // SMs (an SM's FP64 rate, not bandwidth, bounds it).  Per-SM work in units
+    // of one 64 x 64 tile: ceil(tiles / SMs) x (tile area / 64^2); the smaller
+    // tile size wins ties.  Each element's sum runs over K in the same order
+    // whatever the tile, so the results are identical.
+    const int64_t t32 = (int64_t)ceil_div(N, 32) * ceil_div(M, 32), t16 = (int64_t)ceil_div(N, 16) * ceil_div(M, 16);
+    const double w32 = (double)((t32 + sms - 1) / sms) / 4.0, w16 = (double)((t16 + sms - 1) / sms) / 16.0;
+    if (w16 <= w32) {
+      dim3 g3(ceil_div(N, 16), ceil_div(M, 16));
+      gemm_sub_kernel<T, 16, 16, BK, 1, 1><<<g3, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower,
+                                                             stop_flag);
+    } else {
+      dim3 g2(ceil_div(N, 32), ceil_div(M, 32));
+      gemm_sub_kernel<T, 32, 32, BK, 2, 2><<<g2, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower,
+                                                             stop_flag);
+    }
   } else {
     gemm_sub_kernel<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(
         M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, lower, stop_flag);
