@@ -400,16 +400,16 @@ int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, Dev
 template <typename T>
 static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* dSt)
 {
-  static bool attr_set = false;
-  const int max_bs = 128;
-  if (!attr_set) {
-    size_t diag = potrf_diag_smem<T>(max_bs);
-    GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag));
-    size_t trs = sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 32 + max_bs);
-    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_blocked_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)trs));
-    attr_set = true;
-  }
+  constexpr int max_bs = 128;
+  static const cudaError_t attr = [] {         // once per process (thread-safe static initialisation)
+    cudaError_t e = cudaFuncSetAttribute(potrf_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)potrf_diag_smem<T>(max_bs));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsm_rlt_blocked_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * (max_bs * (max_bs + 1) + max_bs * 32 + max_bs)));
+    return e;
+  }();
+  GBS_CUDA_TRY(attr);
   if (n < 32) {
     PhaseScope ps(s, PH_POTRF_DIAG, (double)n * n * n / 3.0, sizeof(T) * (double)n * n);
     potrf_diag_kernel<T><<<1, 256, potrf_diag_smem<T>(n), s>>>(dA, lda, n, 0, dSt);
@@ -486,12 +486,9 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
   GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
   const int grid = std::min(nblk, 2 * device_sm_count());
   constexpr size_t smem = trsm_persistent_smem<T, NB, RC>();
-  static bool attr = false;
-  if (!attr) {
-    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_persistent_kernel<T, NB, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-    attr = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(trsm_persistent_kernel<T, NB, RC>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  GBS_CUDA_TRY(attr);
   for (int c0 = 0; c0 < nrhs; c0 += RC) {
     const int nc = std::min(RC, nrhs - c0);
     GBS_CUDA_TRY(cudaMemsetAsync(w.flags.p, 0, sizeof(int) * (size_t)(nblk + 2), s));

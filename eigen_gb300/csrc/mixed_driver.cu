@@ -484,15 +484,16 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kInvSmem));
-  static bool attr = false;
-  const int max_bs = 128;
-  if (!attr) {
-    GBS_CUDA_TRY(cudaFuncSetAttribute(potrf_diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)potrf_diag_smem<float>(max_bs)));
-    GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_rlt_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64 + max_bs))));
-    attr = true;
-  }
+  constexpr int max_bs = 128;
+  static const cudaError_t attr = [] {         // once per process (thread-safe static initialisation)
+    cudaError_t e = cudaFuncSetAttribute(potrf_diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)potrf_diag_smem<float>(max_bs));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsm_rlt_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(float) * (max_bs * (max_bs + 1) + max_bs * 64 + max_bs)));
+    return e;
+  }();
+  GBS_CUDA_TRY(attr);
   int bs = n < 32 ? n : std::min(std::max((n / 8 / 16) * 16, 8), max_bs);
   for (int k = 0; k < n; k += bs) {
     const int b = std::min(bs, n - k);

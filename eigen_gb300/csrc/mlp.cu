@@ -288,12 +288,9 @@ static int grad_pass(gbs_mlp* o, const float* d_x, const float* d_t, const int* 
   GBS_TRY(o->lossp.reserve(sizeof(double) * (size_t)nparts));
   cudaStream_t s = o->stream;
   const size_t smem = sizeof(float) * grad_smem_floats(o->in);
-  static bool attr = false;
-  if (!attr) {
-    GBS_CUDA_TRY(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(float) * grad_smem_floats(kMaxIn))));
-    attr = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)(sizeof(float) * grad_smem_floats(kMaxIn)));
+  GBS_CUDA_TRY(attr);
   {
     PhaseScope ps(s, PH_ROUTER, 6.0 * count * (double)o->P, 4.0 * count * (o->in + 1));
     mlp_grad_kernel<<<nparts, kSamplesPerCTA, smem, s>>>(o->in, o->params.as<float>(), d_x, d_t, d_idx, count, count,

@@ -28,12 +28,11 @@ static int launch_panel(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k
 template <typename T, int RPT>
 static int panel_capacity()
 {
-  static int cap = -1;
-  if (cap < 0) {
+  static const int cap = [] {                  // once per process (thread-safe static initialisation)
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_lu_kernel<T, kPanelNB, RPT>, kPanelThreads, 0);
-    cap = per_sm * device_sm_count();
-  }
+    return per_sm * device_sm_count();
+  }();
   return cap;
 }
 
@@ -41,9 +40,8 @@ static int panel_capacity()
 template <typename T, int RPT>
 static int cluster_panel_limit()
 {
-  static int lim = -1;
-  if (lim < 0) {
-    lim = 0;
+  static const int limit = [] {                // once per process (thread-safe static initialisation)
+    int lim = 0;
     const void* k = (const void*)panel_lu_cluster_kernel<T, kPanelNB, RPT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) cudaGetLastError();
     for (int c = kMaxPanelCluster; c >= 1 && lim == 0; c /= 2) {
@@ -61,8 +59,9 @@ static int cluster_panel_limit()
       if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters > 0) lim = c;
       else cudaGetLastError();
     }
-  }
-  return lim;
+    return lim;
+  }();
+  return limit;
 }
 
 template <typename T, int RPT>

@@ -484,11 +484,9 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   CUtensorMap tmA, tmB;
   GBS_TRY(make_tmap(&tmA, ws.ak.p, esize, M, Kp, ldk, BM));
   GBS_TRY(make_tmap(&tmB, ws.bk.p, esize, N, Kp, ldk, BN));
-  static bool attr = false;
-  if (!attr) {
-    GBS_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  GBS_CUDA_TRY(attr);
   TcParams p;
   p.M = M;
   p.N = N;
