@@ -133,3 +133,57 @@ def test_rcond_within_10x_of_truth():
         truth = 1.0 / (O.sym_l1_norm(s) * O.l1_norm(inv))
         est = O.llt_rcond(fl, O.sym_l1_norm(s))
         assert truth / 10 < est < truth * 10
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_batched_oracle_equals_the_pinned_per_item_oracle(dtype):
+    """The batched CPU baseline (the C4 oracle leg of bench.py) factors and
+    solves each item with the per-item oracle pinned above: identical bytes,
+    including failing and singular items."""
+    import ctypes as C
+    rng = np.random.default_rng(7)
+    sizes = [int(rng.integers(1, 65)) for _ in range(40)]
+    kinds = [i % 2 for i in range(40)]
+    mats, rhs = [], []
+    for i, (n, k) in enumerate(zip(sizes, kinds)):
+        if k == 0:
+            m = O.spd(500 + i, n)
+            if i % 7 == 3:
+                m[n // 2, n // 2] = -1.0                # not SPD
+        else:
+            m = O.gauss(600 + i, n, n)
+            if i % 9 == 5:
+                m[:, n // 3] = 0.0                      # exactly singular
+        mats.append(np.asfortranarray(m.astype(dtype)))
+        rhs.append(O.gauss(700 + i, n, 1)[:, 0].astype(dtype))
+    lib = O.port()
+    sfx = "d" if dtype == np.float64 else "s"
+    for kind in (0, 1):
+        idx = [i for i in range(40) if kinds[i] == kind]
+        ns = np.array([sizes[i] for i in idx], dtype=np.int32)
+        off = np.concatenate([[0], np.cumsum(ns.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+        roff = np.concatenate([[0], np.cumsum(ns.astype(np.int64))[:-1]]).astype(np.int64)
+        a = np.concatenate([mats[i].reshape(-1, order="F") for i in idx]).astype(dtype)
+        b = np.concatenate([rhs[i] for i in idx]).astype(dtype)
+        info = np.zeros(len(idx), dtype=np.int32)
+        if kind == 0:
+            getattr(lib, f"oracle_batched_llt_solve_{sfx}")(len(idx), ns, off, a.ctypes.data_as(C.c_void_p), roff,
+                                                              b.ctypes.data_as(C.c_void_p), info)
+        else:
+            tr = np.zeros(int(ns.sum()), dtype=np.int32)
+            getattr(lib, f"oracle_batched_lu_solve_{sfx}")(len(idx), ns, off, a.ctypes.data_as(C.c_void_p), roff,
+                                                             b.ctypes.data_as(C.c_void_p), tr, info)
+        for q, i in enumerate(idx):
+            n = sizes[i]
+            f = a[off[q]:off[q] + n * n].reshape((n, n), order="F")
+            x = b[roff[q]:roff[q] + n]
+            if kind == 0:
+                fo, io = O.llt(mats[i])
+                assert info[q] == io and np.array_equal(np.tril(f), np.tril(fo))
+                if io < 0:
+                    assert np.array_equal(x, O.llt_solve(fo, rhs[i].reshape(-1, 1))[:, 0], equal_nan=True)
+            else:
+                fo, tro, _, fz = O.lu(mats[i])
+                assert info[q] == fz and np.array_equal(f, fo)
+                assert np.array_equal(tr[roff[q]:roff[q] + n], tro)
+                assert np.array_equal(x, O.lu_solve(fo, tro, rhs[i].reshape(-1, 1))[:, 0], equal_nan=True)
