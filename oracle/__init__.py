@@ -1,8 +1,9 @@
 """CPU oracle for the dense factor-and-solve path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import this package, and only as the checker: the product
-(``eigen_gb300`` / ``libgb300solve.so``) never calls into it.
+``bench.py`` may import this package, and only to check results or time the
+CPU baseline: the product (``eigen_gb300`` / ``libgb300solve.so``) never calls
+into it.
 
 Two back ends with the same numpy-level API:
 

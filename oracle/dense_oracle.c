@@ -1,6 +1,6 @@
 /*
- * Test infrastructure: the CPU oracle (checker) for the dense factor-and-solve
- * path.  Not part of the product; only tests/, the smoke check and the
+ * Test infrastructure: the CPU oracle (results to compare against) for the
+ * dense factor-and-solve path.  Not part of the product; only tests/, the smoke check and the
  * benchmark's CPU-baseline leg load it.  See dense_oracle_impl.h for the
  * reference functions each routine restates.
  *

@@ -1,7 +1,8 @@
 /*
  * Test infrastructure: the CPU oracle for the dense factor-and-solve path.
  * Only the tests, the smoke check and the CPU-baseline leg of the benchmark use
- * this code, as the checker.  The product (libgb300solve) never links it.
+ * this code, to check results or time the baseline.  The product (libgb300solve)
+ * never links it.
  *
  * This file is included twice by dense_oracle.c, once with T=double and once
  * with T=float; SFX(name) appends the type suffix (_d / _s) and SQRT is the

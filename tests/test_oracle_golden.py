@@ -137,7 +137,7 @@ def test_rcond_within_10x_of_truth():
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
 def test_batched_oracle_equals_the_pinned_per_item_oracle(dtype):
-    """The batched CPU baseline (the C4 oracle leg of bench.py) factors and
+    """The batched CPU baseline (the oracle leg of bench.py --config batched) factors and
     solves each item with the per-item oracle pinned above: identical bytes,
     including failing and singular items."""
     import ctypes as C
