@@ -57,6 +57,9 @@ class BatchedSolver:
                                           C.c_void_p(s)), "batched.solve")
 
     def autotune(self, d_a, d_b, d_info, d_piv, persist=False):
+        """Chooses each size group's kernel variant by timing the whole batch
+        on these buffers; every run starts from their contents, which are
+        restored on return.  Returns config()."""
         L.check(L.lib().gbs_batched_autotune(self._h, C.c_void_p(d_a.data_ptr()), C.c_void_p(d_b.data_ptr()),
                                              C.c_void_p(d_info.data_ptr()), C.c_void_p(d_piv.data_ptr()),
                                              int(persist)), "batched.autotune")
