@@ -71,6 +71,10 @@ int device_sm_count()
 int DevBuf::reserve(size_t b)
 {
   if (b <= bytes && p) return GBS_SUCCESS;
+  if (borrowed) {
+    gbs_set_last_message("workspace request exceeds a fixed (borrowed) device buffer");
+    return GBS_INVALID_ARGUMENT;
+  }
   release();
   size_t want = std::max<size_t>(b, 256);
   cudaError_t e = cudaMalloc(&p, want);
@@ -87,7 +91,7 @@ int DevBuf::reserve(size_t b)
 
 void DevBuf::release()
 {
-  if (p) cudaFree(p);
+  if (p && !borrowed) cudaFree(p);
   p = nullptr;
   bytes = 0;
 }
@@ -396,6 +400,23 @@ int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, Dev
   return GBS_SUCCESS;
 }
 
+template <typename T>
+int getrf_preload()
+{
+  cudaFuncAttributes fa;
+  const void* kernels[] = {
+      (const void*)laswp_map_kernel,
+      (const void*)laswp_gather_kernel<T>,
+      (const void*)laswp_kernel<T>,
+      (const void*)trsm_lunit_kernel<T, kPanelNB>,
+      (const void*)gemm_sub_kernel<T, 64, 64, 16, 4, 4>,
+      (const void*)gemm_sub_kernel<T, 32, 32, 16, 2, 2>,
+      (const void*)gemm_sub_kernel<T, 16, 16, 16, 1, 1>,
+  };
+  for (const void* k : kernels) GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, k));
+  return panel_preload<T>();
+}
+
 // ------------------------------------------------------------------ LLT
 template <typename T>
 static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* dSt)
@@ -674,6 +695,7 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
 // ------------------------------------------------------------------ instantiations
 #define GBS_INSTANTIATE(T)                                                                                      \
   template int getrf_device<T>(cudaStream_t, int, int, T*, int64_t, int*, DeviceStatus*, DevBuf&);               \
+  template int getrf_preload<T>();                                                                              \
   template int potrf_device<T>(cudaStream_t, int, T*, int64_t, int, DeviceStatus*, DevBuf&);                     \
   template int tri_solve_device<T>(cudaStream_t, int, int, const T*, int64_t, int, int, int, T*, int64_t,       \
                                    SolveWork&, const T*);                                                    \

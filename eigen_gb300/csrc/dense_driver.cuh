@@ -15,10 +15,14 @@ namespace gbs {
 int ensure_device();
 int device_sm_count();
 
-// Growable device buffer; never shrinks.
+// Growable device buffer; never shrinks.  A borrowed buffer is a view of
+// memory someone else owns (the allocation-free LU's fixed array): reserve()
+// never allocates for it and fails with GBS_INVALID_ARGUMENT when asked for
+// more than it holds, and release() never frees it.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool borrowed = false;
   int reserve(size_t b);
   void release();
   template <typename U> U* as() const { return (U*)p; }
@@ -88,6 +92,16 @@ int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, i
 
 template <typename T>
 int getrf_device(cudaStream_t s, int m, int n, T* dA, int64_t lda, int* dTr, DeviceStatus* dSt, DevBuf& scratch);
+
+// Loads every kernel getrf_device<T> can launch, for any shape, and runs its
+// one-time capacity queries.  CUDA loads kernels lazily on their first launch,
+// and loading one can take device memory; a caller that must not allocate
+// later runs this once per device beforehand.  panel_preload<T> does the same
+// for the panel kernels (their own translation unit).
+template <typename T>
+int getrf_preload();
+template <typename T>
+int panel_preload();
 
 template <typename T>
 int potrf_device(cudaStream_t s, int n, T* dA, int64_t lda, int upper, DeviceStatus* dSt, DevBuf& tmp);

@@ -27,31 +27,6 @@ constexpr int kMaxDim = 65536;   // largest m and n accepted (panel scratch fits
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Host code may not use g_noalloc_scratch as an address: it names a host-side
-// stand-in.  The device address comes from cudaGetSymbolAddress, once per
-// device, with that device current.
-std::mutex g_addr_mu;
-std::vector<void*> g_addr;
-
-int scratch_address(void** out)
-{
-  int dev = 0;
-  GBS_CUDA_TRY(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(g_addr_mu);
-  if ((int)g_addr.size() <= dev) g_addr.resize(dev + 1, nullptr);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      gbs_set_last_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
-      return GBS_CUDA_ERROR;
-    }
-    g_addr[dev] = p;
-  }
-  *out = g_addr[dev];
-  return GBS_SUCCESS;
-}
-
 // The status word keeps the previous call's contents: start every call from
 // zero (barrier counters, timeout flag, swap count) with info = -1.
 __global__ void noalloc_reset_status(DeviceStatus* st)
@@ -74,6 +49,39 @@ __global__ void noalloc_finish(const DeviceStatus* st, int* ipiv, int size, int*
     if (st->timeout) *info = -(100 + GBS_TIMEOUT);
     else *info = st->info >= 0 ? st->info + 1 : 0;
   }
+}
+
+// Host code may not use g_noalloc_scratch as an address: it names a host-side
+// stand-in.  The device address comes from cudaGetSymbolAddress, once per
+// device, with that device current.
+std::mutex g_addr_mu;
+std::vector<void*> g_addr;
+
+int scratch_address(void** out)
+{
+  int dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_addr_mu);
+  if ((int)g_addr.size() <= dev) g_addr.resize(dev + 1, nullptr);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      gbs_set_last_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+      return GBS_CUDA_ERROR;
+    }
+    // Kernels load lazily on their first launch, which can take device
+    // memory.  Load here every kernel a call of any shape can launch (the
+    // cluster or the cooperative panel, each GEMM tile size, the interchange
+    // kernels), so later calls of other shapes load nothing.
+    cudaFuncAttributes fa;
+    GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)noalloc_reset_status));
+    GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)noalloc_finish));
+    GBS_TRY(getrf_preload<double>());
+    g_addr[dev] = p;
+  }
+  *out = g_addr[dev];
+  return GBS_SUCCESS;
 }
 
 }  // namespace
@@ -108,15 +116,13 @@ extern "C" int gbs_dgetrf_noalloc(int m, int n, double* d_a, int lda, int* d_ipi
   GBS_CUDA_TRY(cudaGetLastError());
   int rc = GBS_SUCCESS;
   if (size > 0) {
-    // A non-owning view of the static array: it is already large enough, so
-    // reserve() never allocates, and it is detached before destruction so
-    // nothing is freed.
+    // A borrowed view of the static array, which is large enough for every
+    // panel of this call (checked above).
     DevBuf view;
+    view.borrowed = true;      // reserve() refuses to grow it, release() never frees it
     view.p = (unsigned char*)base + kStatusBytes;
     view.bytes = kScratchBytes - kStatusBytes;
     rc = getrf_device<double>(s, m, n, d_a, lda, d_ipiv, st, view);
-    view.p = nullptr;
-    view.bytes = 0;
   }
   if (rc != GBS_SUCCESS) return rc;
   count_launch();

@@ -134,4 +134,20 @@ int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int*
   return launch_panel<T, 2>(s, a, lda, m, nbc, k0, tr, scratch, st, P);
 }
 
+template <typename T>
+int panel_preload()
+{
+  constexpr int rpt_max = sizeof(T) == 8 ? 1 : 2;
+  cudaFuncAttributes fa;
+  GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)panel_lu_kernel<T, kPanelNB, 1>));
+  GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)panel_lu_kernel<T, kPanelNB, 2>));
+  GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)panel_lu_cluster_kernel<T, kPanelNB, 1>));
+  GBS_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)panel_lu_cluster_kernel<T, kPanelNB, rpt_max>));
+  (void)panel_capacity<T, 1>();
+  (void)panel_capacity<T, 2>();
+  (void)cluster_panel_limit<T, 1>();
+  (void)cluster_panel_limit<T, rpt_max>();
+  return GBS_SUCCESS;
+}
+
 }  // namespace gbs

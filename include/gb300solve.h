@@ -128,8 +128,11 @@ int gbs_spotrs(const char* uplo, const int* n, const int* nrhs, const float* a, 
  * (each call resets what must start at zero): calls whose work overlaps on the
  * GPU (different streams, or several host threads) race on it and must be
  * serialized by the caller.  The first call on a device does the set-up for
- * that device (loading the kernels and looking up the array's device address),
- * so make it before any section that must not allocate.  Profiling
+ * that device: it loads every kernel that a call of any shape can launch (CUDA
+ * otherwise loads kernels lazily, on first launch, which can take device
+ * memory) and looks up the array's device address.  Make that first call
+ * before any section that must not allocate; later calls of any shape then
+ * allocate nothing.  Profiling
  * (gbs_profile_enable) must stay off, since it creates CUDA events. */
 int gbs_dgetrf_noalloc(int m, int n, double* d_a, int lda, int* d_ipiv, int* d_info, void* stream);
 

@@ -18,6 +18,29 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: large sizes (seconds of CPU oracle work)")
 
 
+_PARITY: list[tuple[str, str, float, float]] = []
+
+
+def record_parity(case: str, what: str, value: float, bound: float) -> None:
+    """Keeps an achieved error next to the bound it was asserted against; the
+    session's worst ratio per quantity is printed in the terminal summary."""
+    _PARITY.append((case, what, float(value), float(bound)))
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    if not _PARITY:
+        return
+    worst: dict[str, tuple[str, float, float]] = {}
+    for case, what, v, b in _PARITY:
+        r = v / b if b > 0 else 0.0
+        if what not in worst or r > worst[what][1] / max(worst[what][2], 1e-300):
+            worst[what] = (case, v, b)
+    terminalreporter.section("achieved parity (worst case per quantity)")
+    for what in sorted(worst):
+        case, v, b = worst[what]
+        terminalreporter.write_line(f"{what:44s} {v:9.2e}  bound {b:8.1e}  ({case})")
+
+
 def _has_gpu() -> bool:
     try:
         import torch

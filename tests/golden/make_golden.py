@@ -8,8 +8,11 @@ Writes tests/golden/eigen_dense.json (case list + scalars) and
 tests/golden/eigen_dense.npz (arrays).  Inputs are not stored: every case
 records the generator (oracle.gauss / oracle.uniform / oracle.spd with its
 seed), whose bytes are identical on every host.  Small cases store the full
-factors; large cases store pivots, solutions and a fixed sample of factor
-entries.
+factors; large cases store pivots, solutions, a fixed sample of factor entries
+and a sketch F R of the whole factor (R a seeded n x 4 or n x 8 Gaussian
+matrix).  Every case also records the noise floor of the reference's
+algorithm: the distance between the reference's factor and solution and those
+of the C restatement (same blocking, another rounding order).
 
 What each case pins (reference API used):
   lu    PartialPivLU<MatrixX?>(A): matrixLU(), permutationP().indices(),
@@ -43,6 +46,23 @@ def sample_idx(n: int) -> np.ndarray:
     return np.sort(rng.choice(n * n, size=min(SAMPLE, n * n), replace=False)).astype(np.int64)
 
 
+def sketch_cols(n: int) -> int:
+    return 4 if n > 4096 else 8
+
+
+def sketch_matrix(n: int) -> np.ndarray:
+    """R (n x k, seeded generator) of the factor sketch F R.  Every entry of
+    the factor enters the sketch, so ||(F - F_ref) R|| / ||F_ref R|| tracks the
+    relative Frobenius difference of the whole factor (a Gaussian random
+    projection), where the sampled entries see only 2048 of them."""
+    return O.gauss(77000 + n, n, sketch_cols(n))
+
+
+def rel(a: np.ndarray, b: np.ndarray) -> float:
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
 def gen(spec: dict) -> np.ndarray:
     k = spec["gen"]
     if k == "gauss":
@@ -63,6 +83,26 @@ def gen(spec: dict) -> np.ndarray:
         a[:, spec["col"]] = 0.0
     elif k == "ones":
         a = np.ones((spec["m"], spec["n"]), order="F")
+    elif k in ("tie_rows", "near_tie_rows"):
+        # `pairs` twin rows r, r+1 with row r+1 = -(row r) over the columns
+        # [0, c0 + pairs): both twins see the same operations, so their
+        # magnitudes stay equal through the first c0 elimination steps (many
+        # blocked updates).  The twins are small (x 1/8) before column c0 and
+        # dominant (x 64) in [c0, c0 + pairs), so at those steps the column
+        # maximum is a tie between twins, broken by the first-maximum rule.
+        # near_tie_rows scales the copy by (1 + 1e-10 g): the decision then
+        # rests on a margin of ~1e-10, far above the rounding noise, and must
+        # not depend on the operation order.  Beyond c0 + pairs the twins are
+        # independent, so the matrix is nonsingular.
+        a = O.gauss(spec["seed"], spec["m"], spec["n"])
+        p, c0 = spec["pairs"], spec["c0"]
+        rows = np.arange(p) * (spec["m"] // p)
+        a[rows, :c0] *= 0.125
+        a[rows, c0:c0 + p] *= 64.0
+        scale = np.ones(p)
+        if k == "near_tie_rows":
+            scale = 1.0 + 1e-10 * O.gauss(spec["seed"] + 1, p, 1)[:, 0]
+        a[rows + 1, :c0 + p] = -a[rows, :c0 + p] * scale[:, None]
     else:
         raise ValueError(k)
     if spec.get("dtype", "f64") == "f32":
@@ -73,6 +113,22 @@ def gen(spec: dict) -> np.ndarray:
 def rhs(spec: dict, nrhs: int) -> np.ndarray:
     b = O.gauss(spec["seed"] + 7919, spec["n"], nrhs)
     return np.asfortranarray(b.astype(np.float32)) if spec.get("dtype", "f64") == "f32" else b
+
+
+def tie_decisions(spec: dict, tr: np.ndarray) -> int:
+    """Steps at which the reference's pivot was one twin while the other twin
+    was still a candidate (an exact or 1e-10 tie decided by the rule)."""
+    p = spec["pairs"]
+    rows = np.arange(p) * (spec["m"] // p)
+    twin = {int(r): int(r) + 1 for r in rows}
+    twin.update({int(r) + 1: int(r) for r in rows})
+    order = list(range(spec["m"]))
+    ties = 0
+    for k, t in enumerate(tr):
+        order[k], order[t] = order[t], order[k]
+        if order[k] in twin and twin[order[k]] in order[k + 1:]:
+            ties += 1
+    return ties
 
 
 def lu_case(spec: dict, arrays: dict, name: str) -> dict:
@@ -91,6 +147,8 @@ def lu_case(spec: dict, arrays: dict, name: str) -> dict:
     getattr(lib, pre + "getrf_")(C.byref(m_), C.byref(n_), ag, C.byref(lda), ipiv, C.byref(info))
     out = dict(spec, kind="lu", rcond=rc, det=det, nb_transpositions=nbt, first_zero_pivot=fz,
                getrf_info=int(info.value), l1_norm=O.l1_norm(a))
+    if spec["gen"] in ("tie_rows", "near_tie_rows"):
+        out["tie_decisions"] = tie_decisions(spec, tr)
     arrays[name + "perm"] = perm.astype(np.int32)
     arrays[name + "tr"] = tr.astype(np.int32)
     arrays[name + "ipiv"] = ipiv[:n].astype(np.int32)
@@ -103,6 +161,15 @@ def lu_case(spec: dict, arrays: dict, name: str) -> dict:
         arrays[name + "lu_idx"] = idx
         arrays[name + "lu_val"] = fact.reshape(-1, order="F")[idx]
         arrays[name + "lu_diag"] = np.diag(fact).copy()
+        arrays[name + "lu_sketch"] = fact.astype(np.float64) @ sketch_matrix(n)
+    # the noise floor: the C restatement of the same algorithm (same blocking,
+    # other rounding order) against the reference, whole factor and solution
+    f_o, tr_o, _, _ = O.lu(a)
+    out["pivots_oracle_equal"] = bool(np.array_equal(tr_o, tr))
+    out["factor_floor"] = rel(f_o, fact)
+    if fz < 0:
+        out["x_floor"] = rel(O.lu_solve(f_o, tr_o, b), x)
+        out["xt_floor"] = rel(O.lu_solve(f_o, tr_o, b, transpose=True), xt)
     return out
 
 
@@ -145,6 +212,12 @@ def llt_case(spec: dict, arrays: dict, name: str) -> dict:
         arrays[name + "fact_idx"] = idx
         arrays[name + "fact_val"] = tri.reshape(-1, order="F")[idx]
         arrays[name + "fact_diag"] = np.diag(fact).copy()
+        arrays[name + "fact_sketch"] = tri.astype(np.float64) @ sketch_matrix(n)
+    f_o, info_o = O.llt(a, upper=upper)
+    tri_o = np.triu(f_o) if upper else np.tril(f_o)
+    out["factor_floor"] = rel(tri_o, tri)
+    if info == 0:
+        out["x_floor"] = rel(O.llt_solve(f_o, b, upper=upper), x)
     return out
 
 
@@ -160,6 +233,9 @@ def cases():
     for n, col in [(5, 2), (40, 0), (100, 57), (300, 299)]:
         yield "lu", dict(gen="zero_col", seed=400 + n, m=n, n=n, col=col)
     yield "lu", dict(gen="ones", seed=0, m=20, n=20)
+    for n, pairs, c0 in [(512, 16, 300), (2048, 32, 1500)]:
+        yield "lu", dict(gen="tie_rows", seed=1100 + n, m=n, n=n, pairs=pairs, c0=c0)
+        yield "lu", dict(gen="near_tie_rows", seed=1200 + n, m=n, n=n, pairs=pairs, c0=c0)
     yield "lu", dict(gen="gauss", seed=8192, m=8192, n=8192, nrhs=2)
     for m, n in [(10, 4), (100, 37), (300, 129), (400, 70)]:
         yield "getrf", dict(gen="gauss", seed=500 + m, m=m, n=n)

@@ -5,14 +5,24 @@ Every call goes through the C ABI (libgb300solve.so).  Checked against
   * the CPU oracle (oracle/, pinned to those fixtures by test_oracle_golden.py).
 
 Parity criteria (pivots are integer work, so bit-exact):
-  * transpositions / permutation identical to the reference's;
-  * LLT factor and LU factors within 1e-12 relative Frobenius of the
-    reference (FP32: 2e-5);
-  * LU solutions: backward error at the FP64 floor (<= 1e-14 here) and
-    forward difference to the reference's solution below 1e-9;
+  * transpositions / permutation identical to the reference's, including
+    exact and 1e-10 pivot ties decided after hundreds of blocked updates;
+  * LLT factor, LLT solution and LU factors within 1e-12 relative Frobenius
+    of the reference at every size (FP32: 2e-5), unscaled.  Above 129 the
+    whole factor is checked three ways: against a sketch F R of the
+    reference's whole factor (R a seeded Gaussian n x 4 or n x 8), against
+    2048 sampled entries and the diagonal, and against the C restatement's
+    whole factor computed here;
+  * the whole-factor difference also stays within 3x the reference's own
+    noise floor (its distance to the C restatement: same blocking, another
+    rounding order), so the different blocking adds nothing beyond rounding;
+  * LU solutions: backward error at the FP64 floor (<= 1e-14) and a forward
+    difference within 10x the noise floor of the reference's solution (the
+    forward difference is bounded by the conditioning, not by 1e-12);
   * rcond equal to the reference's to 1e-6 relative (same algorithm, same
     decisions), and within 10x of the exact value;
   * info() / first failing column / first zero pivot identical.
+The achieved errors are printed in pytest's terminal summary.
 """
 import ctypes as C
 
@@ -22,7 +32,8 @@ import pytest
 import oracle as O
 from eigen_gb300 import LLT, PartialPivLU, getrf, getrs, llt_blocked, partial_lu_blocked, potrf, potrs
 from eigen_gb300 import _lib
-from tests.conftest import Golden, case_id
+from tests.conftest import Golden, case_id, record_parity
+from tests.golden.make_golden import sketch_matrix
 
 pytestmark = pytest.mark.gpu
 G = Golden()
@@ -35,6 +46,33 @@ def rel(a, b):
 
 def ftol(case):
     return 2e-5 if case.get("dtype") == "f32" else 1e-12
+
+
+def check(case, what, value, bound):
+    record_parity(case_id(case), what, value, bound)
+    assert value <= bound, f"{what}: {value:.3e} > {bound:.1e}"
+
+
+def check_factor(case, f, oracle_f, full_key, idx_key, val_key, diag_key, sketch_key):
+    """f against the reference's factor (whole, or sampled + diagonal + sketch)
+    and against the C restatement's whole factor."""
+    tol = ftol(case)
+    f64 = case.get("dtype") != "f32"
+    full = G.arr(case, full_key)
+    if full is not None:
+        check(case, "factor vs reference (whole)", rel(f, full), tol)
+    else:
+        idx = G.arr(case, idx_key)
+        check(case, "factor vs reference (2048 entries)", rel(f.reshape(-1, order="F")[idx], G.arr(case, val_key)),
+              tol)
+        if G.arr(case, diag_key) is not None:
+            check(case, "factor diagonal vs reference", rel(np.diag(f), G.arr(case, diag_key)), tol)
+        sk = G.arr(case, sketch_key)
+        d = rel(f.astype(np.float64) @ sketch_matrix(case["n"]), sk)
+        check(case, "factor vs reference (whole, sketch)", d, tol)
+        if f64:
+            check(case, "factor sketch / reference noise floor", d, max(3 * case["factor_floor"], 1e-15))
+    check(case, "factor vs C restatement (whole)", rel(f, oracle_f), tol)
 
 
 LU = G.cases("lu")
@@ -52,14 +90,9 @@ def test_lu_matches_reference(case):
     assert lu.nb_transpositions() == case["nb_transpositions"]
     assert lu.first_zero_pivot() == case["first_zero_pivot"]
     f = lu.matrixLU()
-    full = G.arr(case, "lu")
-    scale = max(1.0, n / 256)
-    if full is not None:
-        assert rel(f, full) <= ftol(case) * scale
-    else:
-        idx = G.arr(case, "lu_idx")
-        assert rel(f.reshape(-1, order="F")[idx], G.arr(case, "lu_val")) <= ftol(case) * scale
-        assert rel(np.diag(f), G.arr(case, "lu_diag")) <= ftol(case) * scale
+    f_o, tr_o, _, _ = O.lu(a)
+    assert np.array_equal(tr_o, G.arr(case, "tr"))
+    check_factor(case, f, f_o, "lu", "lu_idx", "lu_val", "lu_diag", "lu_sketch")
     assert lu.l1_norm() == pytest.approx(case["l1_norm"], rel=1e-6)
     if case["first_zero_pivot"] >= 0:
         return
@@ -68,14 +101,15 @@ def test_lu_matches_reference(case):
     x = lu.solve(b)
     xt = lu.solve_transposed(b)
     if a.dtype == np.float64:
-        assert O.backward_error(a, x, b) <= 1e-14
-        if n <= 2048:
-            assert O.backward_error(np.asfortranarray(a.T), xt, b) <= 1e-14
-        # forward difference is bounded by the conditioning: the reference
-        # differs from itself (two builds) by 2.4e-10 at n = 8192
-        fwd = 1e-9 if n <= 2048 else 1e-8
-        assert rel(x, G.arr(case, "x")) < fwd
-        assert rel(xt, G.arr(case, "xt")) < fwd
+        check(case, "LU solve backward error", O.backward_error(a, x, b), 1e-14)
+        check(case, "LU transposed solve backward error", O.backward_error(np.asfortranarray(a.T), xt, b), 1e-14)
+        # the forward difference is bounded by the conditioning: measured
+        # against the reference's own spread (its distance to the C
+        # restatement of the same algorithm)
+        check(case, "LU solution forward diff (10x noise floor)", rel(x, G.arr(case, "x")),
+              max(10 * case["x_floor"], 1e-13))
+        check(case, "LU transposed solution forward diff", rel(xt, G.arr(case, "xt")),
+              max(10 * case["xt_floor"], 1e-13))
     else:
         assert rel(x, G.arr(case, "x")) < 1e-3
     if n <= 2048:
@@ -105,16 +139,14 @@ def test_llt_matches_reference(case):
             llt.solve(G.rhs(case, 1))
         return
     tri = np.triu(m) if upper else np.tril(m)
-    full = G.arr(case, "fact")
-    if full is not None:
-        assert rel(tri, full) <= ftol(case)
-    else:
-        idx = G.arr(case, "fact_idx")
-        assert rel(tri.reshape(-1, order="F")[idx], G.arr(case, "fact_val")) <= ftol(case)
+    f_o, info_o = O.llt(a, upper=upper)
+    assert info_o == -1
+    check_factor(case, tri, np.triu(f_o) if upper else np.tril(f_o), "fact", "fact_idx", "fact_val", "fact_diag",
+                 "fact_sketch")
     nrhs = G.arr(case, "x").shape[1]
     b = G.rhs(case, nrhs)
     x = llt.solve(b)
-    assert rel(x, G.arr(case, "x")) <= ftol(case) * 100
+    check(case, "LLT solution vs reference", rel(x, G.arr(case, "x")), ftol(case) if a.dtype == np.float64 else 2e-4)
     assert llt.rcond() == pytest.approx(case["rcond"], rel=1e-6 if a.dtype == np.float64 else 1e-3)
     assert llt.l1_norm() == pytest.approx(case["l1_norm"], rel=1e-6)
 

@@ -9,6 +9,7 @@ import pytest
 
 import oracle as O
 from tests.conftest import Golden, case_id
+from tests.golden.make_golden import sketch_matrix
 
 G = Golden()
 MAX_N_CPU = 2048   # the 8192 case is exercised by the GPU tests
@@ -39,11 +40,18 @@ def test_oracle_lu_matches_reference(case):
     assert (fz + 1 if fz >= 0 else 0) == case["getrf_info"]
     full = G.arr(case, "lu")
     if full is not None:
-        assert rel(f, full) <= tol(case) * max(1, case["n"] / 64)
+        assert rel(f, full) <= tol(case)
     else:
         idx = G.arr(case, "lu_idx")
-        assert rel(f.reshape(-1, order="F")[idx], G.arr(case, "lu_val")) <= tol(case) * 10
-        assert rel(np.diag(f), G.arr(case, "lu_diag")) <= tol(case) * 10
+        assert rel(f.reshape(-1, order="F")[idx], G.arr(case, "lu_val")) <= tol(case)
+        assert rel(np.diag(f), G.arr(case, "lu_diag")) <= tol(case)
+        # whole factor: the sketch F R sees every entry; its distance equals
+        # the recorded noise floor up to the projection's spread
+        d = rel(f.astype(np.float64) @ sketch_matrix(case["n"]), G.arr(case, "lu_sketch"))
+        assert d <= tol(case)
+        assert d <= 3 * case["factor_floor"] + 1e-16
+    if case["gen"] in ("tie_rows", "near_tie_rows"):
+        assert case["tie_decisions"] >= case["pairs"] - 1, "the tie construction no longer creates ties"
     if case["first_zero_pivot"] < 0:
         nrhs = G.arr(case, "x").shape[1]
         b = G.rhs(case, nrhs)
@@ -93,10 +101,13 @@ def test_oracle_llt_matches_reference(case):
     else:
         idx = G.arr(case, "fact_idx")
         assert rel(tri.reshape(-1, order="F")[idx], G.arr(case, "fact_val")) <= tol(case)
+        d = rel(tri.astype(np.float64) @ sketch_matrix(case["n"]), G.arr(case, "fact_sketch"))
+        assert d <= tol(case)
+        assert d <= 3 * case["factor_floor"] + 1e-16
     nrhs = G.arr(case, "x").shape[1]
     b = G.rhs(case, nrhs)
     x = O.llt_solve(f, b, upper=upper)
-    assert rel(x, G.arr(case, "x")) <= tol(case) * 100
+    assert rel(x, G.arr(case, "x")) <= (tol(case) if a.dtype == np.float64 else 2e-4)
     rc = O.llt_rcond(f, O.sym_l1_norm(a, upper), upper=upper)
     assert rc == pytest.approx(case["rcond"], rel=1e-9 if a.dtype == np.float64 else 1e-4)
     assert O.sym_l1_norm(a, upper) == pytest.approx(case["l1_norm"], rel=1e-12)

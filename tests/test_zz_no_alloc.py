@@ -75,23 +75,42 @@ def test_noalloc_matches_existing_entry_point_on_two_calls_in_a_row():
     _same(torch, a1)                        # the scratch's old contents do not leak into a new call
 
 
-def test_noalloc_leaves_device_free_memory_unchanged():
+@pytest.mark.parametrize("m,n", [(12000, 64), (40000, 32)])
+def test_noalloc_tall_panels_match_existing_entry_point(m, n):
+    """Panels taller than one thread-block cluster holds (m > 8192) run on the
+    grid-cooperative panel kernel, whose candidate-exchange buffers and grid
+    barrier counters live in the fixed array; 40000 rows need two rows per
+    thread.  Two calls in a row, each equal to gbs_dgetrf."""
     torch = pytest.importorskip("torch")
-    a = O.gauss(4711, 900, 900)
-    _noalloc_getrf(torch, a)                # first call on this device: set-up
-    d_a = torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
-    d_ipiv = torch.zeros(900, dtype=torch.int32, device="cuda")
-    d_info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    a = O.gauss(52000 + m, m, n)
+    _same(torch, a)
+    _same(torch, a)
+
+
+def test_noalloc_leaves_device_free_memory_unchanged():
+    """After one small call (the per-device set-up), calls of other shapes --
+    a square matrix on the cluster panel and a tall one on the cooperative
+    panel, with other GEMM tile sizes -- leave free device memory unchanged."""
+    torch = pytest.importorskip("torch")
+    _noalloc_getrf(torch, O.gauss(4710, 40, 40))     # first call on this device: set-up
+    L = _lib.lib()
+    shapes = [(900, 900), (20000, 48)]
+    bufs = []
+    for i, (m, n) in enumerate(shapes):
+        a = O.gauss(4711 + i, m, n)
+        bufs.append((m, n, torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t(),
+                     torch.zeros(min(m, n), dtype=torch.int32, device="cuda"),
+                     torch.full((1,), -7, dtype=torch.int32, device="cuda")))
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
-    L = _lib.lib()
     for _ in range(2):
-        _lib.check(L.gbs_dgetrf_noalloc(900, 900, C.c_void_p(d_a.data_ptr()), 900, C.c_void_p(d_ipiv.data_ptr()),
-                                        C.c_void_p(d_info.data_ptr()),
-                                        C.c_void_p(torch.cuda.current_stream().cuda_stream)), "noalloc")
+        for m, n, d_a, d_ipiv, d_info in bufs:
+            _lib.check(L.gbs_dgetrf_noalloc(m, n, C.c_void_p(d_a.data_ptr()), m, C.c_void_p(d_ipiv.data_ptr()),
+                                            C.c_void_p(d_info.data_ptr()),
+                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)), "noalloc")
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free0
-    assert int(d_info.item()) == 0
+    assert all(int(b[4].item()) == 0 for b in bufs)
 
 
 def test_noalloc_refuses_sizes_beyond_its_scratch():
