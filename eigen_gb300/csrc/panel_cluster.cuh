@@ -1,19 +1,45 @@
 // Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
 //
 // Same arithmetic and pivot rule as panel_lu_kernel (unblocked_lu,
-// PartialPivLU.h:365-409; first maximum wins, Visitor.h:173-186), but the
-// per-column exchange goes through distributed shared memory and the
-// cluster's hardware barrier instead of global scratch and a grid barrier:
-//   1. each CTA reduces its rows to one candidate (value, row);
-//   2. it pushes the candidate and the candidate's row (CTA 0 also row j) into
-//      every CTA's shared memory (double-buffered by column parity), then one
-//      cluster barrier;
-//   3. every CTA picks the same winner from its local copies: no remote reads
-//      on the critical path.
-// One barrier per column is enough: a slot is rewritten two columns later,
-// after its reader has passed the barrier that follows its reads.
+// PartialPivLU.h:365-409; first maximum wins, Visitor.h:173-186), with the
+// per-column exchange through distributed shared memory and the cluster's
+// hardware barrier instead of global scratch and a grid barrier.
+//
+// Layout.  Each thread holds RPT rows of the panel in registers.  At step j a
+// row's registers hold its columns j .. NB-1 in slots 0 .. NB-1-j: after the
+// rank-1 update of step j every row shifts left by one slot, so the current
+// column is always slot 0 and the column loop runs as a plain loop (a small
+// body that stays in the instruction cache) instead of NB unrolled copies.
+//
+// Rows never move.  Each thread-row carries its current position; the
+// interchange of step j swaps the positions of the pivot row and the row at
+// position j, so the pivot search sees exactly the reference's row order (the
+// first maximum is the lowest position) without copying a row between CTAs.
+// Finished entries (the row's L part, and its U part once it is a pivot row)
+// collect in shared memory and are written once, at the row's final position.
+//
+// Pivot search on integer keys: an entry x maps to bits(|x|) + 1, which orders
+// like |x|, and a NaN to 0 (a NaN is never the first maximum unless it is the
+// column's first entry, which maps to the key of +inf, the largest).  The
+// largest key, then the lowest position, wins -- the reference's strict '>'
+// scan -- in two or three redux.sync instructions per warp.
+//
+// Per column j:
+//   1. every CTA picks the same winner from its local copies of the cluster's
+//      candidates (no remote reads on the critical path), scales its rows and
+//      updates column j+1 only;
+//   2. each CTA reduces its rows to one candidate for column j+1; the owning
+//      thread finishes its row's update, and its warp stores row and key into
+//      every CTA (one destination CTA per lane, 16-byte stores);
+//   3. cluster barrier: the warps that stored remotely arrive with release,
+//      the rest relaxed; between arrive and wait every thread applies the
+//      rank-1 update to its rows' other columns, off the critical path.
+// The candidate slots are triple-buffered by column: a slot is rewritten for
+// column j+3, whose writers have passed the barrier of column j+2, which every
+// CTA reaches only after its update of column j -- the last read of the slot.
 // Cluster barriers are hardware barriers over co-scheduled CTAs: no spin loop,
-// nothing that can wait forever.
+// nothing that can wait forever.  The status word (swap count, first zero
+// pivot) is read once and written once per launch.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -25,19 +51,134 @@ namespace gbs {
 constexpr int kClusterPanelThreads = 512;
 constexpr int kMaxPanelCluster = 16;
 
+template <typename T> struct PivotKey;
+template <> struct PivotKey<float> { typedef unsigned int type; };
+template <> struct PivotKey<double> { typedef unsigned long long type; };
+
+// Integer pivot key of entry x; first: x is the column's first entry (position j).
+template <typename T>
+__device__ __forceinline__ typename PivotKey<T>::type pivot_key(T x, bool first)
+{
+  typedef typename PivotKey<T>::type K;
+  if (sizeof(T) == 4) {
+    if (x != x) return first ? (K)0x7F800001u : (K)0;
+    return (K)__float_as_uint(fabsf((float)x)) + (K)1;
+  }
+  if (x != x) return first ? (K)0x7FF0000000000001ull : (K)0;
+  return (K)__double_as_longlong(fabs((double)x)) + (K)1;
+}
+
+// Warp-wide (largest key, lowest position); every lane gets the result.
+__device__ __forceinline__ void warp_keymax(unsigned int& k, int& i)
+{
+  const unsigned int km = __reduce_max_sync(0xffffffffu, k);
+  i = (int)__reduce_min_sync(0xffffffffu, k == km ? (unsigned int)i : 0x7fffffffu);
+  k = km;
+}
+__device__ __forceinline__ void warp_keymax(unsigned long long& k, int& i)
+{
+  const unsigned int hi = (unsigned int)(k >> 32), lo = (unsigned int)k;
+  const unsigned int hm = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned int lm = __reduce_max_sync(0xffffffffu, hi == hm ? lo : 0u);
+  const bool top = hi == hm && lo == lm;
+  i = (int)__reduce_min_sync(0xffffffffu, top ? (unsigned int)i : 0x7fffffffu);
+  k = ((unsigned long long)hm << 32) | lm;
+}
+
+__device__ __forceinline__ void cluster_arrive(bool release)
+{
+  if (release) asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  else asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
 template <typename T, int NB>
 struct ClusterPanelShared {
-  T crows[2][kMaxPanelCluster][NB];   // every CTA's candidate row, pushed by its owner
-  T cval[2][kMaxPanelCluster];
-  int cidx[2][kMaxPanelCluster];
-  T rowj[2][NB];                      // row j of the panel, pushed by CTA 0
-  T mine[NB], minej[NB];              // this CTA's candidate row and row j, staged for the push
-  T wval[kClusterPanelThreads / 32];
+  typedef typename PivotKey<T>::type K;
+  __align__(16) T crows[3][kMaxPanelCluster][NB];   // every CTA's candidate row (slot s = column j + s)
+  K ckey[3][kMaxPanelCluster];
+  int cidx[3][kMaxPanelCluster];
+  __align__(16) T outrow[NB];                       // this CTA's candidate row, staged for the stores
+  K wkey[kClusterPanelThreads / 32];
   int widx[kClusterPanelThreads / 32];
-  int spiv[NB];                       // the panel's pivots (rows relative to the panel)
+  int spiv[NB];                       // the panel's pivots (positions relative to the panel)
   int tgt[2 * NB], src[2 * NB];       // the interchanges as (target row, source row), relative
   T l11[NB][NB + 1];                  // unit-lower L11 of the panel (CTA 0, for the fused TRSM)
 };
+
+// Dynamic shared memory of one CTA: the finished entries of its rows,
+// fin[c * (threads * RPT) + slot] for column c.
+template <typename T, int NB, int RPT>
+constexpr size_t cluster_panel_dyn_smem()
+{
+  return sizeof(T) * (size_t)NB * kClusterPanelThreads * RPT;
+}
+
+// This CTA's candidate (largest key, lowest position) from each thread's
+// best (bk, bi); every lane of every warp gets it.
+template <typename T, int NB>
+__device__ __forceinline__ void cluster_panel_cta_candidate(ClusterPanelShared<T, NB>& sh,
+                                                            typename PivotKey<T>::type bk, int bi,
+                                                            typename PivotKey<T>::type& ck, int& ci)
+{
+  typedef typename PivotKey<T>::type K;
+  constexpr int NW = kClusterPanelThreads / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  warp_keymax(bk, bi);
+  if (lane == 0) { sh.wkey[warp] = bk; sh.widx[warp] = bi; }
+  __syncthreads();
+  ck = lane < NW ? sh.wkey[lane] : (K)0;
+  ci = lane < NW ? sh.widx[lane] : 0x7fffffff;
+  warp_keymax(ck, ci);
+}
+
+// The owner warp (its row staged in sh.outrow) stores row, key and position
+// into slot sl of every CTA; a CTA without a candidate stores an empty one
+// from warp 0.  Returns whether this warp stored into other CTAs.
+template <typename T, int NB>
+__device__ __forceinline__ bool cluster_panel_push(ClusterPanelShared<T, NB>& sh, int sl,
+                                                   typename PivotKey<T>::type ck, int ci, bool owner_warp, int C,
+                                                   int rank)
+{
+  namespace cg = cooperative_groups;
+  typedef typename PivotKey<T>::type K;
+  cg::cluster_group cluster = cg::this_cluster();
+  constexpr int CH = NB * (int)sizeof(T) / 16;         // 16-byte chunks of a row
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (ci != 0x7fffffff) {
+    if (!owner_warp) return false;
+    // (destination, chunk) pairs dealt over the lanes: lane l serves CTA
+    // l % C with chunks l / C, l / C + 32 / C, ...
+    const int d = lane % C;
+    ClusterPanelShared<T, NB>* rs = cluster.map_shared_rank(&sh, d);
+    for (int ch = lane / C; ch < CH; ch += 32 / C)
+      reinterpret_cast<float4*>(rs->crows[sl][rank])[ch] = reinterpret_cast<const float4*>(sh.outrow)[ch];
+    if (lane < C) {
+      rs->ckey[sl][rank] = ck;
+      rs->cidx[sl][rank] = ci;
+    }
+    return true;
+  }
+  if (warp != 0) return false;
+  if (lane < C) {
+    ClusterPanelShared<T, NB>* rs = cluster.map_shared_rank(&sh, lane);
+    rs->ckey[sl][rank] = (K)0;
+    rs->cidx[sl][rank] = 0x7fffffff;
+  }
+  return true;
+}
+
+// Rank-1 update of a row's columns j+2.. and the shift by one slot; slot 1
+// (column j+1) was updated already.
+template <typename T, int NB>
+__device__ __forceinline__ void cluster_panel_shift_update(T (&v)[NB], T l, const T* u)
+{
+  v[0] = v[1];
+#pragma unroll
+  for (int c = 1; c < NB - 1; ++c) v[c] = fma(-l, u[c + 1], v[c + 1]);
+  v[NB - 1] = T(0);
+}
 
 // a: the panel (m rows, nbc <= NB columns) at row and column k0 of its
 // matrix.  map (may be null): the panel's interchanges as a row map (count,
@@ -45,132 +186,162 @@ struct ClusterPanelShared {
 // trsm_cols > 0 (needs nbc == NB): CTA 0 also applies the interchanges to the
 // trsm_cols columns right of the panel and replaces their top NB rows by
 // L11^-1 times them (the U12 block row); the caller leaves those columns out
-// of the gather.
+// of the gather.  Dynamic shared memory: cluster_panel_dyn_smem<T, NB, RPT>().
 template <typename T, int NB, int RPT>
 __global__ void __launch_bounds__(kClusterPanelThreads)
 panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, int* __restrict__ tr,
                         DeviceStatus* st, int* __restrict__ map, int trsm_cols)
 {
+  static_assert(NB == 32, "one lane per panel column");
+  typedef typename PivotKey<T>::type K;
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   __shared__ ClusterPanelShared<T, NB> sh;
+  extern __shared__ __align__(16) unsigned char cluster_panel_dyn[];
+  T* fin = reinterpret_cast<T*>(cluster_panel_dyn);
+  constexpr int S = kClusterPanelThreads * RPT;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = rank * kClusterPanelThreads + tid;
   const int G = C * kClusterPanelThreads;
+  const bool keeper = rank == 0 && tid == 0;        // keeps the status counters of this launch
+  int swaps = 0, first_zero = -1;
 
   T v[RPT][NB];
+  int pos[RPT];
 #pragma unroll
   for (int q = 0; q < RPT; ++q) {
     const int r = g + q * G;
+    pos[q] = r;
 #pragma unroll
     for (int c = 0; c < NB; ++c) v[q][c] = (r < m && c < nbc) ? a[(int64_t)c * lda + r] : T(0);
   }
 
-#pragma unroll
-  for (int j = 0; j < NB; ++j) {
-    if (j >= nbc) break;
-    const int par = j & 1;
-    // 1. this CTA's candidate: first max of |a(r, j)|, r >= j
-    T bs = T(-2);
+  // the candidates of column 0, as loaded
+  {
+    K bk = 0;
     int bi = 0x7fffffff;
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int r = g + q * G;
-      if (r < m && r >= j) {
-        const T x = v[q][j];
-        const T sc = (r == j) ? ((x != x) ? T(INFINITY) : gbs_abs(x)) : pivot_score(x);
-        if (better(sc, r, bs, bi)) { bs = sc; bi = r; }
+    for (int q = 0; q < RPT; ++q)
+      if (pos[q] < m) {
+        const K key = pivot_key<T>(v[q][0], pos[q] == 0);
+        if (key > bk || (key == bk && pos[q] < bi)) { bk = key; bi = pos[q]; }
       }
-    }
-    warp_argmax(bs, bi);
-    if (lane == 0) { sh.wval[warp] = bs; sh.widx[warp] = bi; }
-    __syncthreads();
-    bs = lane < kClusterPanelThreads / 32 ? sh.wval[lane] : T(-2);     // every warp reduces the same values
-    bi = lane < kClusterPanelThreads / 32 ? sh.widx[lane] : 0x7fffffff;
-    warp_argmax(bs, bi);
-    bs = __shfl_sync(0xffffffffu, bs, 0);
-    bi = __shfl_sync(0xffffffffu, bi, 0);
+    K ck;
+    int ci;
+    cluster_panel_cta_candidate<T, NB>(sh, bk, bi, ck, ci);
+    const bool ow = ci != 0x7fffffff && sh.widx[warp] == ci;
+    if (ow) {
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int r = g + q * G;
-      if (r < m && r == bi) {
+      for (int q = 0; q < RPT; ++q)
+        if (pos[q] == ci) {
 #pragma unroll
-        for (int c = 0; c < NB; ++c) sh.mine[c] = v[q][c];
-      }
-      if (r < m && r == j) {
-#pragma unroll
-        for (int c = 0; c < NB; ++c) sh.minej[c] = v[q][c];
-      }
-    }
-    __syncthreads();
-    // 2. push the candidate (and, from CTA 0, row j) into every CTA's shared memory
-    for (int e = tid; e < C * NB; e += kClusterPanelThreads) {
-      const int d = e / NB, c = e % NB;
-      ClusterPanelShared<T, NB>* rs = cluster.map_shared_rank(&sh, d);
-      rs->crows[par][rank][c] = sh.mine[c];
-      if (rank == 0) rs->rowj[par][c] = sh.minej[c];
-      if (c == 0) {
-        rs->cval[par][rank] = bs;
-        rs->cidx[par][rank] = bi;
-      }
-    }
-    cluster.sync();
-    // 3. every warp picks the same winner from the local copies
-    T s = lane < C ? sh.cval[par][lane] : T(-2);
-    int i = lane < C ? sh.cidx[par][lane] : 0x7fffffff;
-    int cw = lane;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const T so = __shfl_xor_sync(0xffffffffu, s, off);
-      const int io = __shfl_xor_sync(0xffffffffu, i, off);
-      const int co = __shfl_xor_sync(0xffffffffu, cw, off);
-      if (better(so, io, s, i)) { s = so; i = io; cw = co; }
-    }
-    const int p = __shfl_sync(0xffffffffu, i, 0);
-    const int wr = __shfl_sync(0xffffffffu, cw, 0);
-    const T* u = sh.crows[par][wr];
-    const T* oldj = sh.rowj[par];
-    const T piv = u[j];
-    const bool nz = (piv != T(0));   // biggest_in_corner != 0 (NaN counts as nonzero)
-    if (tid == 0) sh.spiv[j] = p;
-    if (rank == 0 && tid == 0) {
-      tr[j] = k0 + p;
-      if (nz && p != j) st->nb_transpositions += 1;
-      if (!nz && st->info < 0) st->info = k0 + j;
-    }
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int r = g + q * G;
-      if (r >= m) continue;
-      if (nz && p != j) {
-        if (r == j) {
-#pragma unroll
-          for (int c = 0; c < NB; ++c) v[q][c] = u[c];
-        } else if (r == p) {
-#pragma unroll
-          for (int c = 0; c < NB; ++c) v[q][c] = oldj[c];
+          for (int c = 0; c < NB; ++c) sh.outrow[c] = v[q][c];
         }
-      }
-      if (r > j) {
-        if (nz) v[q][j] = v[q][j] / piv;
-        const T l = v[q][j];
-#pragma unroll
-        for (int c = j + 1; c < NB; ++c) v[q][c] = fma(-l, u[c], v[q][c]);
-      }
+      __syncwarp();
     }
+    cluster_arrive(cluster_panel_push<T, NB>(sh, 0, ck, ci, ow, C, rank));
+    cluster_wait();
   }
 
+  int sl = 0;
+#pragma unroll 1
+  for (int j = 0; j < nbc; ++j) {
+    // 1. every warp picks the same winner from the local copies
+    K wk = lane < C ? sh.ckey[sl][lane] : (K)0;
+    int wi = lane < C ? sh.cidx[sl][lane] : 0x7fffffff;
+    warp_keymax(wk, wi);
+    const int p = wi;
+    const int cw = __ffs(__ballot_sync(0xffffffffu, lane < C && sh.cidx[sl][lane] == p)) - 1;
+    const T* u = sh.crows[sl][cw];
+    const T piv = u[0];
+    const bool nz = (piv != T(0));   // biggest_in_corner != 0 (NaN counts as nonzero)
+    if (tid == 0) sh.spiv[j] = p;
+    if (keeper) {
+      tr[j] = k0 + p;
+      if (nz && p != j) ++swaps;
+      if (!nz && first_zero < 0) first_zero = k0 + j;
+    }
+    T l[RPT];
+    bool live[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int r = pos[q];
+      const int slot = tid + q * kClusterPanelThreads;
+      if (r == p) {
+        // the pivot row: its values are row j of U (the row it stored)
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+          if (j + c < nbc) fin[(j + c) * S + slot] = v[q][c];
+        pos[q] = j;
+      } else if (r == j && nz) {
+        pos[q] = p;                  // the row at position j takes the pivot row's place
+      }
+      live[q] = pos[q] < m && pos[q] > j;
+      l[q] = T(0);
+      if (live[q]) {
+        T lq = v[q][0];
+        if (nz) lq = lq / piv;
+        l[q] = lq;
+        fin[j * S + slot] = lq;
+        v[q][1] = fma(-lq, u[1], v[q][1]);
+      }
+    }
+    if (j + 1 == nbc) break;
+    const int sn = sl == 2 ? 0 : sl + 1;
+    // 2. the candidates of column j+1
+    K bk = 0;
+    int bi = 0x7fffffff;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      if (live[q]) {
+        const K key = pivot_key<T>(v[q][1], pos[q] == j + 1);
+        if (key > bk || (key == bk && pos[q] < bi)) { bk = key; bi = pos[q]; }
+      }
+    K ck;
+    int ci;
+    cluster_panel_cta_candidate<T, NB>(sh, bk, bi, ck, ci);
+    const bool ow = ci != 0x7fffffff && sh.widx[warp] == ci;
+    bool done[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) done[q] = false;
+    if (ow) {
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+        if (pos[q] == ci) {
+          cluster_panel_shift_update<T, NB>(v[q], l[q], u);
+#pragma unroll
+          for (int c = 0; c < NB; ++c) sh.outrow[c] = v[q][c];
+          done[q] = true;
+        }
+      __syncwarp();
+    }
+    cluster_arrive(cluster_panel_push<T, NB>(sh, sn, ck, ci, ow, C, rank));
+    // 3. the rank-1 update of the other columns while the barrier completes
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      if (live[q] && !done[q]) cluster_panel_shift_update<T, NB>(v[q], l[q], u);
+    cluster_wait();
+    sl = sn;
+  }
+  if (keeper) {
+    if (swaps) st->nb_transpositions += swaps;
+    if (first_zero >= 0 && st->info < 0) st->info = first_zero;
+  }
+
+  __syncthreads();
 #pragma unroll
   for (int q = 0; q < RPT; ++q) {
-    const int r = g + q * G;
+    const int r = pos[q];
     if (r < m) {
-#pragma unroll
-      for (int c = 0; c < NB; ++c)
-        if (c < nbc) a[(int64_t)c * lda + r] = v[q][c];
+      const int slot = tid + q * kClusterPanelThreads;
+      for (int c = 0; c < nbc; ++c) a[(int64_t)c * lda + r] = fin[c * S + slot];
     }
   }
+  // the fused TRSM below reads L11, whose rows other CTAs may have written;
+  // without it, no CTA touches another's shared memory after the last barrier
+  if (trsm_cols > 0) cluster.sync();
 
   // the panel's interchanges as (target, source) rows: targets are the
   // panel's rows and the pivot rows below them; the source of a target runs
@@ -183,24 +354,24 @@ panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, 
       if (tid < nbc) row = tid;
       else if (tid >= NB && tid - NB < nbc && sh.spiv[tid - NB] >= nbc) row = sh.spiv[tid - NB];
       if (row < 0) row = 0;
-      int pos = row;
+      int p = row;
       for (int jj = nbc - 1; jj >= 0; --jj) {
         const int pj = sh.spiv[jj];
-        if (pos == jj) pos = pj;
-        else if (pos == pj) pos = jj;
+        if (p == jj) p = pj;
+        else if (p == pj) p = jj;
       }
       sh.tgt[tid] = row;
-      sh.src[tid] = pos;
+      sh.src[tid] = p;
       if (map) {
         map[1 + tid] = k0 + row;
-        map[257 + tid] = k0 + pos;
+        map[257 + tid] = k0 + p;
         if (tid == 0) map[0] = 2 * NB;
       }
     }
     if (trsm_cols > 0) {
-      if (tid < NB) {                          // L11 from the rows this CTA holds (rows 0..NB-1, slot 0)
-#pragma unroll
-        for (int c = 0; c < NB; ++c) sh.l11[tid][c] = v[0][c];
+      for (int e = tid; e < NB * NB; e += kClusterPanelThreads) {
+        const int r = e % NB, c = e / NB;
+        sh.l11[r][c] = (r > c && r < m) ? a[(int64_t)c * lda + r] : T(0);
       }
       __syncthreads();
       // interchanges on the trsm_cols columns, one warp per column
@@ -238,7 +409,6 @@ panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, 
       }
     }
   }
-  cluster.sync();      // no CTA leaves while another may still read its shared memory
 }
 
 }  // namespace gbs

@@ -44,6 +44,11 @@ static int cluster_panel_limit()
     int lim = 0;
     const void* k = (const void*)panel_lu_cluster_kernel<T, kPanelNB, RPT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) cudaGetLastError();
+    const int dyn = (int)cluster_panel_dyn_smem<T, kPanelNB, RPT>();
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;                                // no cluster panel: the cooperative kernel takes every panel
+    }
     for (int c = kMaxPanelCluster; c >= 1 && lim == 0; c /= 2) {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
@@ -53,6 +58,7 @@ static int cluster_panel_limit()
       at[0].val.clusterDim.z = 1;
       cfg.gridDim = dim3(c);
       cfg.blockDim = dim3(kClusterPanelThreads);
+      cfg.dynamicSmemBytes = dyn;
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int nclusters = 0;
@@ -77,6 +83,7 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
   at[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(kClusterPanelThreads);
+  cfg.dynamicSmemBytes = cluster_panel_dyn_smem<T, kPanelNB, RPT>();
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;

@@ -501,7 +501,8 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   p.err = &st->timeout;
   const int tiles = p.tiles_m * p.tiles_n;
   const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
-  const double flops = 2.0 * M * (double)N * K * (kind == TC_TF32X3 ? 3 : 1) * (lower ? 0.5 : 1.0);
+  // algorithmic flops of the update (a 3xTF32 update issues three such products on the tensor cores)
+  const double flops = 2.0 * M * (double)N * K * (lower ? 0.5 : 1.0);
   const double bytes = 8.0 * M * (double)N * (lower ? 0.5 : 1.0) + (double)(M + N) * Kp * esize;
   PhaseScope ps(s, PH_TC_GEMM, flops, bytes);
   tc_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
