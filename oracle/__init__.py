@@ -58,6 +58,10 @@ def port() -> C.CDLL:
             f.argtypes = [_L, p, _L, C.c_int]
             f = getattr(lib, f"oracle_perm_from_transpositions_{sfx}"); f.restype = None
             f.argtypes = [_L, _ip, _ip]
+            f = getattr(lib, f"oracle_ldlt_{sfx}"); f.restype = C.c_int
+            f.argtypes = [_L, p, _L, _ip, C.POINTER(C.c_int)]
+            f = getattr(lib, f"oracle_ldlt_solve_{sfx}"); f.restype = None
+            f.argtypes = [_L, p, _L, _ip, _L, p, _L]
             vp = C.c_void_p
             f = getattr(lib, f"oracle_batched_llt_solve_{sfx}"); f.restype = None
             f.argtypes = [_L, _ip, _lp, vp, _lp, vp, _ip]
@@ -94,6 +98,8 @@ def ref() -> C.CDLL:
             f.argtypes = [_L, p, _L, _L, p, _L, p, _ip, p, p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
             f = getattr(lib, f"ref_lu_blocked_{sfx}"); f.restype = _L
             f.argtypes = [_L, _L, p, _L, _ip, C.POINTER(C.c_int)]
+            f = getattr(lib, f"ref_ldlt_{sfx}"); f.restype = C.c_int
+            f.argtypes = [_L, p, _L, C.c_int, _L, p, _L, p, _ip, p, C.POINTER(C.c_double), _ip]
         lib.ref_llt_blocked_d.restype = _L
         lib.ref_llt_blocked_d.argtypes = [_L, _dp, _L]
         ip = C.POINTER(C.c_int)
@@ -209,6 +215,42 @@ def llt_rcond(fact: np.ndarray, a_norm: float, upper: bool = False) -> float:
     return getattr(port(), f"oracle_rcond_{_sfx(fact)}")(2 if upper else 1, n, fact, max(n, 1), dummy, a_norm)
 
 
+SIGN_NAMES = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")   # LDLT.h:22
+
+
+def ldlt(a: np.ndarray, upper: bool = False):
+    """LDLT of the lower (upper) triangle: (matrixLDLT, transpositions, ok, sign).
+    Upper runs the lower algorithm on the transpose, as the reference does
+    (LDLT.h:453-461); the other triangle keeps the input."""
+    f = np.array(a, order="F", copy=True)
+    n = f.shape[0]
+    w = np.asfortranarray(f.T) if upper else f
+    tr = np.zeros(max(n, 1), dtype=np.int32)
+    sign = C.c_int(2)
+    ok = getattr(port(), f"oracle_ldlt_{_sfx(f)}")(n, w, max(n, 1), tr, C.byref(sign))
+    if upper:
+        f = np.asfortranarray(w.T)
+    return f, tr[:n], bool(ok), int(sign.value)
+
+
+def ldlt_solve(fact: np.ndarray, tr: np.ndarray, b: np.ndarray, upper: bool = False) -> np.ndarray:
+    x = np.array(b, order="F", copy=True, dtype=fact.dtype)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1, order="F")
+    n = fact.shape[0]
+    w = np.asfortranarray(fact.T) if upper else fact
+    getattr(port(), f"oracle_ldlt_solve_{_sfx(fact)}")(n, w, max(n, 1), np.ascontiguousarray(tr, dtype=np.int32),
+                                                       x.shape[1], x, max(n, 1))
+    return x.reshape(b.shape, order="F") if b.ndim == 1 else x
+
+
+def ldlt_rcond(fact: np.ndarray, tr: np.ndarray, a_norm: float, upper: bool = False) -> float:
+    n = fact.shape[0]
+    w = np.asfortranarray(fact.T) if upper else fact
+    return getattr(port(), f"oracle_rcond_{_sfx(fact)}")(3, n, w, max(n, 1), np.ascontiguousarray(tr, dtype=np.int32),
+                                                          a_norm)
+
+
 def backward_error(a: np.ndarray, x: np.ndarray, b: np.ndarray) -> float:
     """max over columns of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf),
     residual accumulated in extended precision."""
@@ -267,6 +309,25 @@ def ref_lu_blocked(a: np.ndarray):
     nbt = C.c_int(0)
     ret = getattr(ref(), f"ref_lu_blocked_{_sfx(f)}")(m, n, f, max(m, 1), tr, C.byref(nbt))
     return f, tr[: min(m, n)], int(nbt.value), int(ret)
+
+
+def ref_ldlt(a: np.ndarray, b: np.ndarray | None = None, upper: bool = False):
+    """Eigen LDLT<Matrix, Lower|Upper>: (matrixLDLT, transpositionsP().indices(),
+    info (0 Success / 1 NumericalIssue), isPositive, isNegative, x, rcond)."""
+    lib = ref()
+    a = np.asfortranarray(a)
+    n = a.shape[0]
+    fact = np.zeros((n, n), dtype=a.dtype, order="F")
+    tr = np.zeros(max(n, 1), dtype=np.int32)
+    nrhs = 0 if b is None else (1 if b.ndim == 1 else b.shape[1])
+    bb = np.zeros((n, max(nrhs, 1)), dtype=a.dtype, order="F") if b is None else \
+        np.asfortranarray(b.reshape(n, -1), dtype=a.dtype)
+    x = np.zeros((n, max(nrhs, 1)), dtype=a.dtype, order="F")
+    rc = C.c_double(np.nan)
+    flags = np.zeros(2, dtype=np.int32)
+    info = getattr(lib, f"ref_ldlt_{_sfx(a)}")(n, a, max(n, 1), int(upper), nrhs, bb, max(n, 1), fact, tr, x,
+                                               C.byref(rc), flags)
+    return fact, tr[:n], int(info), bool(flags[0]), bool(flags[1]), x[:, :nrhs], rc.value
 
 
 def ref_llt_blocked(a: np.ndarray):

@@ -11,6 +11,7 @@
  * exact power-of-two scaling only (no libm), so x86 and Arm hosts produce
  * identical bytes.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>

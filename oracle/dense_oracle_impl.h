@@ -393,13 +393,18 @@ void SFX(oracle_lu_solve_transposed)(long n, const T *lu, long ld, const int *tr
 
 /* ---------------------------------------------------------------- rcond
  * ConditionEstimator.h:56-142 (Hager / Higham 1-norm estimate of inv(A)) and
- * :157-169 (rcond_estimate_helper).  kind 0 = LU (a holds LU, tr the
+ * :157-169 (rcond_estimate_helper).  kind 3 = LDLT (a holds L and D, tr the
+ * transpositions; the solve is self-adjoint).  kind 0 = LU (a holds LU, tr the
  * transpositions), kind 1 = LLT lower, kind 2 = LLT upper. */
+void SFX(oracle_ldlt_solve)(long n, const T *a, long lda, const int *tr, long nrhs, T *b, long ldb);
+
 static void SFX(dec_solve)(int kind, long n, const T *a, long lda, const int *tr, T *v, int adjoint)
 {
   if (kind == 0) {
     if (adjoint) SFX(oracle_lu_solve_transposed)(n, a, lda, tr, 1, v, n);
     else         SFX(oracle_lu_solve)(n, a, lda, tr, 1, v, n);
+  } else if (kind == 3) {
+    SFX(oracle_ldlt_solve)(n, a, lda, tr, 1, v, n);   /* self-adjoint */
   } else {
     SFX(oracle_llt_solve)(n, a, lda, kind == 2, 1, v, n);
   }
@@ -464,6 +469,116 @@ double SFX(oracle_rcond)(int kind, long n, const T *a, long lda, const int *tr, 
   if (n == 1) return 1.0;
   T inv = (T)SFX(oracle_inv_l1_estimate)(kind, n, a, lda, tr);
   return inv == (T)0 ? 0.0 : (double)(((T)1 / inv) / (T)matrix_norm);
+}
+
+/* ---------------------------------------------------------------- LDLT
+ * Eigen/src/Cholesky/LDLT.h:291-383, ldlt_inplace<Lower>::unblocked, on the
+ * lower triangle.  Step k: the first maximum of |a_ii| over i = k..n-1 (the
+ * diagonal beyond k is not updated yet, so the pivots follow the input's
+ * diagonal; Visitor.h:173-186), the symmetric interchange written on the lower
+ * triangle (:318-331), then the left-looking column (:339-344)
+ *   t = D(0:k) A10^T,  a_kk -= A10 t,  A21 -= A20 t,
+ * and A21 /= a_kk when |a_kk| > 0 (:354-357).  A zero (or NaN) pivot leaves
+ * its column unscaled; the result is NumericalIssue when such a column is not
+ * zero below the diagonal or a nonzero pivot follows a zero one (:356-360).
+ * A zero first pivot (the whole diagonal zero) ends the factorization with
+ * identity transpositions (:345-353).  sign uses the reference's SignMatrix
+ * order: 0 PositiveSemiDef, 1 NegativeSemiDef, 2 ZeroSign, 3 Indefinite
+ * (:362-369).  Returns 1 (Success) or 0 (NumericalIssue). */
+int SFX(oracle_ldlt)(long n, T *a, long lda, int *tr, int *sign)
+{
+  *sign = 2;
+  if (n <= 1) {
+    if (n == 1) {
+      tr[0] = 0;
+      const T d = AT(a, lda, 0, 0);
+      *sign = d > (T)0 ? 0 : d < (T)0 ? 1 : 2;
+    }
+    return 1;
+  }
+  T *temp = (T *)malloc(sizeof(T) * (size_t)n);
+  int found_zero = 0, ret = 1;
+  for (long k = 0; k < n; ++k) {
+    long p = k;
+    T best = SFX(absv)(AT(a, lda, k, k));
+    for (long i = k + 1; i < n; ++i) {
+      const T v = SFX(absv)(AT(a, lda, i, i));
+      if (v > best) { best = v; p = i; }
+    }
+    tr[k] = (int)p;
+    if (p != k) {
+      const long s = n - p - 1;
+      for (long j = 0; j < k; ++j) { T t = AT(a, lda, k, j); AT(a, lda, k, j) = AT(a, lda, p, j); AT(a, lda, p, j) = t; }
+      for (long i = 0; i < s; ++i) {
+        T t = AT(a, lda, p + 1 + i, k); AT(a, lda, p + 1 + i, k) = AT(a, lda, p + 1 + i, p); AT(a, lda, p + 1 + i, p) = t;
+      }
+      { T t = AT(a, lda, k, k); AT(a, lda, k, k) = AT(a, lda, p, p); AT(a, lda, p, p) = t; }
+      for (long i = k + 1; i < p; ++i) { T t = AT(a, lda, i, k); AT(a, lda, i, k) = AT(a, lda, p, i); AT(a, lda, p, i) = t; }
+    }
+    const long rs = n - k - 1;
+    if (k > 0) {
+      for (long j = 0; j < k; ++j) temp[j] = AT(a, lda, j, j) * AT(a, lda, k, j);
+      T dot = 0;
+      for (long j = 0; j < k; ++j) dot += AT(a, lda, k, j) * temp[j];
+      AT(a, lda, k, k) -= dot;
+      for (long i = k + 1; i < n; ++i) {
+        T acc = AT(a, lda, i, k);
+        for (long j = 0; j < k; ++j) acc -= AT(a, lda, i, j) * temp[j];
+        AT(a, lda, i, k) = acc;
+      }
+    }
+    const T akk = AT(a, lda, k, k);
+    const int valid = SFX(absv)(akk) > (T)0;
+    if (k == 0 && !valid) {
+      *sign = 2;
+      for (long j = 0; j < n; ++j) {
+        tr[j] = (int)j;
+        for (long i = j + 1; i < n; ++i)
+          if (!(AT(a, lda, i, j) == (T)0)) ret = 0;
+      }
+      free(temp);
+      return ret;
+    }
+    if (rs > 0 && valid) {
+      for (long i = k + 1; i < n; ++i) AT(a, lda, i, k) /= akk;
+    } else if (rs > 0) {
+      for (long i = k + 1; i < n; ++i)
+        if (!(AT(a, lda, i, k) == (T)0)) ret = 0;
+    }
+    if (found_zero && valid) ret = 0;
+    else if (!valid) found_zero = 1;
+    if (*sign == 0) { if (akk < (T)0) *sign = 3; }
+    else if (*sign == 1) { if (akk > (T)0) *sign = 3; }
+    else if (*sign == 2) { if (akk > (T)0) *sign = 0; else if (akk < (T)0) *sign = 1; }
+  }
+  free(temp);
+  return ret;
+}
+
+/* LDLT.h:540-577 (_solve_impl): b <- P b, L^-1, the pseudo-inverse of D
+ * (entries with |d| <= 1/highest give zero), L^-T, P^T. */
+void SFX(oracle_ldlt_solve)(long n, const T *a, long lda, const int *tr, long nrhs, T *b, long ldb)
+{
+  const T tol = (T)1 / (sizeof(T) == 8 ? (T)DBL_MAX : (T)FLT_MAX);
+  for (long c = 0; c < nrhs; ++c) {
+    T *x = b + (size_t)c * (size_t)ldb;
+    for (long k = 0; k < n; ++k)
+      if (tr[k] != k) { T t = x[k]; x[k] = x[tr[k]]; x[tr[k]] = t; }
+    for (long j = 0; j < n; ++j)
+      for (long i = j + 1; i < n; ++i) x[i] -= AT(a, lda, i, j) * x[j];
+    for (long i = 0; i < n; ++i) {
+      const T d = AT(a, lda, i, i);
+      if (SFX(absv)(d) > tol) x[i] /= d;
+      else x[i] = (T)0;
+    }
+    for (long j = n - 1; j >= 0; --j) {
+      T s = x[j];
+      for (long i = j + 1; i < n; ++i) s -= AT(a, lda, i, j) * x[i];
+      x[j] = s;
+    }
+    for (long k = n - 1; k >= 0; --k)
+      if (tr[k] != k) { T t = x[k]; x[k] = x[tr[k]]; x[tr[k]] = t; }
+  }
 }
 
 /* ---------------------------------------------------------------- batched

@@ -7,6 +7,8 @@
 //   LLT<MatrixXd/MatrixXf, Lower|Upper>(A), .matrixLLT(), .info(), .solve(B), .rcond()
 //   PartialPivLU<MatrixXd/MatrixXf>(A), .matrixLU(), .permutationP(), .solve(B),
 //   .transpose().solve(B), .rcond(), .determinant()
+//   LDLT<MatrixXd/MatrixXf, Lower|Upper>(A), .matrixLDLT(), .transpositionsP(),
+//   .info(), .isPositive(), .isNegative(), .solve(B), .rcond()
 #include <Eigen/Dense>
 #include <cstring>
 
@@ -51,9 +53,44 @@ int lu_run(long n, const S* a, long lda, long nrhs, const S* b, long ldb, S* fac
   return 0;
 }
 
+// LDLT<Matrix, UpLo>(A): matrixLDLT(), transpositionsP().indices(), info(),
+// isPositive() / isNegative() (flags[0], flags[1]), solve(B), rcond().
+template <typename S, int UpLo>
+int ldlt_run(long n, const S* a, long lda, long nrhs, const S* b, long ldb, S* fact, int* tr, S* x, double* rcond,
+             int* flags)
+{
+  typedef Matrix<S, Dynamic, Dynamic> M;
+  Map<const M, 0, OuterStride<> > A(a, n, n, OuterStride<>(lda));
+  LDLT<M, UpLo> ldlt(A);
+  Map<M>(fact, n, n) = ldlt.matrixLDLT();
+  for (long i = 0; i < n; ++i) tr[i] = ldlt.transpositionsP().indices()(i);
+  flags[0] = ldlt.isPositive() ? 1 : 0;
+  flags[1] = ldlt.isNegative() ? 1 : 0;
+  if (nrhs > 0) {
+    Map<const M, 0, OuterStride<> > B(b, n, nrhs, OuterStride<>(ldb));
+    Map<M>(x, n, nrhs) = ldlt.solve(B);
+  }
+  if (rcond) *rcond = double(ldlt.rcond());
+  return ldlt.info() == Success ? 0 : 1;
+}
+
 }  // namespace
 
 extern "C" {
+
+int ref_ldlt_d(long n, const double* a, long lda, int upper, long nrhs, const double* b, long ldb, double* fact,
+               int* tr, double* x, double* rcond, int* flags)
+{
+  return upper ? ldlt_run<double, Upper>(n, a, lda, nrhs, b, ldb, fact, tr, x, rcond, flags)
+               : ldlt_run<double, Lower>(n, a, lda, nrhs, b, ldb, fact, tr, x, rcond, flags);
+}
+
+int ref_ldlt_s(long n, const float* a, long lda, int upper, long nrhs, const float* b, long ldb, float* fact,
+               int* tr, float* x, double* rcond, int* flags)
+{
+  return upper ? ldlt_run<float, Upper>(n, a, lda, nrhs, b, ldb, fact, tr, x, rcond, flags)
+               : ldlt_run<float, Lower>(n, a, lda, nrhs, b, ldb, fact, tr, x, rcond, flags);
+}
 
 int ref_llt_d(long n, const double* a, long lda, int upper, long nrhs, const double* b, long ldb, double* fact,
               double* x, double* rcond)

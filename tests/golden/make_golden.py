@@ -46,6 +46,23 @@ def sample_idx(n: int) -> np.ndarray:
     return np.sort(rng.choice(n * n, size=min(SAMPLE, n * n), replace=False)).astype(np.int64)
 
 
+# LDLT cases whose arithmetic is exact, so info and the sign do not depend on
+# rounding (LDLT.h:345-369)
+NAN = float("nan")
+LDLT_EXACT = {
+    "zero": [[0.0] * 5 for _ in range(5)],                                   # ZeroSign, Success
+    "zero_diag": [[0, 1, 0], [1, 0, 2], [0, 2, 0]],                          # whole diagonal zero: NumericalIssue
+    "diag_mixed": [[3, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, -2, 0, 0],
+                   [0, 0, 0, 0, 0], [0, 0, 0, 0, 5]],                        # Indefinite, zero pivots last
+    "semidef": [[4, 2, 0], [2, 1, 0], [0, 0, 0]],                            # PositiveSemiDef, Success
+    "zero_then_nonzero": [[1, 1, 0], [1, 1, 0], [0, 0, 0.5]],                # NumericalIssue
+    "nan_first": [[NAN, 1, 0], [1, 2, 0], [0, 0, 3]],                        # NaN first: the zero-diagonal branch
+    "ties": [[2, 1, 0, 0, 1], [1, -2, 1, 0, 0], [0, 1, 2, 1, 0],
+             [0, 0, 1, -2, 1], [1, 0, 0, 1, 2]],                             # equal |diagonal|: first one wins
+    "negdef": [[-4, 1, 0], [1, -3, 1], [0, 1, -5]],                          # NegativeSemiDef
+}
+
+
 def sketch_cols(n: int) -> int:
     return 4 if n > 4096 else 8
 
@@ -103,6 +120,11 @@ def gen(spec: dict) -> np.ndarray:
         if k == "near_tie_rows":
             scale = 1.0 + 1e-10 * O.gauss(spec["seed"] + 1, p, 1)[:, 0]
         a[rows + 1, :c0 + p] = -a[rows, :c0 + p] * scale[:, None]
+    elif k == "sym_gauss":  # symmetric indefinite: (G + G^T) / 2
+        g = O.gauss(spec["seed"], spec["n"], spec["n"])
+        a = np.asfortranarray((g + g.T) / 2)
+    elif k == "ldlt_exact":  # small patterns in exact arithmetic (zero / NaN pivots, diagonal ties)
+        a = np.asfortranarray(np.array(LDLT_EXACT[spec["pattern"]], dtype=np.float64))
     else:
         raise ValueError(k)
     if spec.get("dtype", "f64") == "f32":
@@ -221,6 +243,39 @@ def llt_case(spec: dict, arrays: dict, name: str) -> dict:
     return out
 
 
+def ldlt_case(spec: dict, arrays: dict, name: str) -> dict:
+    """LDLT<MatrixX?, Lower|Upper>(A): matrixLDLT(), transpositionsP(), info(),
+    isPositive(), isNegative(), solve(B), rcond(); and the C restatement's
+    distance to them (the noise floor)."""
+    a = gen(spec)
+    n = spec["n"]
+    upper = spec.get("upper", False)
+    nrhs = spec.get("nrhs", 2)
+    b = rhs(spec, nrhs)
+    fact, tr, info, pos, neg, x, rc = O.ref_ldlt(a, b, upper=upper)
+    out = dict(spec, kind="ldlt", info=info, is_positive=pos, is_negative=neg,
+               rcond=rc if np.isfinite(rc) else None, l1_norm=O.sym_l1_norm(a, upper))
+    tri = np.triu(fact) if upper else np.tril(fact)
+    arrays[name + "tr"] = tr.astype(np.int32)
+    arrays[name + "x"] = x
+    if n <= FULL_MAX:
+        arrays[name + "fact"] = fact
+    else:
+        idx = sample_idx(n)
+        arrays[name + "fact_idx"] = idx
+        arrays[name + "fact_val"] = tri.reshape(-1, order="F")[idx]
+        arrays[name + "fact_diag"] = np.diag(fact).copy()
+        arrays[name + "fact_sketch"] = tri.astype(np.float64) @ sketch_matrix(n)
+    f_o, tr_o, ok_o, sign_o = O.ldlt(a, upper=upper)
+    tri_o = np.triu(f_o) if upper else np.tril(f_o)
+    out["transpositions_oracle_equal"] = bool(np.array_equal(tr_o, tr))
+    out["sign_oracle"] = O.SIGN_NAMES[sign_o]
+    out["factor_floor"] = rel(tri_o, tri) if np.all(np.isfinite(tri)) else None
+    xo = O.ldlt_solve(f_o, tr_o, b, upper=upper)
+    out["x_floor"] = rel(xo, x) if np.all(np.isfinite(x)) else None
+    return out
+
+
 def cases():
     lu_sizes = [1, 2, 3, 4, 5, 8, 15, 16, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 256, 257, 300,
                 512, 1000, 2048]
@@ -251,6 +306,19 @@ def cases():
     for n, col in [(10, 6), (100, 77), (300, 130)]:
         yield "llt", dict(gen="late_fail", seed=950 + n, m=n, n=n, col=col)
     yield "llt", dict(gen="late_fail", seed=990, m=150, n=150, col=20, upper=True)
+    for n in [1, 2, 3, 5, 16, 17, 31, 32, 33, 64, 65, 100, 200, 512, 1000, 2048]:
+        yield "ldlt", dict(gen="spd", seed=1300 + n, m=n, n=n)
+    for n in [3, 33, 129, 257]:
+        yield "ldlt", dict(gen="spd", seed=1400 + n, m=n, n=n, upper=True)
+    for n in [9, 65, 200]:
+        yield "ldlt", dict(gen="spd", seed=1500 + n, m=n, n=n, dtype="f32")
+    for n in [5, 17, 64, 200]:
+        yield "ldlt", dict(gen="sym_gauss", seed=1600 + n, m=n, n=n)
+    yield "ldlt", dict(gen="sym_gauss", seed=1700, m=40, n=40, upper=True)
+    for pat in LDLT_EXACT:
+        k = len(LDLT_EXACT[pat])
+        yield "ldlt", dict(gen="ldlt_exact", pattern=pat, seed=1800, m=k, n=k)
+        yield "ldlt", dict(gen="ldlt_exact", pattern=pat, seed=1801, m=k, n=k, upper=True)
 
 
 def main() -> None:
@@ -263,6 +331,8 @@ def main() -> None:
             rec = lu_case(spec, arrays, name)
         elif kind == "getrf":
             rec = lu_rect_case(spec, arrays, name)
+        elif kind == "ldlt":
+            rec = ldlt_case(spec, arrays, name)
         else:
             rec = llt_case(spec, arrays, name)
         rec["name"] = name

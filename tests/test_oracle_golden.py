@@ -198,3 +198,38 @@ def test_batched_oracle_equals_the_pinned_per_item_oracle(dtype):
                 assert info[q] == fz and np.array_equal(f, fo)
                 assert np.array_equal(tr[roff[q]:roff[q] + n], tro)
                 assert np.array_equal(x, O.lu_solve(fo, tro, rhs[i].reshape(-1, 1))[:, 0], equal_nan=True)
+
+
+LDLT = [c for c in G.cases("ldlt") if c["n"] <= MAX_N_CPU]
+
+
+@pytest.mark.parametrize("case", LDLT, ids=[case_id(c) + ("-" + c["pattern"] if "pattern" in c else "") for c in LDLT])
+def test_oracle_ldlt_matches_reference(case):
+    """The C restatement of LDLT.h against the reference's own outputs:
+    identical transpositions, info and sign; factor and solution within the
+    tolerance, or within the recorded noise floor where diagonal pivoting
+    grows the rounding (indefinite matrices)."""
+    a = G.input(case)
+    upper = case.get("upper", False)
+    f, tr, ok, sign = O.ldlt(a, upper=upper)
+    assert np.array_equal(tr, G.arr(case, "tr")), "transpositions differ from the reference"
+    assert (0 if ok else 1) == case["info"]
+    assert (sign in (0, 2)) == case["is_positive"] and (sign in (1, 2)) == case["is_negative"]
+    full = G.arr(case, "fact")
+    tri = (lambda m: np.triu(m) if upper else np.tril(m))
+    if full is not None:
+        assert np.array_equal(f - tri(f), full - tri(full), equal_nan=True), "the other triangle must stay as given"
+        if case["factor_floor"] is None:
+            assert np.array_equal(f, full, equal_nan=True)
+        else:
+            assert rel(tri(f), tri(full)) <= max(tol(case), 1.001 * case["factor_floor"])
+    else:
+        d = rel(tri(f).astype(np.float64) @ sketch_matrix(case["n"]), G.arr(case, "fact_sketch"))
+        assert d <= max(tol(case), 3 * case["factor_floor"])
+    b = G.rhs(case, G.arr(case, "x").shape[1])
+    x = O.ldlt_solve(f, tr, b, upper=upper)
+    if case["x_floor"] is not None:
+        assert rel(x, G.arr(case, "x")) <= max(tol(case), 1.001 * case["x_floor"])
+    if case["rcond"] is not None and case["info"] == 0 and case["gen"] == "spd":
+        rc = O.ldlt_rcond(f, tr, O.sym_l1_norm(a, upper), upper=upper)
+        assert rc == pytest.approx(case["rcond"], rel=1e-9 if a.dtype == np.float64 else 1e-4)
