@@ -88,6 +88,25 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_lu_device_matrix": (c_vp, [c_vp, C.POINTER(c_i64)]),
     "gbs_lu_synchronize": (c_int, [c_vp]),
     "gbs_lu_set_stream": (c_int, [c_vp, c_vp]),
+    # LDLT object
+    "gbs_ldlt_create": (c_int, [C.POINTER(c_vp), c_int, c_int]),
+    "gbs_ldlt_destroy": (c_int, [c_vp]),
+    "gbs_ldlt_compute": (c_int, [c_vp, c_i64, c_vp, c_i64]),
+    "gbs_ldlt_compute_device": (c_int, [c_vp, c_i64, c_vp, c_i64]),
+    "gbs_ldlt_info": (c_int, [c_vp]),
+    "gbs_ldlt_sign": (c_int, [c_vp]),
+    "gbs_ldlt_is_positive": (c_int, [c_vp]),
+    "gbs_ldlt_is_negative": (c_int, [c_vp]),
+    "gbs_ldlt_solve": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
+    "gbs_ldlt_solve_device": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
+    "gbs_ldlt_rcond": (c_int, [c_vp, c_dp]),
+    "gbs_ldlt_l1_norm": (c_int, [c_vp, c_dp]),
+    "gbs_ldlt_matrix": (c_int, [c_vp, c_vp, c_i64]),
+    "gbs_ldlt_vector_d": (c_int, [c_vp, c_vp]),
+    "gbs_ldlt_transpositions": (c_int, [c_vp, c_vp]),
+    "gbs_ldlt_device_matrix": (c_vp, [c_vp, C.POINTER(c_i64)]),
+    "gbs_ldlt_synchronize": (c_int, [c_vp]),
+    "gbs_ldlt_set_stream": (c_int, [c_vp, c_vp]),
     # tensor cores
     "gbs_tc_gemm_sub": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_int, c_vp]),
     # mixed precision

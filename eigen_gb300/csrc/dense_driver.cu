@@ -226,6 +226,13 @@ int gemm_sub_device(cudaStream_t s, int phase, int M, int N, int K, const T* A, 
   return gemm_sub<T>(s, phase, M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, 0, nullptr);
 }
 
+template <typename T>
+int syrk_sub_device(cudaStream_t s, int phase, int n, int K, const T* A, int64_t a_rs, int64_t a_cs, const T* B,
+                    int64_t b_rs, int64_t b_cs, T* C, int64_t ldc)
+{
+  return gemm_sub<T>(s, phase, n, n, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, 1, nullptr);
+}
+
 // B(kb x ncols) <- L^{-1} B for a unit-lower L of kb <= 128 rows with many
 // columns: 32-row blocks solved one column per thread, SIMT updates between.
 template <typename T>
@@ -602,6 +609,7 @@ static int dec_solve(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, c
                      SolveWork& w)
 {
   if (kind == 0) GBS_TRY(lu_solve_device<T>(s, n, 1, dF, ld, dTr, v, n, adjoint, w));
+  else if (kind == 3) GBS_TRY(ldlt_solve_device<T>(s, n, 1, dF, ld, dTr, v, n, w));   // self-adjoint
   else GBS_TRY(llt_solve_device<T>(s, n, 1, dF, ld, kind == 2, v, n, w));
   return solve_status(s, w);
 }
@@ -708,6 +716,8 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
                                          SolveWork&, double*);                                                               \
   template int copy_matrix_device<T>(cudaStream_t, const T*, int64_t, T*, int64_t, int, int);                   \
   template int gemm_sub_device<T>(cudaStream_t, int, int, int, int, const T*, int64_t, int64_t, const T*, int64_t, \
+                                  int64_t, T*, int64_t);                                                       \
+  template int syrk_sub_device<T>(cudaStream_t, int, int, int, const T*, int64_t, int64_t, const T*, int64_t,     \
                                   int64_t, T*, int64_t);                                                       \
   template int trsm_lunit_wide<T>(cudaStream_t, int, int, const T*, int64_t, T*, int64_t);                     \
   template int laswp_gather_device<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int, int, int, DevBuf&); \

@@ -48,6 +48,7 @@ struct HostBuf {
 // timeout flag and one ready flag per block row; one per stream of use.
 struct SolveWork {
   DevBuf flags;
+  DevBuf tmp;     // row-permutation scratch of the LDLT solve
 };
 
 // Per-call workspace for the stateless (plug-in / LAPACK) entry points: a
@@ -135,7 +136,8 @@ template <typename T>
 int l1_norm_device(cudaStream_t s, const T* dA, int64_t lda, int m, int n, int sym, int upper, double* d_out,
                    double* h_out);
 
-// Hager/Higham estimate of ||A^{-1}||_1 (ConditionEstimator.h:56-142); kind 0 = LU,
+// Hager/Higham estimate of ||A^{-1}||_1 (ConditionEstimator.h:56-142); kind 3 =
+// LDLT (dF the lower factor of the permuted matrix, dTr its row order), kind 0 = LU,
 // 1 = LLT lower, 2 = LLT upper.  `vec` holds 2n scalars of device scratch.
 template <typename T>
 int inv_l1_estimate_device(cudaStream_t s, int kind, int n, const T* dF, int64_t ld, const int* dTr,
@@ -150,6 +152,18 @@ int copy_matrix_device(cudaStream_t s, const T* a, int64_t lda, T* b, int64_t ld
 template <typename T>
 int gemm_sub_device(cudaStream_t s, int phase, int M, int N, int K, const T* A, int64_t a_rs, int64_t a_cs, const T* B,
                     int64_t b_rs, int64_t b_cs, T* C, int64_t ldc);
+
+// Lower triangle of C (n x n) -= op(A) op(B) (the SYRK form of gemm_sub_device).
+template <typename T>
+int syrk_sub_device(cudaStream_t s, int phase, int n, int K, const T* A, int64_t a_rs, int64_t a_cs, const T* B,
+                    int64_t b_rs, int64_t b_cs, T* C, int64_t ldc);
+
+// LDLT solve (LDLT.h:540-577) on the lower factor W (unit L strictly below the
+// diagonal, D on it, ld) of the symmetrically permuted matrix; perm[i] = the
+// original row at position i.  In place on B (n x nrhs).
+template <typename T>
+int ldlt_solve_device(cudaStream_t s, int n, int nrhs, const T* W, int64_t ld, const int* perm, T* B, int64_t ldb,
+                      SolveWork& w);
 
 // B(kb x ncols) <- L^{-1} B, L unit lower with kb <= 128 rows and many columns.
 template <typename T>

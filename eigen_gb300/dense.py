@@ -172,6 +172,72 @@ class LLT(_Decomposition):
         return l @ l.T
 
 
+class LDLT(_Decomposition):
+    """Eigen::LDLT<Matrix<S,Dynamic,Dynamic>, UpLo> on the GPU (Cholesky with
+    diagonal pivoting, A = P^T L D L^T P, LDLT.h)."""
+    _prefix = "ldlt"
+    SIGNS = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")   # LDLT.h:22
+
+    def __init__(self, a=None, dtype=np.float64, upper: bool = False):
+        if a is not None and not isinstance(dtype, int):
+            dtype = a.dtype if not _is_torch_cuda(a) else {"torch.float64": np.float64,
+                                                           "torch.float32": np.float32}[str(a.dtype)]
+        super().__init__(dtype)
+        self.upper = upper
+        L.check(L.lib().gbs_ldlt_create(C.byref(self._h), self._code, L.GBS_UPPER if upper else L.GBS_LOWER),
+                "ldlt.create")
+        if a is not None:
+            self.compute(a)
+
+    def compute(self, a):
+        return self._compute(a)
+
+    def info(self) -> int:
+        return L.lib().gbs_ldlt_info(self._h)
+
+    def sign(self) -> int:
+        return int(L.lib().gbs_ldlt_sign(self._h))
+
+    def isPositive(self) -> bool:
+        return bool(L.lib().gbs_ldlt_is_positive(self._h))
+
+    def isNegative(self) -> bool:
+        return bool(L.lib().gbs_ldlt_is_negative(self._h))
+
+    def solve(self, b):
+        return self._solve(b)
+
+    def matrixLDLT(self):
+        return self._matrix()
+
+    def vectorD(self):
+        out = np.empty(self._n, dtype=_np_dtype(self._code))
+        L.check(L.lib().gbs_ldlt_vector_d(self._h, out.ctypes.data_as(C.c_void_p)), "ldlt.vector_d")
+        return out
+
+    def transpositionsP(self) -> np.ndarray:
+        out = np.zeros(max(self._n, 1), dtype=np.int32)
+        L.check(L.lib().gbs_ldlt_transpositions(self._h, out.ctypes.data_as(C.c_void_p)), "ldlt.transpositions")
+        return out[: self._n]
+
+    def matrixL(self):
+        m = self._matrix()
+        l = np.tril(m, -1) if not self.upper else np.triu(m, 1).T
+        return np.asfortranarray(l + np.eye(self._n, dtype=m.dtype))
+
+    def reconstructedMatrix(self):
+        """P^T L D L^T P (LDLT.h:594-618)."""
+        l = self.matrixL()
+        r = l @ np.diag(self.vectorD()) @ l.T
+        tr = self.transpositionsP()
+        p = np.arange(self._n)
+        for k in range(self._n):
+            p[[k, tr[k]]] = p[[tr[k], k]]
+        out = np.empty_like(r)
+        out[np.ix_(p, p)] = r
+        return out
+
+
 class PartialPivLU(_Decomposition):
     """Eigen::PartialPivLU<Matrix<S,Dynamic,Dynamic>> on the GPU."""
     _prefix = "lu"

@@ -195,6 +195,43 @@ void* gbs_lu_device_matrix(gbs_lu* lu, int64_t* ld);
 int gbs_lu_synchronize(gbs_lu* lu);
 int gbs_lu_set_stream(gbs_lu* lu, void* stream);
 
+/* gbs_ldlt mirrors Eigen::LDLT<Matrix<S,Dynamic,Dynamic>, UpLo> (LDLT.h:59-287),
+ * Cholesky with diagonal pivoting, A = P^T L D L^T P:
+ *   compute        LDLT::compute (LDLT.h:491-524): copy, ||A||_1 (symmetric,
+ *                  stored triangle read), ldlt_inplace<UpLo>::unblocked
+ *                  (LDLT.h:291-383); the transpositions are the reference's,
+ *                  bit for bit
+ *   info           GBS_SUCCESS or GBS_NUMERICAL_ISSUE, the reference's rule: a
+ *                  zero pivot whose column is not zero below the diagonal, or
+ *                  a nonzero pivot after a zero one
+ *   sign           LDLT.h:22 SignMatrix: 0 PositiveSemiDef, 1 NegativeSemiDef,
+ *                  2 ZeroSign, 3 Indefinite; is_positive / is_negative as
+ *                  isPositive() / isNegative() (LDLT.h:169-181)
+ *   solve          _solve_impl (LDLT.h:540-577), with D's pseudo-inverse
+ *   rcond          LDLT::rcond (ConditionEstimator.h:157-169)
+ *   matrix         matrixLDLT(): L strictly below (above, Upper) the diagonal,
+ *                  D on it, the other triangle as given
+ *   vector_d       vectorD(); transpositions: transpositionsP().indices() */
+typedef struct gbs_ldlt gbs_ldlt;
+int gbs_ldlt_create(gbs_ldlt** out, int dtype, int uplo);
+int gbs_ldlt_destroy(gbs_ldlt* ldlt);
+int gbs_ldlt_compute(gbs_ldlt* ldlt, int64_t n, const void* a, int64_t lda);
+int gbs_ldlt_compute_device(gbs_ldlt* ldlt, int64_t n, const void* d_a, int64_t lda);
+int gbs_ldlt_info(const gbs_ldlt* ldlt);
+int gbs_ldlt_sign(const gbs_ldlt* ldlt);
+int gbs_ldlt_is_positive(const gbs_ldlt* ldlt);
+int gbs_ldlt_is_negative(const gbs_ldlt* ldlt);
+int gbs_ldlt_solve(gbs_ldlt* ldlt, int64_t nrhs, const void* b, int64_t ldb, void* x, int64_t ldx);
+int gbs_ldlt_solve_device(gbs_ldlt* ldlt, int64_t nrhs, const void* d_b, int64_t ldb, void* d_x, int64_t ldx);
+int gbs_ldlt_rcond(gbs_ldlt* ldlt, double* rcond);
+int gbs_ldlt_l1_norm(const gbs_ldlt* ldlt, double* l1);
+int gbs_ldlt_matrix(gbs_ldlt* ldlt, void* out, int64_t ld);
+int gbs_ldlt_vector_d(gbs_ldlt* ldlt, void* out);
+int gbs_ldlt_transpositions(gbs_ldlt* ldlt, int* out);
+void* gbs_ldlt_device_matrix(gbs_ldlt* ldlt, int64_t* ld);
+int gbs_ldlt_synchronize(gbs_ldlt* ldlt);
+int gbs_ldlt_set_stream(gbs_ldlt* ldlt, void* stream);
+
 /* ------------------------------------------------------------------ tensor cores
  * The trailing update of the low-precision tiers as a standalone GEMM,
  * C (m x n, FP32) -= A (m x k) * B (k x n), all column-major on the device,
