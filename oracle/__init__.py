@@ -62,6 +62,8 @@ def port() -> C.CDLL:
             f.argtypes = [_L, p, _L, _ip, C.POINTER(C.c_int)]
             f = getattr(lib, f"oracle_ldlt_solve_{sfx}"); f.restype = None
             f.argtypes = [_L, p, _L, _ip, _L, p, _L]
+            f = getattr(lib, f"oracle_llt_rank_update_{sfx}"); f.restype = _L
+            f.argtypes = [_L, p, _L, p, C.c_double]
             vp = C.c_void_p
             f = getattr(lib, f"oracle_batched_llt_solve_{sfx}"); f.restype = None
             f.argtypes = [_L, _ip, _lp, vp, _lp, vp, _ip]
@@ -100,6 +102,16 @@ def ref() -> C.CDLL:
             f.argtypes = [_L, _L, p, _L, _ip, C.POINTER(C.c_int)]
             f = getattr(lib, f"ref_ldlt_{sfx}"); f.restype = C.c_int
             f.argtypes = [_L, p, _L, C.c_int, _L, p, _L, p, _ip, p, C.POINTER(C.c_double), _ip]
+            f = getattr(lib, f"ref_llt_rank_update_{sfx}"); f.restype = C.c_int
+            f.argtypes = [_L, p, _L, C.c_int, p, C.c_double, p]
+            sp = C.POINTER(C.c_double if sfx == "d" else C.c_float)
+            ip_ = C.POINTER(C.c_int)
+            f = getattr(lib, f"{sfx}gemm_"); f.restype = C.c_int
+            f.argtypes = [C.c_char_p, C.c_char_p, ip_, ip_, ip_, sp, p, ip_, p, ip_, sp, p, ip_]
+            f = getattr(lib, f"{sfx}trsm_"); f.restype = C.c_int
+            f.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, ip_, ip_, sp, p, ip_, p, ip_]
+            f = getattr(lib, f"{sfx}syrk_"); f.restype = C.c_int
+            f.argtypes = [C.c_char_p, C.c_char_p, ip_, ip_, sp, p, ip_, sp, p, ip_]
         lib.ref_llt_blocked_d.restype = _L
         lib.ref_llt_blocked_d.argtypes = [_L, _dp, _L]
         ip = C.POINTER(C.c_int)
@@ -215,6 +227,20 @@ def llt_rcond(fact: np.ndarray, a_norm: float, upper: bool = False) -> float:
     return getattr(port(), f"oracle_rcond_{_sfx(fact)}")(2 if upper else 1, n, fact, max(n, 1), dummy, a_norm)
 
 
+def llt_rank_update(fact: np.ndarray, v: np.ndarray, sigma: float, upper: bool = False):
+    """LLT::rankUpdate on a factor (matrixLLT layout): (updated factor, failing
+    column or -1).  Upper works on the transpose, as the reference does
+    (LLT.h:386-390)."""
+    f = np.array(fact, order="F", copy=True)
+    n = f.shape[0]
+    w = np.asfortranarray(f.T) if upper else f
+    vv = np.asfortranarray(np.asarray(v, dtype=f.dtype).reshape(n, 1))
+    ret = getattr(port(), f"oracle_llt_rank_update_{_sfx(f)}")(n, w, max(n, 1), vv, float(sigma))
+    if upper:
+        f = np.asfortranarray(w.T)
+    return f, int(ret)
+
+
 SIGN_NAMES = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")   # LDLT.h:22
 
 
@@ -328,6 +354,58 @@ def ref_ldlt(a: np.ndarray, b: np.ndarray | None = None, upper: bool = False):
     info = getattr(lib, f"ref_ldlt_{_sfx(a)}")(n, a, max(n, 1), int(upper), nrhs, bb, max(n, 1), fact, tr, x,
                                                C.byref(rc), flags)
     return fact, tr[:n], int(info), bool(flags[0]), bool(flags[1]), x[:, :nrhs], rc.value
+
+
+def ref_llt_rank_update(a: np.ndarray, v: np.ndarray, sigma: float, upper: bool = False):
+    """Eigen LLT<Matrix, Lower|Upper>(A).rankUpdate(v, sigma): (matrixLLT, info
+    (0 Success / 1 NumericalIssue))."""
+    a = np.asfortranarray(a)
+    n = a.shape[0]
+    fact = np.zeros((n, n), dtype=a.dtype, order="F")
+    vv = np.asfortranarray(v.reshape(n, 1), dtype=a.dtype)
+    info = getattr(ref(), f"ref_llt_rank_update_{_sfx(a)}")(n, a, max(n, 1), int(upper), vv, float(sigma), fact)
+    assert info != 2, "the input is not positive definite"
+    return fact, int(info)
+
+
+def _ci(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _cs(x, dtype):
+    return C.byref(C.c_double(x) if dtype == np.float64 else C.c_float(x))
+
+
+def ref_gemm(opa: str, opb: str, alpha, a, b, beta, c):
+    """The reference's BLAS ?gemm_ (blas/level3_impl.h:12-75) on copies: returns C."""
+    c = np.array(c, order="F", copy=True)
+    m, n = c.shape
+    k = a.shape[1] if opa in "Nn" else a.shape[0]
+    getattr(ref(), f"{_sfx(c)}gemm_")(opa.encode(), opb.encode(), _ci(m), _ci(n), _ci(k), _cs(alpha, c.dtype),
+                                      np.asfortranarray(a), _ci(max(a.shape[0], 1)), np.asfortranarray(b),
+                                      _ci(max(b.shape[0], 1)), _cs(beta, c.dtype), c, _ci(max(m, 1)))
+    return c
+
+
+def ref_trsm(side: str, uplo: str, opa: str, diag: str, alpha, a, b):
+    """The reference's BLAS ?trsm_ (blas/level3_impl.h:77-176) on copies: returns X."""
+    b = np.array(b, order="F", copy=True)
+    m, n = b.shape
+    getattr(ref(), f"{_sfx(b)}trsm_")(side.encode(), uplo.encode(), opa.encode(), diag.encode(), _ci(m), _ci(n),
+                                      _cs(alpha, b.dtype), np.asfortranarray(a), _ci(max(a.shape[0], 1)), b,
+                                      _ci(max(m, 1)))
+    return b
+
+
+def ref_syrk(uplo: str, op: str, alpha, a, beta, c):
+    """The reference's BLAS ?syrk_ (blas/level3_impl.h:357-433) on copies: returns C."""
+    c = np.array(c, order="F", copy=True)
+    n = c.shape[0]
+    k = a.shape[1] if op in "Nn" else a.shape[0]
+    getattr(ref(), f"{_sfx(c)}syrk_")(uplo.encode(), op.encode(), _ci(n), _ci(k), _cs(alpha, c.dtype),
+                                      np.asfortranarray(a), _ci(max(a.shape[0], 1)), _cs(beta, c.dtype), c,
+                                      _ci(max(n, 1)))
+    return c
 
 
 def ref_llt_blocked(a: np.ndarray):

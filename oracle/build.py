@@ -5,7 +5,8 @@
   ``-ffp-contract=off`` keeps its results identical on both.
 * ``oracle/_ref/libeigen_ref.so`` -- the reference itself: a small C++ wrapper
   (eigen_ref.cpp) over Eigen's own LLT / PartialPivLU / rcond plus Eigen's own
-  LAPACK shim (lapack/lu.cpp, lapack/cholesky.cpp, blas/xerbla.cpp), compiled
+  LAPACK shim (lapack/lu.cpp, lapack/cholesky.cpp, blas/xerbla.cpp) and BLAS
+  level-3 shim (blas/level3_impl.h), compiled
   directly from the read-only reference tree.  Built only where that tree is
   present; the fixtures it produces are committed under tests/golden/.
 
@@ -62,7 +63,7 @@ def build_reference(force: bool = False) -> Path | None:
     out_dir = HERE / "_ref"
     out_dir.mkdir(exist_ok=True)
     out = out_dir / "libeigen_ref.so"
-    deps = [HERE / "eigen_ref.cpp", HERE / "eigen_lapack_ref.cpp"]
+    deps = [HERE / "eigen_ref.cpp", HERE / "eigen_lapack_ref.cpp", HERE / "eigen_blas_ref.cpp"]
     if not (force or _stale(out, deps)):
         return out
     arch = ["-mavx2", "-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
@@ -71,7 +72,9 @@ def build_reference(force: bool = False) -> Path | None:
     objs = []
     for src, defs in (("eigen_ref.cpp", []),
                       ("eigen_lapack_ref.cpp", ["-DGB_REF_DOUBLE"]),
-                      ("eigen_lapack_ref.cpp", ["-DGB_REF_SINGLE"])):
+                      ("eigen_lapack_ref.cpp", ["-DGB_REF_SINGLE"]),
+                      ("eigen_blas_ref.cpp", ["-DGB_REF_DOUBLE"]),
+                      ("eigen_blas_ref.cpp", ["-DGB_REF_SINGLE"])):
         o = out_dir / (Path(src).stem + ("".join(d[2:].lower() for d in defs) or "") + ".o")
         _run(common + defs + ["-c", str(HERE / src), "-o", str(o)])
         objs.append(str(o))

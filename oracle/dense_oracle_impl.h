@@ -581,6 +581,67 @@ void SFX(oracle_ldlt_solve)(long n, const T *a, long lda, const int *tr, long nr
   }
 }
 
+/* ---------------------------------------------------------------- LLT rank update
+ * Eigen/src/Cholesky/LLT.h:231-299 (llt_rank_update_lower) on the lower factor:
+ * sigma > 0: Givens rotations, one per column (Jacobi.h:226-258 makeGivens of
+ * (l_ii, -t_i), Jacobi.h:317-327 applied to the column and t); sigma <= 0:
+ * the downdate, which stops at the first column whose new diagonal would not
+ * be positive.  Returns that column or -1. */
+long SFX(oracle_llt_rank_update)(long n, T *a, long lda, const T *vec, double sigma_d)
+{
+  const T sigma = (T)sigma_d;
+  T *t = (T *)malloc(sizeof(T) * (size_t)(n > 0 ? n : 1));
+  long ret = -1;
+  if (sigma > (T)0) {
+    const T ss = SQRT(sigma);
+    for (long i = 0; i < n; ++i) t[i] = ss * vec[i];
+    for (long i = 0; i < n; ++i) {
+      const T p = AT(a, lda, i, i), q = -t[i];
+      T c, s, r;
+      if (q == (T)0) { c = p < (T)0 ? (T)-1 : (T)1; s = 0; r = SFX(absv)(p); }
+      else if (p == (T)0) { c = 0; s = q < (T)0 ? (T)1 : (T)-1; r = SFX(absv)(q); }
+      else if (SFX(absv)(p) > SFX(absv)(q)) {
+        const T tt = q / p;
+        T u = SQRT((T)1 + tt * tt);
+        if (p < (T)0) u = -u;
+        c = (T)1 / u; s = -tt * c; r = p * u;
+      } else {
+        const T tt = p / q;
+        T u = SQRT((T)1 + tt * tt);
+        if (q < (T)0) u = -u;
+        s = -(T)1 / u; c = -tt * s; r = q * u;
+      }
+      AT(a, lda, i, i) = r;
+      if (c == (T)1 && s == (T)0) continue;
+      for (long k = i + 1; k < n; ++k) {
+        const T xi = AT(a, lda, k, i), yi = t[k];
+        AT(a, lda, k, i) = c * xi + s * yi;
+        t[k] = -s * xi + c * yi;
+      }
+    }
+  } else {
+    for (long i = 0; i < n; ++i) t[i] = vec[i];
+    T beta = 1;
+    for (long j = 0; j < n; ++j) {
+      const T ljj = AT(a, lda, j, j), dj = ljj * ljj, wj = t[j];
+      const T swj2 = sigma * wj * wj, gamma = dj * beta + swj2;
+      const T x = dj + swj2 / beta;
+      if (x <= (T)0) { ret = j; break; }
+      const T nljj = SQRT(x);
+      AT(a, lda, j, j) = nljj;
+      beta += swj2 / dj;
+      const T f = wj / ljj;
+      for (long k = j + 1; k < n; ++k) t[k] -= f * AT(a, lda, k, j);
+      if (gamma != (T)0) {
+        const T g1 = nljj / ljj, g2 = nljj * sigma * wj / gamma;
+        for (long k = j + 1; k < n; ++k) AT(a, lda, k, j) = g1 * AT(a, lda, k, j) + g2 * t[k];
+      }
+    }
+  }
+  free(t);
+  return ret;
+}
+
 /* ---------------------------------------------------------------- batched
  * The reference has no batch API; the CPU baseline is one decomposition per
  * matrix over an OpenMP parallel-for.  Matrices are packed back to back,

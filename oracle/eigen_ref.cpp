@@ -74,9 +74,35 @@ int ldlt_run(long n, const S* a, long lda, long nrhs, const S* b, long ldb, S* f
   return ldlt.info() == Success ? 0 : 1;
 }
 
+// LLT<Matrix, UpLo>(A).rankUpdate(v, sigma): matrixLLT() and info() after the update.
+template <typename S, int UpLo>
+int llt_rank_update_run(long n, const S* a, long lda, const S* v, double sigma, S* fact)
+{
+  typedef Matrix<S, Dynamic, Dynamic> M;
+  typedef Matrix<S, Dynamic, 1> V;
+  Map<const M, 0, OuterStride<> > A(a, n, n, OuterStride<>(lda));
+  LLT<M, UpLo> llt(A);
+  if (llt.info() != Success) return 2;
+  llt.rankUpdate(Map<const V>(v, n), S(sigma));
+  Map<M>(fact, n, n) = llt.matrixLLT();
+  return llt.info() == Success ? 0 : 1;
+}
+
 }  // namespace
 
 extern "C" {
+
+int ref_llt_rank_update_d(long n, const double* a, long lda, int upper, const double* v, double sigma, double* fact)
+{
+  return upper ? llt_rank_update_run<double, Upper>(n, a, lda, v, sigma, fact)
+               : llt_rank_update_run<double, Lower>(n, a, lda, v, sigma, fact);
+}
+
+int ref_llt_rank_update_s(long n, const float* a, long lda, int upper, const float* v, double sigma, float* fact)
+{
+  return upper ? llt_rank_update_run<float, Upper>(n, a, lda, v, sigma, fact)
+               : llt_rank_update_run<float, Lower>(n, a, lda, v, sigma, fact);
+}
 
 int ref_ldlt_d(long n, const double* a, long lda, int upper, long nrhs, const double* b, long ldb, double* fact,
                int* tr, double* x, double* rcond, int* flags)

@@ -21,6 +21,11 @@ What each case pins (reference API used):
         ?getrf_ ipiv (1-based) and info from the reference's LAPACK shim.
   llt   LLT<MatrixX?, Lower|Upper>(A): matrixLLT(), info(), solve(B), rcond();
         llt_inplace::blocked failing column; ?potrf_ info.
+  ldlt  LDLT<MatrixX?, Lower|Upper>(A): matrixLDLT(), transpositionsP(), info(),
+        isPositive(), isNegative(), solve(B), rcond().
+  blas  the reference's BLAS level-3 shim (blas/level3_impl.h): ?gemm_, ?trsm_,
+        ?syrk_ on seeded operands, every op / side / uplo / diag combination.
+  rank_update  LLT<MatrixXd, Lower|Upper>(A).rankUpdate(v, sigma): factor, info.
 """
 from __future__ import annotations
 
@@ -276,6 +281,90 @@ def ldlt_case(spec: dict, arrays: dict, name: str) -> dict:
     return out
 
 
+def blas_inputs(spec: dict):
+    """Operands of a BLAS case, rebuilt from seeds.  gemm: A (op(A) m x k), B
+    (op(B) k x n), C; trsm: A (a well-conditioned triangle; with diag 'U' its
+    diagonal holds NaN, which the routine must not read), B; syrk: A (op(A)
+    n x k), C.  C holds NaN when beta = 0, which the routine must not read."""
+    s, dt = spec["seed"], (np.float32 if spec.get("dtype") == "f32" else np.float64)
+    f = lambda x: np.asfortranarray(x.astype(dt))
+    if spec["op"] == "gemm":
+        m, n, k = spec["m"], spec["n"], spec["k"]
+        a = O.gauss(s, m, k) if spec["opa"] in "Nn" else O.gauss(s, k, m)
+        b = O.gauss(s + 1, k, n) if spec["opb"] in "Nn" else O.gauss(s + 1, n, k)
+        c = O.gauss(s + 2, m, n)
+        if spec["beta"] == 0:
+            c[::3, ::2] = np.nan
+        return f(a), f(b), f(c)
+    if spec["op"] == "trsm":
+        m, n = spec["m"], spec["n"]
+        na = m if spec["side"] in "Ll" else n
+        a = O.gauss(s, na, na) / np.sqrt(na)
+        a[np.diag_indices(na)] = 2.0 + np.abs(np.diag(a))
+        tri = np.tril(a) if spec["uplo"] in "Ll" else np.triu(a)
+        other = O.gauss(s + 3, na, na)            # the unused triangle: garbage the routine must not read
+        a = tri + (np.triu(other, 1) if spec["uplo"] in "Ll" else np.tril(other, -1))
+        if spec["diag"] in "Uu":
+            a[np.diag_indices(na)] = np.nan
+        return f(a), f(O.gauss(s + 1, m, n)), None
+    n, k = spec["n"], spec["k"]
+    a = O.gauss(s, n, k) if spec["opa"] in "Nn" else O.gauss(s, k, n)
+    c = O.gauss(s + 2, n, n)
+    if spec["beta"] == 0:
+        c[::3, ::2] = np.nan
+    return f(a), f(c), None
+
+
+def blas_case(spec: dict, arrays: dict, name: str) -> dict:
+    """The reference's BLAS shim (blas/level3_impl.h) on seeded operands; the
+    output in full up to 129^2 entries, else as a sketch; the noise floor is
+    the distance of a plain numpy restatement of the same formula."""
+    x, y, z = blas_inputs(spec)
+    op = spec["op"]
+    if op == "gemm":
+        out = O.ref_gemm(spec["opa"], spec["opb"], spec["alpha"], x, y, spec["beta"], z)
+        oa = x if spec["opa"] in "Nn" else x.T
+        ob = y if spec["opb"] in "Nn" else y.T
+        zz = np.zeros_like(z) if spec["beta"] == 0 else spec["beta"] * z
+        other = spec["alpha"] * (oa.astype(np.float64) @ ob.astype(np.float64)) + zz
+    elif op == "trsm":
+        out = O.ref_trsm(spec["side"], spec["uplo"], spec["opa"], spec["diag"], spec["alpha"], x, y)
+        t = np.tril(x) if spec["uplo"] in "Ll" else np.triu(x)
+        t = t.astype(np.float64)
+        if spec["diag"] in "Uu":
+            t[np.diag_indices(t.shape[0])] = 1.0
+        t = t if spec["opa"] in "Nn" else t.T
+        other = spec["alpha"] * (np.linalg.solve(t, y) if spec["side"] in "Ll" else np.linalg.solve(t.T, y.T).T)
+    else:
+        out = O.ref_syrk(spec["uplo"], spec["opa"], spec["alpha"], x, spec["beta"], y)
+        oa = (x if spec["opa"] in "Nn" else x.T).astype(np.float64)
+        zz = np.zeros_like(y) if spec["beta"] == 0 else spec["beta"] * y
+        full = spec["alpha"] * (oa @ oa.T) + zz
+        keep = np.tril if spec["uplo"] in "Ll" else np.triu
+        return_floor = rel(keep(full), keep(out))
+    if out.size <= FULL_MAX * FULL_MAX:
+        arrays[name + "out"] = out
+    else:
+        arrays[name + "out_sketch"] = out.astype(np.float64) @ sketch_matrix(out.shape[1])
+    return dict(spec, kind="blas", floor=return_floor if op == "syrk" else rel(other, out))
+
+
+def rank_update_case(spec: dict, arrays: dict, name: str) -> dict:
+    """LLT<Matrix, Lower|Upper>(A).rankUpdate(v, sigma) of the reference."""
+    a = O.spd(spec["seed"], spec["n"])
+    v = O.gauss(spec["seed"] + 1, spec["n"], 1)[:, 0]
+    fact, info = O.ref_llt_rank_update(a, v, spec["sigma"], spec.get("upper", False))
+    if spec["n"] <= FULL_MAX:
+        arrays[name + "fact"] = fact
+    else:
+        tri = np.triu(fact) if spec.get("upper") else np.tril(fact)
+        arrays[name + "fact_sketch"] = tri @ sketch_matrix(spec["n"])
+    f0, _ = O.llt(a, upper=spec.get("upper", False))
+    fo, ro = O.llt_rank_update(f0, v, spec["sigma"], spec.get("upper", False))
+    tri = (np.triu if spec.get("upper") else np.tril)
+    return dict(spec, kind="rank_update", info=info, floor=rel(tri(fo), tri(fact)))
+
+
 def cases():
     lu_sizes = [1, 2, 3, 4, 5, 8, 15, 16, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 256, 257, 300,
                 512, 1000, 2048]
@@ -319,6 +408,44 @@ def cases():
         k = len(LDLT_EXACT[pat])
         yield "ldlt", dict(gen="ldlt_exact", pattern=pat, seed=1800, m=k, n=k)
         yield "ldlt", dict(gen="ldlt_exact", pattern=pat, seed=1801, m=k, n=k, upper=True)
+    # BLAS level 3 (the reference's shim): every op combination, special alpha / beta
+    sd = 2000
+    for opa in "NT":
+        for opb in "NT":
+            for (m, n, k), (al, be) in [((7, 5, 3), (1.0, 0.0)), ((64, 33, 17), (-1.0, 1.0)),
+                                        ((129, 100, 65), (0.3, 0.7)), ((40, 30, 0), (2.0, 3.0))]:
+                sd += 10
+                yield "blas", dict(gen="blas", op="gemm", opa=opa, opb=opb, m=m, n=n, k=k, alpha=al, beta=be, seed=sd)
+    yield "blas", dict(gen="blas", op="gemm", opa="C", opb="N", m=50, n=40, k=30, alpha=0.0, beta=2.0, seed=2300)
+    yield "blas", dict(gen="blas", op="gemm", opa="N", opb="T", m=1000, n=700, k=600, alpha=-1.0, beta=1.0, seed=2310)
+    yield "blas", dict(gen="blas", op="gemm", opa="T", opb="N", m=300, n=200, k=100, alpha=0.5, beta=0.0,
+                       seed=2320, dtype="f32")
+    for side in "LR":
+        for uplo in "LU":
+            for opa in "NT":
+                for diag in "NU":
+                    sd += 10
+                    yield "blas", dict(gen="blas", op="trsm", side=side, uplo=uplo, opa=opa, diag=diag, m=37, n=23,
+                                       alpha=1.5, seed=sd)
+    yield "blas", dict(gen="blas", op="trsm", side="L", uplo="L", opa="N", diag="N", m=700, n=300, alpha=1.0,
+                       seed=2400)
+    yield "blas", dict(gen="blas", op="trsm", side="R", uplo="U", opa="T", diag="N", m=200, n=500, alpha=-2.0,
+                       seed=2410)
+    yield "blas", dict(gen="blas", op="trsm", side="L", uplo="U", opa="N", diag="U", m=90, n=40, alpha=1.0,
+                       seed=2420, dtype="f32")
+    for uplo in "LU":
+        for opa in "NT":
+            for al, be in [(-1.0, 0.5), (1.0, 0.0)]:
+                sd += 10
+                yield "blas", dict(gen="blas", op="syrk", uplo=uplo, opa=opa, n=40, k=25, alpha=al, beta=be, seed=sd)
+    yield "blas", dict(gen="blas", op="syrk", uplo="L", opa="N", n=600, k=300, alpha=-1.0, beta=1.0, seed=2500)
+    # LLT::rankUpdate: updates and downdates, lower and upper, a failing downdate
+    for n in [1, 5, 40, 300, 1000]:
+        for upper in (False, True):
+            for sigma in (0.7, -0.001, -1e4):
+                if n == 1000 and (upper or sigma == -1e4):
+                    continue
+                yield "rank_update", dict(gen="rank_update", seed=2600 + n, m=n, n=n, sigma=sigma, upper=upper)
 
 
 def main() -> None:
@@ -333,6 +460,10 @@ def main() -> None:
             rec = lu_rect_case(spec, arrays, name)
         elif kind == "ldlt":
             rec = ldlt_case(spec, arrays, name)
+        elif kind == "blas":
+            rec = blas_case(spec, arrays, name)
+        elif kind == "rank_update":
+            rec = rank_update_case(spec, arrays, name)
         else:
             rec = llt_case(spec, arrays, name)
         rec["name"] = name

@@ -200,6 +200,87 @@ def test_batched_oracle_equals_the_pinned_per_item_oracle(dtype):
                 assert np.array_equal(x, O.lu_solve(fo, tro, rhs[i].reshape(-1, 1))[:, 0], equal_nan=True)
 
 
+RANK = G.cases("rank_update")
+
+
+@pytest.mark.parametrize("case", RANK, ids=[f"n{c['n']}-s{c['sigma']}-{'U' if c['upper'] else 'L'}" for c in RANK])
+def test_oracle_llt_rank_update_matches_reference(case):
+    """LLT::rankUpdate (LLT.h:231-299) restated in C against the reference:
+    the same info (a downdate that loses definiteness fails), the factor within
+    1e-12 (the failing downdates: within the recorded floor)."""
+    from tests.golden.make_golden import rel as grel
+    a = O.spd(case["seed"], case["n"])
+    v = O.gauss(case["seed"] + 1, case["n"], 1)[:, 0]
+    upper = case["upper"]
+    f0, _ = O.llt(a, upper=upper)
+    f, r = O.llt_rank_update(f0, v, case["sigma"], upper=upper)
+    assert (1 if r >= 0 else 0) == case["info"]
+    tri = np.triu if upper else np.tril
+    full = G.arr(case, "fact")
+    if full is not None:
+        assert grel(tri(f), tri(full)) <= max(1e-12, 1.001 * case["floor"])
+        assert np.array_equal(f - tri(f), full - tri(full))
+    else:
+        d = grel(tri(f) @ sketch_matrix(case["n"]), G.arr(case, "fact_sketch"))
+        assert d <= max(1e-12, 3 * case["floor"])
+
+
+BLAS = G.cases("blas")
+
+
+def blas_id(c):
+    keys = ("op", "side", "uplo", "opa", "opb", "diag")
+    return "-".join(str(c[k]) for k in keys if k in c) + f"-{c.get('m', c['n'])}x{c['n']}" + \
+        ("-f32" if c.get("dtype") == "f32" else "")
+
+
+@pytest.mark.parametrize("case", BLAS, ids=[blas_id(c) for c in BLAS])
+def test_blas_fixtures_follow_the_blas_formulas(case):
+    """The reference's BLAS outputs stored in the fixtures satisfy the BLAS
+    definitions, checked with plain numpy (a sanity check of the fixtures and of
+    the operand rebuild the GPU tests use): gemm C = alpha op(A) op(B) + beta C
+    with beta = 0 ignoring C; trsm op(A) X = alpha B (X op(A) = alpha B)
+    without reading the diagonal for 'U' or the other triangle; syrk on one
+    triangle, the other untouched."""
+    from tests.golden.make_golden import blas_inputs
+    x, y, z = blas_inputs(case)
+    f64 = case.get("dtype") != "f32"
+    op = case["op"]
+    if op == "gemm":
+        oa = (x if case["opa"] in "Nn" else x.T).astype(np.float64)
+        ob = (y if case["opb"] in "Nn" else y.T).astype(np.float64)
+        zz = np.zeros(z.shape) if case["beta"] == 0 else case["beta"] * z.astype(np.float64)
+        want = case["alpha"] * (oa @ ob) + zz
+    elif op == "trsm":
+        t = (np.tril(x) if case["uplo"] in "Ll" else np.triu(x)).astype(np.float64)
+        if case["diag"] in "Uu":
+            t[np.diag_indices(t.shape[0])] = 1.0
+        t = t if case["opa"] in "Nn" else t.T
+        yy = y.astype(np.float64)
+        want = case["alpha"] * (np.linalg.solve(t, yy) if case["side"] in "Ll" else np.linalg.solve(t.T, yy.T).T)
+    else:
+        oa = (x if case["opa"] in "Nn" else x.T).astype(np.float64)
+        keep = np.tril if case["uplo"] in "Ll" else np.triu
+        zz = np.zeros(y.shape) if case["beta"] == 0 else case["beta"] * y.astype(np.float64)
+        want = keep(case["alpha"] * (oa @ oa.T) + zz)
+    out = G.arr(case, "out")
+    bound = 1e-5 if not f64 else 1e-12
+    if out is not None:
+        if op == "syrk":
+            keep = np.tril if case["uplo"] in "Ll" else np.triu
+            other = ~keep(np.ones(out.shape, dtype=bool))
+            assert np.array_equal(out[other], y[other], equal_nan=True), "syrk wrote the other triangle"
+            assert rel(keep(out), want) <= bound
+        else:
+            assert rel(out, want) <= bound
+    else:
+        if op == "syrk":
+            keep = np.tril if case["uplo"] in "Ll" else np.triu
+            want = want + np.where(~keep(np.ones(want.shape, dtype=bool)), y, 0.0)
+        s = sketch_matrix(want.shape[1])
+        assert rel(G.arr(case, "out_sketch"), want @ s) <= bound
+
+
 LDLT = [c for c in G.cases("ldlt") if c["n"] <= MAX_N_CPU]
 
 
