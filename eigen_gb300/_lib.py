@@ -88,6 +88,18 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_lu_device_matrix": (c_vp, [c_vp, C.POINTER(c_i64)]),
     "gbs_lu_synchronize": (c_int, [c_vp]),
     "gbs_lu_set_stream": (c_int, [c_vp, c_vp]),
+    "gbs_llt_rank_update": (c_int, [c_vp, c_vp, C.c_double]),
+    "gbs_llt_rank_update_device": (c_int, [c_vp, c_vp, C.c_double]),
+    # BLAS level 3 (scalars and sizes by pointer, as in the reference's shim)
+    **{f"gbs_{p}gemm{d}": (c_int, [C.c_char_p, C.c_char_p, c_ip, c_ip, c_ip, c_vp, c_vp, c_ip, c_vp, c_ip, c_vp, c_vp,
+                                   c_ip] + ([c_vp] if d else []))
+       for p in "ds" for d in ("", "_device")},
+    **{f"gbs_{p}trsm{d}": (c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, c_ip, c_ip, c_vp, c_vp, c_ip, c_vp,
+                                   c_ip] + ([c_vp] if d else []))
+       for p in "ds" for d in ("", "_device")},
+    **{f"gbs_{p}syrk{d}": (c_int, [C.c_char_p, C.c_char_p, c_ip, c_ip, c_vp, c_vp, c_ip, c_vp, c_vp, c_ip]
+                           + ([c_vp] if d else []))
+       for p in "ds" for d in ("", "_device")},
     # LDLT object
     "gbs_ldlt_create": (c_int, [C.POINTER(c_vp), c_int, c_int]),
     "gbs_ldlt_destroy": (c_int, [c_vp]),

@@ -272,6 +272,43 @@ extern "C" void* gbs_llt_device_matrix(gbs_llt* o, int64_t* ld)
   return o->A.p;
 }
 
+// LLT::rankUpdate (LLT.h:461-472): info() becomes NumericalIssue when a
+// downdate would make the matrix indefinite (the factor is then left as the
+// reference leaves it, updated up to the failing column), else Success.  The
+// stored ||A||_1 is not changed, as in the reference.
+static int llt_rank_update_common(gbs_llt* o, const void* d_v, double sigma)
+{
+  int failed = -1;
+  const int up = o->uplo == GBS_UPPER;
+  const int n = (int)o->n;
+  if (o->dtype == GBS_F64)
+    GBS_TRY(llt_rank_update_device<double>(o->stream, n, o->A.as<double>(), n, up, (const double*)d_v, sigma, o->tmp,
+                                           &failed));
+  else
+    GBS_TRY(llt_rank_update_device<float>(o->stream, n, o->A.as<float>(), n, up, (const float*)d_v, sigma, o->tmp,
+                                          &failed));
+  o->failed_col = failed;
+  o->info = failed >= 0 ? GBS_NUMERICAL_ISSUE : GBS_SUCCESS;
+  return GBS_SUCCESS;
+}
+
+extern "C" int gbs_llt_rank_update(gbs_llt* o, const void* v, double sigma)
+{
+  if (!o || !o->initialized) return GBS_NOT_INITIALIZED;
+  if (o->n > 0 && !v) return GBS_INVALID_ARGUMENT;
+  const size_t es = esize(o->dtype);
+  GBS_TRY(o->rhs.reserve(es * (size_t)std::max<int64_t>(o->n, 1)));
+  if (o->n > 0) GBS_CUDA_TRY(cudaMemcpyAsync(o->rhs.p, v, es * o->n, cudaMemcpyHostToDevice, o->stream));
+  return llt_rank_update_common(o, o->rhs.p, sigma);
+}
+
+extern "C" int gbs_llt_rank_update_device(gbs_llt* o, const void* d_v, double sigma)
+{
+  if (!o || !o->initialized) return GBS_NOT_INITIALIZED;
+  if (o->n > 0 && !d_v) return GBS_INVALID_ARGUMENT;
+  return llt_rank_update_common(o, d_v, sigma);
+}
+
 extern "C" int gbs_llt_synchronize(gbs_llt* o)
 {
   if (!o) return GBS_INVALID_ARGUMENT;

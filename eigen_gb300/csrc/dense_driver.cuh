@@ -165,6 +165,13 @@ template <typename T>
 int ldlt_solve_device(cudaStream_t s, int n, int nrhs, const T* W, int64_t ld, const int* perm, T* B, int64_t ldb,
                       SolveWork& w);
 
+// LLT::rankUpdate (LLT.h:231-299) on the factor in A (lower, or the upper
+// triangle read as the transposed view), v on the device; *failed = the first
+// column whose downdated diagonal would not be positive, or -1.  Waits for it.
+template <typename T>
+int llt_rank_update_device(cudaStream_t s, int n, T* A, int64_t lda, int upper, const T* d_v, double sigma,
+                           DevBuf& tmp, int* failed);
+
 // B(kb x ncols) <- L^{-1} B, L unit lower with kb <= 128 rows and many columns.
 template <typename T>
 int trsm_lunit_wide(cudaStream_t s, int kb, int ncols, const T* L, int64_t ldl, T* B, int64_t ldb);

@@ -160,6 +160,18 @@ class LLT(_Decomposition):
     def matrixLLT(self):
         return self._matrix()
 
+    def rankUpdate(self, v, sigma: float = 1.0):
+        """LLT::rankUpdate (LLT.h:461-472): the factor of A + sigma v v^T."""
+        if _is_torch_cuda(v):
+            self._bind_torch_stream()
+            L.check(L.lib().gbs_llt_rank_update_device(self._h, C.c_void_p(v.contiguous().data_ptr()), float(sigma)),
+                    "llt.rank_update")
+        else:
+            vv = np.ascontiguousarray(np.asarray(v).reshape(-1), dtype=_np_dtype(self._code))
+            L.check(L.lib().gbs_llt_rank_update(self._h, vv.ctypes.data_as(C.c_void_p), float(sigma)),
+                    "llt.rank_update")
+        return self
+
     def matrixL(self):
         m = self._matrix()
         return np.tril(m) if not self.upper else np.triu(m).T.copy(order="F")

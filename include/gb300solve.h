@@ -161,6 +161,15 @@ void* gbs_llt_device_matrix(gbs_llt* llt, int64_t* ld);     /* device pointer of
 int gbs_llt_synchronize(gbs_llt* llt);
 /* Use a caller-owned CUDA stream (cudaStream_t) instead of the object's own. */
 int gbs_llt_set_stream(gbs_llt* llt, void* stream);
+/* LLT::rankUpdate(v, sigma) (LLT.h:461-472, llt_rank_update_lower LLT.h:231-299):
+ * the factor of A + sigma v v^T from the factor of A, by Givens rotations
+ * (sigma > 0) or the downdate (sigma <= 0).  info() becomes
+ * GBS_NUMERICAL_ISSUE when a downdate would lose definiteness (the factor is
+ * then updated up to that column, as the reference leaves it), else
+ * GBS_SUCCESS; l1_norm() keeps the value of compute(), as in the reference.
+ * v: n scalars, host (rank_update) or device (rank_update_device). */
+int gbs_llt_rank_update(gbs_llt* llt, const void* v, double sigma);
+int gbs_llt_rank_update_device(gbs_llt* llt, const void* d_v, double sigma);
 
 /* gbs_lu mirrors Eigen::PartialPivLU<Matrix<S,Dynamic,Dynamic>> (PartialPivLU.h:75-311):
  *   compute        PartialPivLU::compute (PartialPivLU.h:514-536)
@@ -231,6 +240,52 @@ int gbs_ldlt_transpositions(gbs_ldlt* ldlt, int* out);
 void* gbs_ldlt_device_matrix(gbs_ldlt* ldlt, int64_t* ld);
 int gbs_ldlt_synchronize(gbs_ldlt* ldlt);
 int gbs_ldlt_set_stream(gbs_ldlt* ldlt, void* stream);
+
+/* ------------------------------------------------------------------ BLAS level 3
+ * The reference's BLAS shim on the GPU, same arguments and results as
+ * blas/level3_impl.h: ?gemm_ (:12-75), ?trsm_ (:77-176), ?syrk_ (:357-433).
+ *   gemm   C = alpha op(A) op(B) + beta C (op: 'N', 'T' or 'C'); beta = 0 sets
+ *          C to zero without reading it; k = 0 only scales C
+ *   trsm   solves op(A) X = B (side 'L') or X op(A) = B (side 'R') for the
+ *          uplo triangle of A, then X *= alpha; with diag 'U' the diagonal is
+ *          not read; X overwrites B
+ *   syrk   C = alpha op(A) op(A)^T + beta C (op 'N': A n x k; 'T'/'C': A k x n)
+ *          on the uplo triangle of C only
+ * Returns 0, or the position of the first invalid argument (the number the
+ * reference reports through xerbla; the text is in gbs_last_error()), or
+ * -(100 + gbs_status) on a library error.  Host variants copy their operands
+ * to the GPU and C (B for trsm) back; *_device variants take device buffers
+ * and run stream-ordered on `stream` (NULL: the legacy default stream). */
+int gbs_dgemm(const char* transa, const char* transb, const int* m, const int* n, const int* k, const double* alpha,
+              const double* a, const int* lda, const double* b, const int* ldb, const double* beta, double* c,
+              const int* ldc);
+int gbs_sgemm(const char* transa, const char* transb, const int* m, const int* n, const int* k, const float* alpha,
+              const float* a, const int* lda, const float* b, const int* ldb, const float* beta, float* c,
+              const int* ldc);
+int gbs_dgemm_device(const char* transa, const char* transb, const int* m, const int* n, const int* k,
+                     const double* alpha, const double* d_a, const int* lda, const double* d_b, const int* ldb,
+                     const double* beta, double* d_c, const int* ldc, void* stream);
+int gbs_sgemm_device(const char* transa, const char* transb, const int* m, const int* n, const int* k,
+                     const float* alpha, const float* d_a, const int* lda, const float* d_b, const int* ldb,
+                     const float* beta, float* d_c, const int* ldc, void* stream);
+int gbs_dtrsm(const char* side, const char* uplo, const char* transa, const char* diag, const int* m, const int* n,
+              const double* alpha, const double* a, const int* lda, double* b, const int* ldb);
+int gbs_strsm(const char* side, const char* uplo, const char* transa, const char* diag, const int* m, const int* n,
+              const float* alpha, const float* a, const int* lda, float* b, const int* ldb);
+int gbs_dtrsm_device(const char* side, const char* uplo, const char* transa, const char* diag, const int* m,
+                     const int* n, const double* alpha, const double* d_a, const int* lda, double* d_b,
+                     const int* ldb, void* stream);
+int gbs_strsm_device(const char* side, const char* uplo, const char* transa, const char* diag, const int* m,
+                     const int* n, const float* alpha, const float* d_a, const int* lda, float* d_b, const int* ldb,
+                     void* stream);
+int gbs_dsyrk(const char* uplo, const char* trans, const int* n, const int* k, const double* alpha, const double* a,
+              const int* lda, const double* beta, double* c, const int* ldc);
+int gbs_ssyrk(const char* uplo, const char* trans, const int* n, const int* k, const float* alpha, const float* a,
+              const int* lda, const float* beta, float* c, const int* ldc);
+int gbs_dsyrk_device(const char* uplo, const char* trans, const int* n, const int* k, const double* alpha,
+                     const double* d_a, const int* lda, const double* beta, double* d_c, const int* ldc, void* stream);
+int gbs_ssyrk_device(const char* uplo, const char* trans, const int* n, const int* k, const float* alpha,
+                     const float* d_a, const int* lda, const float* beta, float* d_c, const int* ldc, void* stream);
 
 /* ------------------------------------------------------------------ tensor cores
  * The trailing update of the low-precision tiers as a standalone GEMM,
