@@ -38,6 +38,10 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_last_error": (C.c_char_p, []),
     "gbs_version": (C.c_char_p, []),
     "gbs_device_count": (c_int, []),
+    # failure detection
+    "gbs_set_wait_limit": (C.c_double, [C.c_double]),
+    "gbs_selftest_solve_timeout": (c_int, [c_int]),
+    "gbs_selftest_barrier_timeout": (c_int, []),
     # plug-in level
     "gbs_llt_blocked_d": (c_i64, [c_i64, c_vp, c_i64, c_int]),
     "gbs_llt_blocked_s": (c_i64, [c_i64, c_vp, c_i64, c_int]),

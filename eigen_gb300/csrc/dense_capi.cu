@@ -58,6 +58,40 @@ extern "C" int gbs_device_count(void)
   return usable;
 }
 
+extern "C" double gbs_set_wait_limit(double seconds)
+{
+  const double prev = (double)wait_limit_ns() * 1e-9;
+  set_wait_limit_ns(seconds > 0 ? (uint64_t)(seconds * 1e9 + 0.5) : 0);
+  return prev;
+}
+
+namespace {
+
+// Runs one diagnostic on a private stream that is destroyed afterwards.
+template <typename F>
+int on_private_stream(F&& f)
+{
+  GBS_TRY(ensure_device());
+  cudaStream_t s;
+  GBS_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const int rc = f(s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int gbs_selftest_solve_timeout(int n)
+{
+  return on_private_stream([n](cudaStream_t s) { return tri_solve_timeout_selftest(s, n); });
+}
+
+extern "C" int gbs_selftest_barrier_timeout(void)
+{
+  return on_private_stream([](cudaStream_t s) { return barrier_timeout_selftest(s); });
+}
+
 // =================================================================== LLT object
 struct gbs_llt {
   int dtype = GBS_F64;

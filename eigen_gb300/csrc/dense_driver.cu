@@ -2,6 +2,7 @@
 // loops, triangular solves, ||A||_1 and the Hager/Higham rcond estimator,
 // all stream-ordered on device buffers.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -154,11 +155,18 @@ WorkspaceLease::~WorkspaceLease()
 }
 
 // ------------------------------------------------------------------ status
+static std::atomic<uint64_t> g_wait_limit_ns{kSpinDeadlineNs};
+
+uint64_t wait_limit_ns() { return g_wait_limit_ns.load(std::memory_order_relaxed); }
+
+void set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns ? ns : kSpinDeadlineNs, std::memory_order_relaxed); }
+
 int reset_status(DeviceStatus* d_st, cudaStream_t s)
 {
   DeviceStatus h;
   memset(&h, 0, sizeof(h));
   h.info = -1;
+  h.limit_ns = wait_limit_ns();
   // the status word is tiny: a kernel-free 32-byte upload per factorization
   GBS_CUDA_TRY(cudaMemcpyAsync(d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   GBS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -512,6 +520,11 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
   const int forward = (lower != 0) != (trans != 0);
   const int nblk = ceil_div(n, NB);
   GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
+  if (!w.err.p) {
+    GBS_TRY(w.err.reserve(16));
+    GBS_CUDA_TRY(cudaMemsetAsync(w.err.p, 0, 16, s));
+  }
+  const uint64_t limit = wait_limit_ns();
   const int grid = std::min(nblk, 2 * device_sm_count());
   constexpr size_t smem = trsm_persistent_smem<T, NB, RC>();
   static const cudaError_t attr = cudaFuncSetAttribute(trsm_persistent_kernel<T, NB, RC>,
@@ -523,7 +536,7 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
     PhaseScope ps(s, PH_TRI_SOLVE, (double)n * n * nc, sizeof(T) * (0.5 * (double)n * n + 2.0 * n * nc));
     trsm_persistent_kernel<T, NB, RC><<<grid, RC * 32, smem, s>>>(n, nc, tri, rs, cs, forward, unit,
                                                                    B + (int64_t)c0 * ldb, ldb, w.flags.as<int>(),
-                                                                   dinv);
+                                                                   dinv, w.err.as<int>(), limit);
     GBS_CUDA_TRY(cudaGetLastError());
   }
   return GBS_SUCCESS;
@@ -532,14 +545,65 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
 int solve_status(cudaStream_t s, SolveWork& w)
 {
   GBS_CUDA_TRY(cudaStreamSynchronize(s));
-  if (!w.flags.p) return GBS_SUCCESS;
-  int h[2] = {0, 0};
-  GBS_CUDA_TRY(cudaMemcpy(h, w.flags.p, sizeof(h), cudaMemcpyDeviceToHost));
-  if (h[1]) {
+  if (!w.err.p) return GBS_SUCCESS;
+  int h = 0;
+  GBS_CUDA_TRY(cudaMemcpy(&h, w.err.p, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h) {
+    GBS_CUDA_TRY(cudaMemset(w.err.p, 0, sizeof(h)));    // the next solve on this workspace starts clean
     gbs_set_last_message("a triangular-solve wait timed out");
     return GBS_TIMEOUT;
   }
   return GBS_SUCCESS;
+}
+
+// Failure-detection diagnostics.  The persistent solve of an n x n system
+// (identity triangle, one right-hand side) with the ticket counter started at
+// 1: no CTA ever takes block 0, so its ready flag is never published and every
+// CTA's first wait runs out; after the first timeout the others see the flag
+// and leave, so the launch ends after about one wait limit.
+int tri_solve_timeout_selftest(cudaStream_t s, int n)
+{
+  constexpr int NB = tri_solve_nb<double>();
+  constexpr int RC = 16;
+  if (n < 2 * NB) n = 2 * NB;
+  const int nblk = ceil_div(n, NB);
+  DevBuf tri, b;
+  SolveWork w;
+  GBS_TRY(tri.reserve(sizeof(double) * (size_t)n * n));
+  GBS_TRY(b.reserve(sizeof(double) * (size_t)n));
+  GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
+  GBS_TRY(w.err.reserve(16));
+  GBS_CUDA_TRY(cudaMemsetAsync(tri.p, 0, sizeof(double) * (size_t)n * n, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(b.p, 0, sizeof(double) * (size_t)n, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(w.flags.p, 0, sizeof(int) * (size_t)(nblk + 2), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(w.err.p, 0, 16, s));
+  static const int one = 1;
+  GBS_CUDA_TRY(cudaMemcpyAsync(w.flags.p, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  const int grid = std::min(nblk, 2 * device_sm_count());
+  constexpr size_t smem = trsm_persistent_smem<double, NB, RC>();
+  GBS_CUDA_TRY(cudaFuncSetAttribute(trsm_persistent_kernel<double, NB, RC>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  count_launch();
+  trsm_persistent_kernel<double, NB, RC><<<grid, RC * 32, smem, s>>>(n, 1, tri.as<double>(), 1, n, 1, 1,
+                                                                    b.as<double>(), n, w.flags.as<int>(), nullptr,
+                                                                    w.err.as<int>(), wait_limit_ns());
+  GBS_CUDA_TRY(cudaGetLastError());
+  return solve_status(s, w);
+}
+
+// Two CTAs meet at a grid barrier that counts three arrivals.
+__global__ void barrier_selftest_kernel(DeviceStatus* st) { grid_barrier(st, gridDim.x + 1); }
+
+int barrier_timeout_selftest(cudaStream_t s)
+{
+  DevBuf st;
+  GBS_TRY(st.reserve(sizeof(DeviceStatus)));
+  GBS_TRY(reset_status(st.as<DeviceStatus>(), s));
+  count_launch();
+  barrier_selftest_kernel<<<2, 32, 0, s>>>(st.as<DeviceStatus>());
+  GBS_CUDA_TRY(cudaGetLastError());
+  DeviceStatus h;
+  return read_status(st.as<DeviceStatus>(), &h, s);
 }
 
 template <typename T>

@@ -44,10 +44,13 @@ struct HostBuf {
   HostBuf& operator=(const HostBuf&) = delete;
 };
 
-// Device workspace of the persistent triangular solve: ticket counter,
-// timeout flag and one ready flag per block row; one per stream of use.
+// Device workspace of the persistent triangular solve: ticket counter and one
+// ready flag per block row (zeroed before each launch), and a timeout flag that
+// stays set across launches until solve_status reads and clears it; one per
+// stream of use.
 struct SolveWork {
   DevBuf flags;
+  DevBuf err;
   DevBuf tmp;     // row-permutation scratch of the LDLT solve
 };
 
@@ -70,6 +73,12 @@ struct WorkspaceLease {
 // ---- plain-path drivers (device pointers, stream-ordered; the status word
 // must be zero-initialised with info = -1 before a factorization)
 int reset_status(DeviceStatus* d_st, cudaStream_t s);
+// Sets the process-wide wait limit (0: the 2 s default).
+void set_wait_limit_ns(uint64_t ns);
+// Failure-detection diagnostics: one launch each whose wait never succeeds;
+// both return GBS_TIMEOUT when the wait expired and the launch ended.
+int tri_solve_timeout_selftest(cudaStream_t s, int n);
+int barrier_timeout_selftest(cudaStream_t s);
 int read_status(const DeviceStatus* d_st, DeviceStatus* h_st, cudaStream_t s);
 
 constexpr int kPanelNB = 32;   // columns factored per panel launch

@@ -588,8 +588,10 @@ trsm_rlt_blocked_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restr
 // side (rows spread over lanes, shuffles carry x_r), writes x_i and raises its
 // flag.  A CTA only takes a ticket while running and only waits on lower
 // tickets, so the lowest unfinished block always progresses.  work: [0] ticket
-// counter, [1] timeout flag, [2..] one ready flag per block; zeroed before
-// launch.  Dynamic shared memory: trsm_persistent_smem<T, NB, RC>().
+// counter, [1] unused, [2..] one ready flag per block; zeroed before launch.
+// err: timeout flag, set to 1 when a wait runs past limit_ns and left set
+// across launches until the host reads it.  Dynamic shared memory:
+// trsm_persistent_smem<T, NB, RC>().
 template <typename T, int NB>
 struct TrsmSuper { static constexpr int value = 256 / NB; };
 
@@ -607,7 +609,7 @@ constexpr size_t trsm_persistent_smem()
 template <typename T, int NB, int RC>
 __global__ void __launch_bounds__(RC * 32, 2)
 trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, int64_t cs, int forward, int unit,
-                       T* B, int64_t ldb, int* work, const T* __restrict__ dinv)
+                       T* B, int64_t ldb, int* work, const T* __restrict__ dinv, int* err, uint64_t limit_ns)
 {
   constexpr int PER = NB / 32;
   constexpr int SUPER = TrsmSuper<T, NB>::value;
@@ -617,8 +619,8 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
   static_assert(G * NB == RC * 32 && CPT * G == RC, "thread mapping");
   const int nblk = (n + NB - 1) / NB;
   int* counter = work;
-  int* err = work + 1;
   int* flags = work + 2;
+  const uint64_t limit = effective_limit(limit_ns);
   extern __shared__ __align__(16) unsigned char trsm_sm[];
   T(*sT)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(trsm_sm);                         // [KMAX][NB+1], k-major
   T(*sX)[RC] = reinterpret_cast<T(*)[RC]>(trsm_sm + sizeof(T) * KMAX * (NB + 1));     // [KMAX][RC]
@@ -681,7 +683,7 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
           unsigned int spins = 0;
           while (ld_acquire_u32((const unsigned int*)&flags[bj0]) == 0u) {
             if ((++spins & 63u) == 0 &&
-                (ld_volatile_i32(err) || globaltimer_ns() - t0 > kSpinDeadlineNs)) {
+                (ld_volatile_i32(err) || globaltimer_ns() - t0 > limit)) {
               atomicExch(err, 1);
               ok = 0;
               break;

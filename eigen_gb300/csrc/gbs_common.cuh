@@ -37,7 +37,8 @@ struct DeviceStatus {
   int timeout;              // set to 1 by any wait that ran out of time
   int info;                 // LLT: first failing column (-1 = none); LU: first zero pivot (-1)
   int nb_transpositions;    // LU: number of actual row swaps
-  int pad[3];
+  int pad0;
+  unsigned long long limit_ns;  // wait limit of this factorization's spins (0: the default)
 };
 
 __device__ __forceinline__ uint64_t globaltimer_ns()
@@ -59,8 +60,15 @@ __device__ __forceinline__ int ld_volatile_i32(const int* p)
   return *(const volatile int*)p;
 }
 
-// Wait limit of every inter-CTA spin in this library (2 s of wall time).
+// Default wait limit of every inter-CTA spin in this library (2 s of wall
+// time).  The limit in force is a process-wide runtime value
+// (gbs_set_wait_limit) that the host passes to each launch; 0 means this default.
 constexpr uint64_t kSpinDeadlineNs = 2000000000ull;
+
+// Host: the wait limit the next launches get, in nanoseconds.
+uint64_t wait_limit_ns();
+
+__host__ __device__ __forceinline__ uint64_t effective_limit(uint64_t ns) { return ns ? ns : kSpinDeadlineNs; }
 
 // Sense-free grid barrier for a cooperative launch (all CTAs co-resident).
 // Returns false (on every thread of the CTA) if the barrier timed out or if
@@ -79,11 +87,12 @@ __device__ __forceinline__ bool grid_barrier(DeviceStatus* st, unsigned int nblo
       __threadfence();
       atomicAdd(&st->bar_gen, 1u);
     } else {
+      const uint64_t limit = effective_limit(*(const volatile unsigned long long*)&st->limit_ns);
       uint64_t t0 = globaltimer_ns();
       unsigned int spins = 0;
       while (ld_acquire_u32(&st->bar_gen) == gen) {
         if ((++spins & 63u) == 0) {
-          if (ld_volatile_i32(&st->timeout) || globaltimer_ns() - t0 > kSpinDeadlineNs) {
+          if (ld_volatile_i32(&st->timeout) || globaltimer_ns() - t0 > limit) {
             atomicExch(&st->timeout, 1);
             ok = 0;
             break;

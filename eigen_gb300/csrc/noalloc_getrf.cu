@@ -29,9 +29,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // The status word keeps the previous call's contents: start every call from
 // zero (barrier counters, timeout flag, swap count) with info = -1.
-__global__ void noalloc_reset_status(DeviceStatus* st)
+__global__ void noalloc_reset_status(DeviceStatus* st, unsigned long long limit_ns)
 {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
+    st->limit_ns = limit_ns;
     st->bar_count = 0;
     st->bar_gen = 0;
     st->timeout = 0;
@@ -112,7 +113,7 @@ extern "C" int gbs_dgetrf_noalloc(int m, int n, double* d_a, int lda, int* d_ipi
   }
 
   count_launch();
-  noalloc_reset_status<<<1, 32, 0, s>>>(st);
+  noalloc_reset_status<<<1, 32, 0, s>>>(st, wait_limit_ns());
   GBS_CUDA_TRY(cudaGetLastError());
   int rc = GBS_SUCCESS;
   if (size > 0) {

@@ -177,6 +177,7 @@ struct TcParams {
   int tf32;                 // 1: kind::tf32, 0: kind::f16
   uint32_t idesc;
   int* err;
+  uint64_t limit_ns;        // wait limit of the pipeline's mbarrier waits (0: the default)
 };
 
 __device__ __forceinline__ bool skip_tile(const TcParams& p, int tm, int tn)
@@ -213,7 +214,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
   const int num_tiles = p.tiles_m * p.tiles_n;
-  const uint64_t LIMIT = kSpinDeadlineNs;
+  const uint64_t LIMIT = effective_limit(p.limit_ns);
 
   if (warp == 0) {
     if (lane == 0) {
@@ -499,6 +500,7 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   p.tf32 = esize == 4;
   p.idesc = idesc_for(kind == TC_BF16 ? 1 : kind == TC_FP16 ? 0 : 2, BM, BN);
   p.err = &st->timeout;
+  p.limit_ns = wait_limit_ns();
   const int tiles = p.tiles_m * p.tiles_n;
   const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
   // algorithmic flops of the update (a 3xTF32 update issues three such products on the tensor cores)

@@ -63,6 +63,27 @@ const char* gbs_version(void);
 /* Number of usable sm_103a devices (0 when none). */
 int gbs_device_count(void);
 
+/* Failure detection (no counterpart in the reference, whose CPU code has no
+ * inter-thread waits).  Every wait of one CTA on another (grid barriers of the
+ * cooperative panel kernels, ready flags of the persistent triangular solve,
+ * mbarrier waits of the tensor-core GEMM) gives up after a wall-time limit;
+ * the launch then ends, the call returns GBS_TIMEOUT (-(100 + GBS_TIMEOUT)
+ * where a call returns statuses negated) and the CUDA context stays usable.
+ * gbs_set_wait_limit sets that limit for the launches issued after it, process
+ * wide; seconds <= 0 restores the 2 s default.  Returns the previous limit in
+ * seconds. */
+double gbs_set_wait_limit(double seconds);
+/* Diagnostics of the bounded waits: each runs one launch whose wait can never
+ * be satisfied and reports what the caller would see, on a private stream.
+ *  - gbs_selftest_solve_timeout: the persistent triangular solve of an n x n
+ *    system with the first block's ready flag never published;
+ *  - gbs_selftest_barrier_timeout: a grid barrier that counts one CTA more than
+ *    the launch has.
+ * Both return GBS_TIMEOUT when the waits expired and the launch ended cleanly
+ * (any other status is a failure of the mechanism). */
+int gbs_selftest_solve_timeout(int n);
+int gbs_selftest_barrier_timeout(void);
+
 /* ------------------------------------------------------------------ 1. plug-in
  * Replaces internal::llt_inplace<Scalar,Lower|Upper>::blocked(m)
  * (Eigen/src/Cholesky/LLT.h:331-360; LAPACKE form LLT_LAPACKE.h:64-88).

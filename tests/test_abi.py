@@ -59,3 +59,18 @@ def test_no_device_is_reported_not_faked():
     r = L.gbs_partial_lu_blocked_d(3, 3, a.ctypes.data_as(C.c_void_p), 3, tr.ctypes.data_as(C.c_void_p), C.byref(nbt))
     assert r == -(100 + _lib.GBS_NO_DEVICE)
     assert b"device" in L.gbs_last_error()
+
+
+def test_wait_limit_setter_round_trips():
+    """gbs_set_wait_limit is host state only: it returns the previous limit and
+    restores the 2 s default for values <= 0."""
+    from eigen_gb300 import _lib
+    L = _lib.lib()
+    first = L.gbs_set_wait_limit(0.25)
+    try:
+        assert L.gbs_set_wait_limit(0.001) == pytest.approx(0.25)
+        assert L.gbs_set_wait_limit(0.0) == pytest.approx(0.001)
+        assert L.gbs_set_wait_limit(-1.0) == pytest.approx(2.0)
+    finally:
+        L.gbs_set_wait_limit(first)
+    assert L.gbs_selftest_barrier_timeout() in (_lib.GBS_NO_DEVICE, _lib.GBS_TIMEOUT)
