@@ -82,6 +82,8 @@ def args_parse():
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--lookahead", type=int, default=0, choices=[0, 1],
+                   help="LU: factor block k+1's panels on a second stream during block k's update (default 0)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
                    help="factor one seeded system and exit (small ncu captures)")
@@ -427,7 +429,7 @@ def run_ours(args):
     A = torch.from_numpy(np.ascontiguousarray(a_host.T)).cuda().t()
     B = torch.from_numpy(np.ascontiguousarray(b_host.T)).cuda().t()
     X = torch.empty(nrhs, n, dtype=torch.float64, device="cuda").t()
-    opt = options(args.path, tol=BE_BAR)
+    opt = options(args.path, tol=BE_BAR, lookahead=bool(args.lookahead))
     info = RefineInfo()
     lu = gb.PartialPivLU(dtype=np.float64)
     L.gbs_lu_set_stream(lu._h, C.c_void_p(stream.cuda_stream))

@@ -347,6 +347,68 @@ int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, i
   return GBS_SUCCESS;
 }
 
+// The same row map for up to 128 interchanges of rows in [i0, m): the source
+// row of every row of [i0, m) in shared memory, the interchanges replayed on
+// it by one thread (constant time each), then the moved rows collected in
+// parallel (the gather does not depend on the order of the entries).
+__global__ void laswp_block_map_kernel(const int* __restrict__ tr, int i0, int i1, int m, int* __restrict__ map)
+{
+  extern __shared__ int src_of[];          // [m - i0]: source row now at row i0 + r
+  __shared__ int s_tr[128];
+  __shared__ int cnt;
+  const int span = m - i0;
+  for (int r = threadIdx.x; r < span; r += blockDim.x) src_of[r] = i0 + r;
+  for (int i = threadIdx.x; i < i1 - i0; i += blockDim.x) s_tr[i] = tr[i0 + i];
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < i1 - i0; ++i) {
+      const int p = s_tr[i] - i0;          // rows >= i0 + i
+      if (p > i && p < span) {
+        const int t = src_of[i];
+        src_of[i] = src_of[p];
+        src_of[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < span; r += blockDim.x) {
+    const int src = src_of[r];
+    if (src != i0 + r) {
+      const int u = atomicAdd(&cnt, 1);
+      if (u < 256) {                       // 128 interchanges move at most 256 rows
+        map[1 + u] = i0 + r;
+        map[257 + u] = src;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) map[0] = min(cnt, 256);
+}
+
+template <typename T>
+int laswp_block_device(cudaStream_t s, T* A, int64_t lda, int m, const int* tr, int i0, int i1, int c0, int c1,
+                       int c2, int c3, DevBuf& map)
+{
+  const int nc = (c1 - c0) + (c3 - c2);
+  if (nc <= 0 || i1 <= i0) return GBS_SUCCESS;
+  const size_t smem = sizeof(int) * (size_t)(m - i0);
+  if (i1 - i0 > 128 || smem > kBlockMapSmemMax)
+    return laswp_gather_device<T>(s, A, lda, tr, i0, i1, c0, c1, c2, c3, map);
+  static const cudaError_t attr = cudaFuncSetAttribute(laswp_block_map_kernel,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)kBlockMapSmemMax);
+  GBS_CUDA_TRY(attr);
+  GBS_TRY(map.reserve(sizeof(int) * kLaswpMapInts));
+  PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * 2 * (i1 - i0));
+  laswp_block_map_kernel<<<1, 1024, smem, s>>>(tr, i0, i1, m, map.as<int>());
+  count_launch();
+  const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
+  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map.as<int>(), c0, c1, c2, c3);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
 template <typename T>
 int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0, int i1, int c0, int c1, int c2,
                         int c3, DevBuf& map)
@@ -785,7 +847,9 @@ double rcond_from_estimate(int64_t n, double matrix_norm, double inv_norm, bool 
                                   int64_t, T*, int64_t);                                                       \
   template int trsm_lunit_wide<T>(cudaStream_t, int, int, const T*, int64_t, T*, int64_t);                     \
   template int laswp_gather_device<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int, int, int, DevBuf&); \
-  template int laswp_map_apply<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int);
+  template int laswp_map_apply<T>(cudaStream_t, T*, int64_t, const int*, int, int, int, int);                 \
+  template int laswp_block_device<T>(cudaStream_t, T*, int64_t, int, const int*, int, int, int, int, int, int,  \
+                                     DevBuf&);
 
 GBS_INSTANTIATE(double)
 GBS_INSTANTIATE(float)

@@ -92,6 +92,8 @@ constexpr int kPanelNB = 32;   // columns factored per panel launch
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
                  DeviceStatus* st, const int** map_out = nullptr, int trsm_cols = 0, bool* trsm_done = nullptr);
+// CTAs of the cluster panel_factor launches for a panel of m rows (one per SM).
+int panel_cluster_ctas(int m);
 
 constexpr int kLaswpMapInts = 520;     // count, 256 target rows, 256 source rows (+ pad)
 
@@ -122,7 +124,9 @@ template <typename T>
 int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, int lower, int trans, int unit,
                      T* B, int64_t ldb, SolveWork& w, const T* dinv = nullptr);
 
-// Block height of tri_solve_device's persistent kernel (its dinv blocks are NB x NB).
+// Block height of tri_solve_device's persistent kernel (its dinv blocks are
+// NB x NB).  A block step costs a fixed flag-to-flag latency plus work that
+// grows with NB^2: FP32 64-row blocks beat both 32 and 128 at n = 8192.
 template <typename T>
 constexpr int tri_solve_nb() { return sizeof(T) == 8 ? 32 : 64; }
 
@@ -190,5 +194,12 @@ int trsm_lunit_wide(cudaStream_t s, int kb, int ncols, const T* L, int64_t ldl, 
 template <typename T>
 int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0, int i1, int c0, int c1, int c2,
                         int c3, DevBuf& map);
+// The same for the interchanges of one outer block (at most 128, rows in
+// [i0, m)): the row map is built in shared memory in constant time per
+// interchange (falls back to laswp_gather_device when [i0, m) is too tall).
+constexpr size_t kBlockMapSmemMax = 160 * 1024;
+template <typename T>
+int laswp_block_device(cudaStream_t s, T* A, int64_t lda, int m, const int* tr, int i0, int i1, int c0, int c1,
+                       int c2, int c3, DevBuf& map);
 
 }  // namespace gbs

@@ -13,6 +13,7 @@ static std::atomic<int> g_enabled{0};
 
 struct Rec {
   cudaEvent_t b, e;
+  cudaStream_t stream;
   int phase;
   double flops, bytes;
   bool closed;
@@ -45,6 +46,7 @@ void prof_begin(cudaStream_t s, int phase)
   r.b = take_event();
   r.e = take_event();
   r.phase = phase;
+  r.stream = s;
   r.flops = r.bytes = 0;
   r.closed = false;
   cudaEventRecord(r.b, s);
@@ -88,6 +90,32 @@ extern "C" int gbs_profile_reset(void)
   }
   g_recs.clear();
   return GBS_SUCCESS;
+}
+
+extern "C" int gbs_profile_timeline(int* phase, int* stream, double* start_ms, double* end_ms, int cap)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  std::vector<cudaStream_t> seen;
+  int cnt = 0;
+  for (auto& r : g_recs) {
+    if (!r.closed) continue;
+    if (cudaEventSynchronize(r.e) != cudaSuccess) return -(100 + GBS_CUDA_ERROR);
+    if (cnt < cap) {
+      float t0 = 0, t1 = 0;
+      if (cudaEventElapsedTime(&t0, g_recs[0].b, r.b) != cudaSuccess ||
+          cudaEventElapsedTime(&t1, g_recs[0].b, r.e) != cudaSuccess)
+        return -(100 + GBS_CUDA_ERROR);
+      int si = 0;
+      while (si < (int)seen.size() && seen[si] != r.stream) ++si;
+      if (si == (int)seen.size()) seen.push_back(r.stream);
+      if (phase) phase[cnt] = r.phase;
+      if (stream) stream[cnt] = si;
+      if (start_ms) start_ms[cnt] = t0;
+      if (end_ms) end_ms[cnt] = t1;
+    }
+    ++cnt;
+  }
+  return cnt;
 }
 
 extern "C" int gbs_profile_collect(int phase, double* ms_total, int64_t* launches, double* flops, double* bytes)

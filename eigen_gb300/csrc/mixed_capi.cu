@@ -37,6 +37,7 @@ extern "C" void gbs_refine_options_default(gbs_refine_options* o)
   o->gmres_restart = d.gmres_restart;
   o->gmres_tol = d.gmres_tol;
   o->shift_factor = d.shift_factor;
+  o->lookahead = d.lookahead;
 }
 
 static int to_options(const gbs_refine_options* o, MixedOptions* m)
@@ -50,6 +51,7 @@ static int to_options(const gbs_refine_options* o, MixedOptions* m)
     d.gmres_restart = o->gmres_restart;
     d.gmres_tol = o->gmres_tol;
     d.shift_factor = o->shift_factor;
+    d.lookahead = o->lookahead;
   }
   if (d.tier < GBS_TIER_FP64 || d.tier > GBS_TIER_FP16 || d.refine < GBS_REFINE_AUTO || d.refine > GBS_REFINE_GMRES ||
       d.max_iter < 0 || d.gmres_restart < 1 || d.gmres_restart > 200 || !(d.tol >= 0) || !(d.shift_factor >= 0)) {

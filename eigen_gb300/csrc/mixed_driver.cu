@@ -7,7 +7,9 @@
 //                at a time by the panel kernel; the outer U12 = L11^-1 A12 as
 //                A12 - (I - L11^-1) A12 on tensor cores (explicit inverse of
 //                the unit-lower diagonal block); inner and outer trailing
-//                updates A22 -= A21 A12 on tensor cores
+//                updates A22 -= A21 A12 on tensor cores; with look-ahead the
+//                panels of block k+1 run on a second stream during block k's
+//                wide trailing update
 //   mixed_potrf  D A D + sigma I = L L^T, D = diag(A)^-1/2 (unit diagonal, so
 //                FP16 cannot overflow), the reference's block size; diagonal
 //                blocks and TRSM on FP32 cores, SYRK on tensor cores
@@ -282,12 +284,41 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
 }
 
 // ------------------------------------------------------------------ workspace pool
+// Second stream of the look-ahead LU: the panels of block k+1 run on it while
+// the caller's stream applies block k's wide trailing update.  It has the
+// highest stream priority, so that when both become ready the panel's cluster
+// is placed before the update's persistent CTAs take the SMs.
+struct Lookahead {
+  cudaStream_t side = nullptr;
+  cudaEvent_t ready = nullptr, panels = nullptr;
+  TcWorkspace tc;
+  DevBuf map;
+  int init()
+  {
+    if (!side) {
+      int least = 0, greatest = 0;
+      GBS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      GBS_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, greatest));
+    }
+    if (!ready) GBS_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    if (!panels) GBS_CUDA_TRY(cudaEventCreateWithFlags(&panels, cudaEventDisableTiming));
+    return GBS_SUCCESS;
+  }
+  ~Lookahead()
+  {
+    if (ready) cudaEventDestroy(ready);
+    if (panels) cudaEventDestroy(panels);
+    if (side) cudaStreamDestroy(side);
+  }
+};
+
 struct MixedWork {
   cudaStream_t stream = nullptr;
   DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv,
       dinv;
   SolveWork sw;
   TcWorkspace tc;
+  Lookahead la;
   HostBuf hstats;
 };
 
@@ -328,66 +359,91 @@ constexpr int kMixedNB = 128;
 constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 // M = I - L^-1 for the lower nb x nb block L (nb <= kMixedNB, ld; unit != 0:
-// unit diagonal, not read), M column-major with ld kMixedNB.  Blocked by 32:
-// the four diagonal blocks are inverted at once (row-by-row substitution on
-// the identity, four threads per column), then block row i of X = L^-1
-// follows from X(i,j) = -X(i,i) sum_{j <= k < i} L(i,k) X(k,j), one block row
-// at a time.  One CTA of 4 kMixedNB threads; rows and columns beyond nb are
-// the identity.
+// unit diagonal, not read), M column-major with ld kMixedNB.  Recursive
+// doubling over 32 x 32 diagonal blocks of X = L^-1:
+//   1. each diagonal block inverted by one warp, lane j holding column j in
+//      registers (substitution on the identity, no barriers);
+//   2. the 64 x 64 halves: X(b, a) = -X(b, b) (L(b, a) X(a, a)) for the block
+//      pairs (0, 1) and (2, 3);
+//   3. the whole block: the same with the 64 x 64 halves.
+// The products run on register tiles from shared memory.  One CTA of
+// 4 kMixedNB threads; rows and columns beyond nb are the identity.
 constexpr int kInvLd = kMixedNB + 1;
 constexpr size_t kInvSmem = sizeof(float) * (2 * kMixedNB * kInvLd + 32 * kInvLd + 4 * kMixedNB);
+static_assert(kMixedNB == 128, "the inverse is written for 128 x 128 blocks");
+
+// C(r0 + i, c) = sign * sum_{k < K} A(r0 + i, k) B(k, c) for i < ROWS: A, B, C
+// row-major sub-blocks in shared memory (leading dimensions lda, ldb, ldc); the
+// lanes of a warp take consecutive columns c, so B and C accesses are
+// conflict-free and A's are broadcasts.
+template <int ROWS, int K>
+__device__ __forceinline__ void smem_tile_product(const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                                                  int r0, int c, float sign)
+{
+  float acc[ROWS];
+#pragma unroll
+  for (int i = 0; i < ROWS; ++i) acc[i] = 0.f;
+#pragma unroll 8
+  for (int k = 0; k < K; ++k) {
+    const float bv = B[k * ldb + c];
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) acc[i] = fmaf(A[(r0 + i) * lda + k], bv, acc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < ROWS; ++i) C[(r0 + i) * ldc + c] = sign * acc[i];
+}
 
 // X = L^-1 of the lower nb x nb block (upper != 0: of U^T for the upper block
 // U at L, i.e. X = U^-T) in shared memory; see unit_lower_inverse_kernel.
 __device__ void tri_inverse_smem(const float* __restrict__ L, int64_t ld, int nb, int unit, int upper, float* sm)
 {
-  float(*Ls)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm);
-  float(*X)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
-  float(*Tb)[kInvLd] = reinterpret_cast<float(*)[kInvLd]>(sm + 2 * kMixedNB * kInvLd);   // [32][..]
-  float* red = sm + 2 * kMixedNB * kInvLd + 32 * kInvLd;                                  // [4 kMixedNB]
-  const int tid = threadIdx.x;
+  constexpr int LD = kInvLd;
+  float* Ls = sm;                                   // [128][LD]
+  float* X = sm + kMixedNB * LD;                    // [128][LD]
+  float* T = sm + 2 * kMixedNB * LD;                // product scratch, up to [64][65]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int e = tid; e < kMixedNB * kMixedNB; e += blockDim.x) {
     const int r = e % kMixedNB, c = e / kMixedNB;
     const bool in = r < nb && c < nb && r >= c && (r != c || !unit);
-    Ls[r][c] = in ? (upper ? L[(int64_t)r * ld + c] : L[(int64_t)c * ld + r]) : (r == c ? 1.f : 0.f);
-    X[r][c] = 0.f;
+    Ls[r * LD + c] = in ? (upper ? L[(int64_t)r * ld + c] : L[(int64_t)c * ld + r]) : (r == c ? 1.f : 0.f);
   }
   __syncthreads();
-  // diagonal 32 x 32 blocks: thread = (block b, column j, quarter q)
-  {
-    const int b = tid / 128, loc = tid % 128, j = loc % 32, q = loc / 32;
-    const int o = 32 * b;
+  // 1. diagonal blocks: x[i] = X(o + i, o + lane); x[k] = 0 for k < lane, so
+  //    the sums may run over every k < i
+  if (warp < 4) {
+    const int o = 32 * warp;
+    float x[32];
+#pragma unroll
     for (int i = 0; i < 32; ++i) {
-      float s = 0.f;
-      for (int k = j + q; k < i; k += 4) s = fmaf(Ls[o + i][o + k], X[o + k][o + j], s);
-      red[tid] = s;
-      __syncthreads();
-      if (q == 0) {
-        const float t = (red[b * 128 + j] + red[b * 128 + 32 + j]) + (red[b * 128 + 64 + j] + red[b * 128 + 96 + j]);
-        X[o + i][o + j] = (i == j ? 1.f : (i > j ? -t : 0.f)) / Ls[o + i][o + i];
-      }
-      __syncthreads();
+      float acc = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+      for (int k = 0; k < i; ++k) acc = fmaf(-Ls[(o + i) * LD + o + k], x[k], acc);
+      x[i] = acc / Ls[(o + i) * LD + o + i];
     }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) X[(o + i) * LD + o + lane] = x[i];
+    for (int i = 0; i < 32; ++i)                     // the blocks right of the diagonal are zero
+      for (int cb = o + 32; cb < kMixedNB; cb += 32) X[(o + i) * LD + cb + lane] = 0.f;
   }
-  // off-diagonal blocks, block row by block row
-  for (int bi = 1; bi < kMixedNB / 32; ++bi) {
-    const int oi = 32 * bi;
-    // Tb(:, 32 bj + c) = sum_{bj <= bk < bi} L(bi, bk) X(bk, bj)
-    for (int e = tid; e < 32 * 32 * bi; e += blockDim.x) {
-      const int r = e % 32, cc = e / 32, bj = cc / 32, c = cc % 32;
-      float s = 0.f;
-      for (int k = 32 * bj; k < oi; ++k) s = fmaf(Ls[oi + r][k], X[k][32 * bj + c], s);
-      Tb[r][cc] = s;
-    }
+  __syncthreads();
+  // 2. block pairs p = 0, 1 (a = 64 p, b = a + 32): T = L(b, a) X(a, a), then
+  //    X(b, a) = -X(b, b) T; thread: column lane, rows 4 g .. 4 g + 3
+  const int p = tid >> 8, g = (tid >> 5) & 7;
+  {
+    const int oa = 64 * p, ob = oa + 32;
+    float* Tp = T + p * 32 * 33;
+    smem_tile_product<4, 32>(Ls + ob * LD + oa, LD, X + oa * LD + oa, LD, Tp, 33, 4 * g, lane, 1.f);
     __syncthreads();
-    // X(bi, bj) = -X(bi, bi) Tb
-    for (int e = tid; e < 32 * 32 * bi; e += blockDim.x) {
-      const int r = e % 32, cc = e / 32;
-      float s = 0.f;
-      for (int k = 0; k <= r; ++k) s = fmaf(X[oi + r][oi + k], Tb[k][cc], s);
-      X[oi + r][cc] = -s;
-    }
+    smem_tile_product<4, 32>(X + ob * LD + ob, LD, Tp, 33, X + ob * LD + oa, LD, 4 * g, lane, -1.f);
+  }
+  __syncthreads();
+  // 3. halves (A = 0..63, B = 64..127): T = L(B, A) X(A, A), X(B, A) = -X(B, B) T;
+  //    thread: column tid % 64, rows 8 (tid / 64) .. + 7
+  {
+    const int c = tid & 63, r0 = 8 * (tid >> 6);
+    smem_tile_product<8, 64>(Ls + 64 * LD, LD, X, LD, T, 65, r0, c, 1.f);
     __syncthreads();
+    smem_tile_product<8, 64>(X + 64 * LD + 64, LD, T, 65, X + 64 * LD, LD, r0, c, -1.f);
   }
   __syncthreads();
 }
@@ -426,51 +482,127 @@ diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int n
   }
 }
 
-int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
-                TcWorkspace& tcw, SolveWork& sw, DevBuf& map, DevBuf& minv)
+// Panels of the outer block [k, k+kb): each 32-column panel, its row
+// interchanges and the block-internal update of the block's columns right of
+// it.  defer: the interchanges are applied inside the block only, and the
+// caller applies the whole block's interchanges to the other columns later
+// (row interchanges commute with the row-wise trailing updates in between).
+static int block_panels(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
+                        int kind, TcWorkspace& tcw, DevBuf& map, int k, int kb, bool defer)
 {
-  (void)sw;
+  const int lo = defer ? k : 0, hi = defer ? k + kb : n;
+  for (int j = k; j < k + kb; j += kPanelNB) {
+    const int jb = std::min(kPanelNB, k + kb - j);
+    float* Ajj = A + (int64_t)j * lda + j;
+    const int rest = k + kb - (j + jb);
+    const int* pmap = nullptr;
+    bool fused = false;       // interchanges + U12 of the block's columns right of the panel done in the panel
+    GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap, rest, &fused));
+    if (pmap && fused) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, lo, j, k + kb, hi));
+    else if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, lo, j, j + jb, hi));
+    else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, lo, j, j + jb, hi, map));
+    if (rest > 0) {
+      float* A12 = A + (int64_t)(j + jb) * lda + j;
+      if (!fused) {
+        PhaseScope ps(s, PH_TRSM_LU, (double)jb * jb * rest, 8.0 * jb * rest);
+        trsm_lunit_kernel<float, kPanelNB><<<cdiv(rest, 128), 128, 0, s>>>(Ajj, lda, jb, A12, lda, rest);
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
+      const int rows = n - (j + jb);
+      if (rows > 0)
+        GBS_TRY(tc_gemm_sub(s, kind, rows, rest, jb, Ajj + jb, 1, lda, A12, 1, lda, A12 + jb, lda, 0, st, tcw));
+    }
+  }
+  return GBS_SUCCESS;
+}
+
+// I - L11^-1 of the block [k, k+kb) into minv.
+static int block_inverse(cudaStream_t s, const float* A, int64_t lda, int k, int kb, float* minv)
+{
+  PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * kb / 3.0, sizeof(float) * 2.0 * kb * kb);
+  unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(A + (int64_t)k * lda + k, lda, kb, minv, 1);
+  GBS_CUDA_TRY(cudaGetLastError());
+  return GBS_SUCCESS;
+}
+
+// Trailing update of block [k, k+kb) on the columns [c0, c1):
+// U12 = A12 - (I - L11^-1) A12 (the GEMM packs its operands first, so C may
+// alias B), then A22 -= L21 U12.  max_ctas > 0 caps the GEMMs' persistent grid.
+static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int kb, int c0, int c1,
+                        const float* minv, DeviceStatus* st, int kind, TcWorkspace& tcw, int max_ctas)
+{
+  const int nc = c1 - c0, rows = n - k - kb;
+  if (nc <= 0) return GBS_SUCCESS;
+  float* Akk = A + (int64_t)k * lda + k;
+  float* A12 = A + (int64_t)c0 * lda + k;
+  GBS_TRY(tc_gemm_sub(s, kind, kb, nc, kb, minv, 1, kMixedNB, A12, 1, lda, A12, lda, 0, st, tcw, max_ctas));
+  GBS_TRY(tc_gemm_sub(s, kind, rows, nc, kb, Akk + kb, 1, lda, A12, 1, lda, A12 + kb, lda, 0, st, tcw, max_ctas));
+  return GBS_SUCCESS;
+}
+
+// The look-ahead schedule (la != null).  Caller's stream s, side stream ss:
+//   ss: panels of block 0
+//   for each block k:
+//     s:  wait for block k's panels; its interchanges on block k+1's
+//         columns; I - L11^-1; update of block k+1's columns (narrow)
+//     ss: wait for the narrow update; panels of block k+1
+//     s:  block k's interchanges on the other columns; update of the columns
+//         right of block k+1 (wide), on the SMs the panels leave free
+// Every element sees the same operations in the same order as in the plain
+// schedule, so both give identical factors and interchanges.
+static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
+                           int kind, TcWorkspace& tcw, DevBuf& map, float* minv, Lookahead& la)
+{
+  cudaStream_t ss = la.side;
+  GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
+  GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, 0, std::min(kMixedNB, n), true));
+  for (int k = 0; k < n; k += kMixedNB) {
+    const int kb = std::min(kMixedNB, n - k);
+    const int nr = n - k - kb;
+    GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.panels, 0));
+    if (nr == 0) {
+      GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, 0, k, k + kb, k + kb, map));
+      break;
+    }
+    const int nb1 = std::min(kMixedNB, nr), c1 = k + kb + nb1;
+    // the interchanges on block k+1's columns gate its panels; the left and
+    // wide columns get them (same map) while those panels run
+    GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, map));
+    GBS_TRY(block_inverse(s, A, lda, k, kb, minv));
+    GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, c1, minv, st, kind, tcw, 0));
+    GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
+    GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, k + kb, nb1, true));
+    GBS_TRY(laswp_map_apply<float>(s, A, lda, map.as<int>(), 0, k, c1, n));
+    // the panel's cluster and the panels' small kernels keep 2 clusters' worth of SMs
+    const int keep = std::min(2 * panel_cluster_ctas(nr), device_sm_count() / 2);
+    GBS_TRY(block_update(s, n, A, lda, k, kb, c1, n, minv, st, kind, tcw, device_sm_count() - keep));
+  }
+  return GBS_SUCCESS;
+}
+
+int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
+                TcWorkspace& tcw, DevBuf& map, DevBuf& minv, Lookahead* la)
+{
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kInvSmem));
   GBS_CUDA_TRY(cudaFuncSetAttribute(diag_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kInvSmem));
+  if (la && n > kMixedNB) {
+    GBS_TRY(la->init());
+    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, map, minv.as<float>(), *la);
+    if (rc != GBS_SUCCESS) cudaStreamSynchronize(la->side);   // nothing of the side stream outlives the call
+    return rc;
+  }
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
-    for (int j = k; j < k + kb; j += kPanelNB) {
-      const int jb = std::min(kPanelNB, k + kb - j);
-      float* Ajj = A + (int64_t)j * lda + j;
-      const int rest = k + kb - (j + jb);
-      const int* pmap = nullptr;
-      bool fused = false;       // interchanges + U12 of the block's columns right of the panel done in the panel
-      GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap, rest, &fused));
-      if (pmap && fused) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, k + kb, n));
-      else if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, 0, j, j + jb, n));
-      else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, 0, j, j + jb, n, map));
-      if (rest > 0) {
-        float* A12 = A + (int64_t)(j + jb) * lda + j;
-        if (!fused) {
-          PhaseScope ps(s, PH_TRSM_LU, (double)jb * jb * rest, 8.0 * jb * rest);
-          trsm_lunit_kernel<float, kPanelNB><<<cdiv(rest, 128), 128, 0, s>>>(Ajj, lda, jb, A12, lda, rest);
-          GBS_CUDA_TRY(cudaGetLastError());
-        }
-        const int rows = n - (j + jb);
-        if (rows > 0)
-          GBS_TRY(tc_gemm_sub(s, kind, rows, rest, jb, Ajj + jb, 1, lda, A12, 1, lda, A12 + jb, lda, 0, st, tcw));
-      }
-    }
-    const int nr = n - k - kb;
-    if (nr > 0) {
-      float* Akk = A + (int64_t)k * lda + k;
-      float* A12 = A + (int64_t)(k + kb) * lda + k;
-      {
-        PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * kb / 3.0, sizeof(float) * 2.0 * kb * kb);
-        unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, kb, minv.as<float>(), 1);
-        GBS_CUDA_TRY(cudaGetLastError());
-      }
-      // U12 = A12 - (I - L11^-1) A12 (the GEMM packs its operands first, so C may alias B)
-      GBS_TRY(tc_gemm_sub(s, kind, kb, nr, kb, minv.as<float>(), 1, kMixedNB, A12, 1, lda, A12, lda, 0, st, tcw));
-      GBS_TRY(tc_gemm_sub(s, kind, nr, nr, kb, Akk + kb, 1, lda, A12, 1, lda, A12 + kb, lda, 0, st, tcw));
+    GBS_TRY(block_panels(s, n, A, lda, tr, st, scratch, kind, tcw, map, k, kb, false));
+    if (n - k - kb > 0) {
+      GBS_TRY(block_inverse(s, A, lda, k, kb, minv.as<float>()));
+      GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, n, minv.as<float>(), st, kind, tcw, 0));
     }
   }
   return GBS_SUCCESS;
@@ -879,8 +1011,8 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
           A, lda, w.a32.as<float>(), n, n, n);
       GBS_CUDA_TRY(cudaGetLastError());
     }
-    GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.sw,
-                        w.map, w.minv));
+    GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.map,
+                        w.minv, opt.lookahead ? &w.la : nullptr));
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {

@@ -5,4 +5,11 @@ namespace gbs {
 template int panel_factor<float>(cudaStream_t, float*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
                                   const int**, int, bool*);
 template int panel_preload<float>();
+
+int panel_cluster_ctas(int m)
+{
+  int c = 1;
+  while (c * kClusterPanelThreads < m && c < kMaxPanelCluster) c *= 2;
+  return c;
+}
 }  // namespace gbs

@@ -458,7 +458,7 @@ int make_tmap(CUtensorMap* tm, const void* base, int esize, int64_t rows, int64_
 
 int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs,
                 const float* B, int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int lower, DeviceStatus* st,
-                TcWorkspace& ws)
+                TcWorkspace& ws, int max_ctas)
 {
   if (M <= 0 || N <= 0 || K <= 0) return GBS_SUCCESS;
   if (kind < TC_BF16 || kind > TC_TF32X3) return GBS_INVALID_ARGUMENT;
@@ -502,7 +502,9 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   p.err = &st->timeout;
   p.limit_ns = wait_limit_ns();
   const int tiles = p.tiles_m * p.tiles_n;
-  const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
+  // persistent CTAs, one per SM; max_ctas > 0 leaves the other SMs to work on another stream
+  const int ctas = max_ctas > 0 ? std::min(max_ctas, device_sm_count()) : device_sm_count();
+  const int grid = tiles < ctas ? tiles : ctas;
   // algorithmic flops of the update (a 3xTF32 update issues three such products on the tensor cores)
   const double flops = 2.0 * M * (double)N * K * (lower ? 0.5 : 1.0);
   const double bytes = 8.0 * M * (double)N * (lower ? 0.5 : 1.0) + (double)(M + N) * Kp * esize;

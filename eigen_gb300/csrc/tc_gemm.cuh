@@ -32,6 +32,6 @@ struct TcWorkspace {
 // A(i,k) = A[i*a_rs + k*a_cs], B(k,j) = B[k*b_rs + j*b_cs].
 int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs,
                 const float* B, int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int lower, DeviceStatus* st,
-                TcWorkspace& ws);
+                TcWorkspace& ws, int max_ctas = 0);
 
 }  // namespace gbs

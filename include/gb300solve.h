@@ -354,6 +354,11 @@ typedef struct gbs_refine_options {
   int gmres_restart;      /* Krylov vectors per GMRES-IR correction (default 40) */
   double gmres_tol;       /* relative target of one GMRES correction (default 1e-10) */
   double shift_factor;    /* SPD tiers: diagonal shift = shift_factor * u of the tier (default 4) */
+  int lookahead;          /* general A: 1 factors each 128-column block's panels on a second,
+                             high-priority stream while the previous block's wide trailing update runs;
+                             0 (default) runs every step on the caller's stream.  Same results either
+                             way; on GB300 the panel's 16-CTA cluster seldom finds a free GPC while
+                             the update runs, so the overlap is small and 0 is as fast. */
 } gbs_refine_options;
 
 typedef struct gbs_refine_info {
@@ -523,6 +528,12 @@ int gbs_profile_reset(void);
 /* Sums, over the phase's recorded launches, device time (ms), launch count,
  * algorithmic flops and bytes.  Waits for the recorded events. */
 int gbs_profile_collect(int phase, double* ms_total, int64_t* launches, double* flops, double* bytes);
+/* The recorded launches in order of issue (a timeline, e.g. to see which
+ * phases of two streams overlap): phase, stream (0, 1, ... in order of first
+ * use), start and end in ms from the first record's start.  Writes at most cap
+ * entries (any pointer may be NULL) and returns the number of records, or
+ * -(100 + gbs_status) on an error.  Waits for the recorded events. */
+int gbs_profile_timeline(int* phase, int* stream, double* start_ms, double* end_ms, int cap);
 
 #ifdef __cplusplus
 }

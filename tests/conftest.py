@@ -19,6 +19,12 @@ def pytest_configure(config):
 
 
 _PARITY: list[tuple[str, str, float, float]] = []
+_NOTES: list[tuple[str, str]] = []
+
+
+def record_note(what: str, text: str) -> None:
+    """A measurement a test made (times, counts), printed in the terminal summary."""
+    _NOTES.append((what, text))
 
 
 def record_parity(case: str, what: str, value: float, bound: float) -> None:
@@ -28,6 +34,10 @@ def record_parity(case: str, what: str, value: float, bound: float) -> None:
 
 
 def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    if _NOTES:
+        terminalreporter.section("measurements")
+        for what, text in _NOTES:
+            terminalreporter.write_line(f"{what}: {text}")
     if not _PARITY:
         return
     worst: dict[str, tuple[str, float, float]] = {}

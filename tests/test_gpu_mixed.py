@@ -146,3 +146,20 @@ def test_mixed_device_orders_after_pending_default_stream_work(spd):
         assert torch.equal(X, X2)
         a = np.asfortranarray(A.cpu().numpy())
         assert O.backward_error(a, X.cpu().numpy(), B.cpu().numpy()) <= BAR
+
+
+@pytest.mark.parametrize("tier", ["tf32x3", "bf16"])
+@pytest.mark.parametrize("n", [300, 2048, 4100])
+def test_lookahead_gives_identical_results(tier, n):
+    """The look-ahead schedule (block k+1's panels on a second stream during
+    block k's wide update) performs every element's operations in the same
+    order as the single-stream schedule: identical solutions and iterations."""
+    a = O.gauss(500 + n, n, n)
+    b = O.gauss(600 + n, n, 2)
+    x1, i1 = solve_mixed(a, b, tier=tier, lookahead=True)
+    x1b, _ = solve_mixed(a, b, tier=tier, lookahead=True)
+    assert np.array_equal(x1, x1b), "the look-ahead solve is not deterministic"
+    x0, i0 = solve_mixed(a, b, tier=tier, lookahead=False)
+    assert np.array_equal(x1, x0)
+    assert i1["iterations"] == i0["iterations"] and i1["fell_back"] == i0["fell_back"]
+    assert O.backward_error(a, x1, b) <= BAR

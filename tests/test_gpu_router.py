@@ -213,3 +213,39 @@ def test_pretrained_router_routes_fresh_systems():
     routed = stats["ir_routed"] + stats["gmres_routed"]
     assert routed > 0.3 * mt.count
     assert stats["ir_failed"] + stats["gmres_failed"] <= 0.05 * routed
+
+
+def test_router_gain_over_the_cascade():
+    """What the shipped network gains over the same solver chain without it,
+    on the same seeded systems (n 32..512, log10 kappa uniform in 1..12): the
+    try-lowest cascade (every item FP32 + refinement, GMRES-IR on the items it
+    leaves, FP64 on the rest) against route-and-solve.  The router must make
+    fewer failed refinement attempts and fewer factorizations, and take less
+    wall time; both must meet the backward-error bound on every item."""
+    from tests.conftest import record_note
+    mb, A, B, logk = R.generate(1500, seed=31)
+    router = R.Router.pretrained()
+    for _ in range(2):                                   # warm-up: kernels, workspaces, autotune entries
+        R.solve_cascade(mb, A, B)
+        R.route_and_solve(router, mb, A, B)
+    tc, tr = [], []
+    for _ in range(3):
+        (Xc, sc), t = R.timed(lambda: R.solve_cascade(mb, A, B))
+        tc.append(t)
+        (Xr, sr), t = R.timed(lambda: R.route_and_solve(router, mb, A, B))
+        tr.append(t)
+    tc, tr = float(np.median(tc)), float(np.median(tr))
+    n = mb.count
+    casc_failed = (n - sc["ir_converged"]) + (sc["gmres_attempts"] - sc["gmres_converged"])
+    casc_factor = n + sc["fp64_solves"]                  # one FP32 LU per item (GMRES reuses it) + FP64 LUs
+    rout_failed = sr["ir_failed"] + sr["gmres_failed"]
+    rout_factor = sr["ir_routed"] + sr["gmres_routed"] + sr["fp64_solves"]
+    record_note("router vs cascade, 1500 systems",
+                f"failed refinement attempts {rout_failed} vs {casc_failed}; factorizations {rout_factor} vs "
+                f"{casc_factor}; wall {tr * 1e3:.1f} ms vs {tc * 1e3:.1f} ms ({tc / tr:.2f}x)")
+    for X in (Xc, Xr):
+        errs = R.backward_errors(mb, A, X, B)
+        assert (errs <= 1e-13).all(), float(errs.max())
+    assert rout_failed < casc_failed
+    assert rout_factor < casc_factor
+    assert tr < tc, (tr, tc)
