@@ -127,6 +127,7 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_tc_gemm_sub": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_int, c_vp]),
     # mixed precision
     "gbs_refine_options_default": (None, [c_vp]),
+    "gbs_dgeresid_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, c_vp]),
     "gbs_dgesv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),
     "gbs_dgesv_mixed": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp]),
     "gbs_dposv_mixed_device": (c_int, [c_int, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),

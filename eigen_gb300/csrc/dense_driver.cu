@@ -582,10 +582,7 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
   const int forward = (lower != 0) != (trans != 0);
   const int nblk = ceil_div(n, NB);
   GBS_TRY(w.flags.reserve(sizeof(int) * (size_t)(nblk + 2)));
-  if (!w.err.p) {
-    GBS_TRY(w.err.reserve(16));
-    GBS_CUDA_TRY(cudaMemsetAsync(w.err.p, 0, 16, s));
-  }
+  GBS_TRY(solve_err_slot(s, w));
   const uint64_t limit = wait_limit_ns();
   const int grid = std::min(nblk, 2 * device_sm_count());
   constexpr size_t smem = trsm_persistent_smem<T, NB, RC>();
@@ -601,6 +598,14 @@ int tri_solve_device(cudaStream_t s, int n, int nrhs, const T* tri, int64_t ld, 
                                                                    dinv, w.err.as<int>(), limit);
     GBS_CUDA_TRY(cudaGetLastError());
   }
+  return GBS_SUCCESS;
+}
+
+int solve_err_slot(cudaStream_t s, SolveWork& w)
+{
+  if (w.err.p) return GBS_SUCCESS;
+  GBS_TRY(w.err.reserve(16));
+  GBS_CUDA_TRY(cudaMemsetAsync(w.err.p, 0, 16, s));
   return GBS_SUCCESS;
 }
 

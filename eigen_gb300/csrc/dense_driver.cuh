@@ -132,6 +132,8 @@ constexpr int tri_solve_nb() { return sizeof(T) == 8 ? 32 : 64; }
 
 // Waits for the stream and reports GBS_TIMEOUT if a solve's wait expired.
 int solve_status(cudaStream_t s, SolveWork& w);
+// Allocates (zeroed) the timeout flag solve_status reads, if not yet there.
+int solve_err_slot(cudaStream_t s, SolveWork& w);
 
 template <typename T>
 int laswp_device(cudaStream_t s, T* B, int64_t ldb, int ncols, const int* dTr, int i0, int i1, int reverse);

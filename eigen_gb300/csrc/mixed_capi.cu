@@ -38,6 +38,7 @@ extern "C" void gbs_refine_options_default(gbs_refine_options* o)
   o->gmres_tol = d.gmres_tol;
   o->shift_factor = d.shift_factor;
   o->lookahead = d.lookahead;
+  o->residual = d.residual;
 }
 
 static int to_options(const gbs_refine_options* o, MixedOptions* m)
@@ -52,9 +53,11 @@ static int to_options(const gbs_refine_options* o, MixedOptions* m)
     d.gmres_tol = o->gmres_tol;
     d.shift_factor = o->shift_factor;
     d.lookahead = o->lookahead;
+    d.residual = o->residual;
   }
   if (d.tier < GBS_TIER_FP64 || d.tier > GBS_TIER_FP16 || d.refine < GBS_REFINE_AUTO || d.refine > GBS_REFINE_GMRES ||
-      d.max_iter < 0 || d.gmres_restart < 1 || d.gmres_restart > 200 || !(d.tol >= 0) || !(d.shift_factor >= 0)) {
+      d.max_iter < 0 || d.gmres_restart < 1 || d.gmres_restart > 200 || !(d.tol >= 0) || !(d.shift_factor >= 0) ||
+      d.residual < GBS_RESID_AUTO || d.residual > GBS_RESID_OZAKI) {
     gbs_set_last_message("invalid gbs_refine_options");
     return GBS_INVALID_ARGUMENT;
   }
@@ -157,4 +160,17 @@ extern "C" int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const 
                                const gbs_refine_options* opt, gbs_refine_info* info)
 {
   return run_host(mixed_llt_solve, n, nrhs, a, lda, b, ldb, x, ldx, opt, info);
+}
+
+extern "C" int gbs_dgeresid_device(int n, int nrhs, const double* d_a, int lda, const double* d_x, int ldx,
+                                   const double* d_b, int ldb, double* d_r, int ldr, int method, void* stream)
+{
+  const int ld_min = n > 1 ? n : 1;
+  if (n < 0 || nrhs < 0 || lda < ld_min || ldx < ld_min || (d_b && ldb < ld_min) || ldr < ld_min ||
+      method < GBS_RESID_AUTO || method > GBS_RESID_OZAKI) {
+    gbs_set_last_message("gbs_dgeresid_device: invalid argument");
+    return GBS_INVALID_ARGUMENT;
+  }
+  GBS_TRY(ensure_device());
+  return residual_device((cudaStream_t)stream, n, nrhs, d_a, lda, d_x, ldx, d_b, ldb, d_r, ldr, method);
 }

@@ -30,6 +30,7 @@
 #include "dense_kernels.cuh"
 #include "gbs_profile.cuh"
 #include "mixed_driver.cuh"
+#include "ozaki.cuh"
 #include "tc_gemm.cuh"
 
 namespace gbs {
@@ -44,6 +45,7 @@ static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 // coalesced over rows.  Partial sums per split are added in split order by
 // residual_reduce (deterministic).
 constexpr int kResRows = 128, kResRC = 16, kResKC = 64;
+constexpr int kOzakiMinN = 1024;      // GBS_RESID_AUTO: tensor-core residuals from this order
 
 template <int RC>
 __global__ void __launch_bounds__(kResRows)
@@ -319,6 +321,8 @@ struct MixedWork {
   SolveWork sw;
   TcWorkspace tc;
   Lookahead la;
+  OzakiMatrix oz;          // A's digit slices when the residuals run on the tensor cores
+  OzakiWork ozw;
   HostBuf hstats;
 };
 
@@ -707,10 +711,23 @@ static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, S
 }
 
 // Y = A X (B == null) or Y = B - A X, FP64 (Y with leading dimension ldy)
+// Slices A for the tensor-core residuals when the options ask for them.
+static int prepare_residual(cudaStream_t s, const Problem& P, int mode, MixedWork& w)
+{
+  w.oz.ready = false;
+  const bool oz = mode == GBS_RESID_OZAKI || (mode == GBS_RESID_AUTO && P.n >= kOzakiMinN);
+  if (!oz) return GBS_SUCCESS;
+  return w.oz.prepare(s, P.n, P.A, P.lda, P.sym);
+}
+
 static int apply_a(cudaStream_t s, const Problem& P, const double* X, int64_t ldx, const double* B, int64_t ldb, double* Y,
                    int64_t ldy, int nrhs, MixedWork& w)
 {
   const int n = P.n;
+  if (w.oz.ready && w.oz.n == n && nrhs <= kResRC) {
+    GBS_TRY(solve_err_slot(s, w.sw));
+    return ozaki_residual(s, w.oz, nrhs, X, ldx, B, ldb, Y, ldy, w.ozw, w.sw.err.as<int>());
+  }
   const int splits = std::max(1, std::min(32, cdiv((int64_t)device_sm_count() * 4, cdiv(n, kResRows))));
   const int kspan = cdiv(cdiv(n, splits), kResKC) * kResKC;
   const int used = cdiv(n, kspan);
@@ -1002,6 +1019,7 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
   Problem P{n, nrhs, A, lda, 0, B, ldb, X, ldx};
   double anorm = 0;
   GBS_TRY(inf_norm(s, P, w, &anorm));
+  GBS_TRY(prepare_residual(s, P, opt.residual, w));
   bool converged = false;
   if (opt.tier != GBS_TIER_FP64) {
     GBS_TRY(reset_status(st, s));
@@ -1066,6 +1084,23 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
   return GBS_SUCCESS;
 }
 
+int residual_device(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* X, int64_t ldx,
+                    const double* B, int64_t ldb, double* R, int64_t ldr, int method)
+{
+  if (n <= 0 || nrhs <= 0) return GBS_SUCCESS;
+  MixedLease lease;
+  if (lease.status != GBS_SUCCESS) return lease.status;
+  MixedWork& w = *lease.w;
+  Problem P{n, nrhs, A, lda, 0, B, ldb, nullptr, 0};
+  GBS_TRY(prepare_residual(s, P, method, w));
+  for (int c0 = 0; c0 < nrhs; c0 += kResRC) {
+    const int nc = std::min(kResRC, nrhs - c0);
+    GBS_TRY(apply_a(s, P, X + (int64_t)c0 * ldx, ldx, B ? B + (int64_t)c0 * ldb : nullptr, ldb, R + (int64_t)c0 * ldr,
+                    ldr, nc, w));
+  }
+  return solve_status(s, w.sw);
+}
+
 // ------------------------------------------------------------------ LLT front end
 int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
                     double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
@@ -1100,6 +1135,7 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
   Problem P{n, nrhs, w.afull.as<double>(), n, 0, B, ldb, X, ldx};
   double anorm = 0;
   GBS_TRY(inf_norm(s, P, w, &anorm));
+  GBS_TRY(prepare_residual(s, P, opt.residual, w));
   bool converged = false;
   int not_spd = 0;
   if (opt.tier != GBS_TIER_FP64) {

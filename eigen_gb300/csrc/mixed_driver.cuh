@@ -17,7 +17,13 @@ struct MixedOptions {
   double gmres_tol = 1e-10;      // relative preconditioned-residual target of one correction
   double shift_factor = 4.0;     // LLT tiers: initial diagonal shift = shift_factor * u_factorization
   int lookahead = 0;             // LU: overlap each block's panels with the previous block's trailing update
+  int residual = GBS_RESID_AUTO; // how the FP64 residuals are computed (gbs_residual_mode)
 };
+
+// R = B - A X (B null: R = A X), FP64-accurate, nrhs columns, on device
+// buffers; method: gbs_residual_mode (AUTO: tensor cores from n = 1024).
+int residual_device(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* X, int64_t ldx,
+                    const double* B, int64_t ldb, double* R, int64_t ldr, int method);
 
 struct MixedResult {
   int tier = GBS_TIER_TF32X3;    // tier that produced the answer (GBS_TIER_FP64 after a fallback)

@@ -24,7 +24,7 @@ REFINE_NAMES = {v: k for k, v in REFINE.items()}
 class RefineOptions(C.Structure):
     _fields_ = [("tier", C.c_int), ("refine", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("gmres_restart", C.c_int), ("gmres_tol", C.c_double), ("shift_factor", C.c_double),
-                ("lookahead", C.c_int)]
+                ("residual", C.c_int), ("lookahead", C.c_int)]
 
 
 class RefineInfo(C.Structure):
@@ -39,8 +39,11 @@ class RefineInfo(C.Structure):
                 "singular": bool(self.singular), "backward_error": self.backward_error, "shift": self.shift}
 
 
+RESIDUAL = {"auto": 0, "fp64": 1, "ozaki": 2}
+
+
 def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=40, gmres_tol=1e-10,
-            shift_factor=4.0, lookahead=False) -> RefineOptions:
+            shift_factor=4.0, lookahead=False, residual="auto") -> RefineOptions:
     o = RefineOptions()
     L.lib().gbs_refine_options_default(C.byref(o))
     o.tier = TIERS[tier] if isinstance(tier, str) else int(tier)
@@ -48,6 +51,7 @@ def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=
     o.tol, o.max_iter, o.gmres_restart, o.gmres_tol, o.shift_factor = tol, max_iter, gmres_restart, gmres_tol, \
         shift_factor
     o.lookahead = int(bool(lookahead))
+    o.residual = RESIDUAL[residual] if isinstance(residual, str) else int(residual)
     return o
 
 

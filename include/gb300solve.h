@@ -345,6 +345,15 @@ typedef enum gbs_tier {
 } gbs_tier;
 
 typedef enum gbs_refine_mode { GBS_REFINE_AUTO = 0, GBS_REFINE_CLASSIC = 1, GBS_REFINE_GMRES = 2 } gbs_refine_mode;
+/* FP64 residuals r = b - A x of the refinement:
+ *  GBS_RESID_FP64:  FP64 fused multiply-adds (the DFMA rate bounds it);
+ *  GBS_RESID_OZAKI: the Ozaki scheme on the bf16 tensor cores -- A and x cut
+ *     into 8 integer digit slices of 7 bits per row / column, every slice
+ *     product exact in FP32 over 1024-long chunks, folded in FP64; as accurate
+ *     as an FP64 GEMV (no rounding beyond 56 bits of each row's and column's
+ *     maximum) at 16 n^2 bytes of device memory for the slices of A;
+ *  GBS_RESID_AUTO:  Ozaki from n = 1024, FP64 below. */
+typedef enum gbs_residual_mode { GBS_RESID_AUTO = 0, GBS_RESID_FP64 = 1, GBS_RESID_OZAKI = 2 } gbs_residual_mode;
 
 typedef struct gbs_refine_options {
   int tier;               /* gbs_tier */
@@ -354,6 +363,7 @@ typedef struct gbs_refine_options {
   int gmres_restart;      /* Krylov vectors per GMRES-IR correction (default 40) */
   double gmres_tol;       /* relative target of one GMRES correction (default 1e-10) */
   double shift_factor;    /* SPD tiers: diagonal shift = shift_factor * u of the tier (default 4) */
+  int residual;           /* gbs_residual_mode of the FP64 residuals (default GBS_RESID_AUTO) */
   int lookahead;          /* general A: 1 factors each 128-column block's panels on a second,
                              high-priority stream while the previous block's wide trailing update runs;
                              0 (default) runs every step on the caller's stream.  Same results either
@@ -373,6 +383,12 @@ typedef struct gbs_refine_info {
 } gbs_refine_info;
 
 void gbs_refine_options_default(gbs_refine_options* opt);
+
+/* R = B - A X (d_b NULL: R = A X) for an n x n FP64 matrix and nrhs columns,
+ * device buffers, with the refinement's residual kernels (method: a
+ * gbs_residual_mode).  Returns when R is final. */
+int gbs_dgeresid_device(int n, int nrhs, const double* d_a, int lda, const double* d_x, int ldx, const double* d_b,
+                        int ldb, double* d_r, int ldr, int method, void* stream);
 
 /* General A (PartialPivLU).  Device buffers, stream-ordered on `stream`
  * (a cudaStream_t; NULL is the legacy default stream, as in every other
