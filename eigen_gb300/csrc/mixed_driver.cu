@@ -314,6 +314,31 @@ struct Lookahead {
   }
 };
 
+// Low-priority stream for work that only the refinement needs (the digit
+// slices of A), so that it runs beside the factorization.
+struct AuxStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  bool pending = false;      // join recorded and not yet waited for
+  int init()
+  {
+    if (!s) {
+      int least = 0, greatest = 0;
+      GBS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      GBS_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least));
+    }
+    if (!fork) GBS_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (!join) GBS_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    return GBS_SUCCESS;
+  }
+  ~AuxStream()
+  {
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
 struct MixedWork {
   cudaStream_t stream = nullptr;
   DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv,
@@ -323,6 +348,7 @@ struct MixedWork {
   Lookahead la;
   OzakiMatrix oz;          // A's digit slices when the residuals run on the tensor cores
   OzakiWork ozw;
+  AuxStream aux;
   HostBuf hstats;
 };
 
@@ -711,20 +737,43 @@ static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, S
 }
 
 // Y = A X (B == null) or Y = B - A X, FP64 (Y with leading dimension ldy)
-// Slices A for the tensor-core residuals when the options ask for them.
+// Slices A for the tensor-core residuals when the options ask for them, on
+// the auxiliary stream (joined by the first residual, and by AuxJoin at the
+// end of the call whatever path it took).
 static int prepare_residual(cudaStream_t s, const Problem& P, int mode, MixedWork& w)
 {
   w.oz.ready = false;
   const bool oz = mode == GBS_RESID_OZAKI || (mode == GBS_RESID_AUTO && P.n >= kOzakiMinN);
-  if (!oz) return GBS_SUCCESS;
-  return w.oz.prepare(s, P.n, P.A, P.lda, P.sym);
+  if (!oz || P.sym) return GBS_SUCCESS;        // the residuals of a lower-stored A stay on FP64 FMA
+  GBS_TRY(w.aux.init());
+  GBS_CUDA_TRY(cudaEventRecord(w.aux.fork, s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(w.aux.s, w.aux.fork, 0));
+  w.aux.pending = true;
+  const int rc = w.oz.prepare(w.aux.s, P.n, P.A, P.lda);
+  GBS_CUDA_TRY(cudaEventRecord(w.aux.join, w.aux.s));
+  return rc;
 }
+
+// Nothing of the auxiliary stream outlives the call that issued it.
+struct AuxJoin {
+  MixedWork& w;
+  explicit AuxJoin(MixedWork& w_) : w(w_) {}
+  ~AuxJoin()
+  {
+    if (w.aux.pending) cudaEventSynchronize(w.aux.join);
+    w.aux.pending = false;
+  }
+};
 
 static int apply_a(cudaStream_t s, const Problem& P, const double* X, int64_t ldx, const double* B, int64_t ldb, double* Y,
                    int64_t ldy, int nrhs, MixedWork& w)
 {
   const int n = P.n;
   if (w.oz.ready && w.oz.n == n && nrhs <= kResRC) {
+    if (w.aux.pending) {
+      GBS_CUDA_TRY(cudaStreamWaitEvent(s, w.aux.join, 0));
+      w.aux.pending = false;
+    }
     GBS_TRY(solve_err_slot(s, w.sw));
     return ozaki_residual(s, w.oz, nrhs, X, ldx, B, ldb, Y, ldy, w.ozw, w.sw.err.as<int>());
   }
@@ -1019,6 +1068,7 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
   Problem P{n, nrhs, A, lda, 0, B, ldb, X, ldx};
   double anorm = 0;
   GBS_TRY(inf_norm(s, P, w, &anorm));
+  AuxJoin aux_join(w);
   GBS_TRY(prepare_residual(s, P, opt.residual, w));
   bool converged = false;
   if (opt.tier != GBS_TIER_FP64) {
@@ -1092,6 +1142,7 @@ int residual_device(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
   if (lease.status != GBS_SUCCESS) return lease.status;
   MixedWork& w = *lease.w;
   Problem P{n, nrhs, A, lda, 0, B, ldb, nullptr, 0};
+  AuxJoin aux_join(w);
   GBS_TRY(prepare_residual(s, P, method, w));
   for (int c0 = 0; c0 < nrhs; c0 += kResRC) {
     const int nc = std::min(kResRC, nrhs - c0);
@@ -1135,6 +1186,7 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
   Problem P{n, nrhs, w.afull.as<double>(), n, 0, B, ldb, X, ldx};
   double anorm = 0;
   GBS_TRY(inf_norm(s, P, w, &anorm));
+  AuxJoin aux_join(w);
   GBS_TRY(prepare_residual(s, P, opt.residual, w));
   bool converged = false;
   int not_spd = 0;

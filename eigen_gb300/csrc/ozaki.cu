@@ -63,52 +63,59 @@ static_assert((int64_t)OZ_CHUNK * 127 * 127 < (1 << 24), "chunk sums must stay e
 
 constexpr unsigned long long kNonFiniteBits = 0x7FF0000000000000ull;
 
-// Exponent e with |v| < 2^e for the largest magnitude v (0 when v = 0).
+// Exponent e with |v| < 2^e for the largest magnitude v (0 when v = 0): the
+// biased exponent field plus one for a normal number, and for a subnormal
+// the position of its highest set mantissa bit.
 __device__ __forceinline__ int bound_exponent(unsigned long long maxbits)
 {
-  const double m = __longlong_as_double((long long)maxbits);
-  if (m == 0.0) return 0;
-  int e = 0;
-  (void)frexp(m, &e);                      // m = f 2^e, 0.5 <= f < 1
-  return e;
+  if (maxbits == 0) return 0;
+  const int ef = (int)(maxbits >> 52);
+  if (ef > 0) return ef - 1022;                          // 1.f x 2^(ef - 1023) < 2^(ef - 1022)
+  return (63 - __clzll(maxbits)) - 1073;                 // highest mantissa bit b: v < 2^(b + 1 - 1074)
+}
+
+// The 56-bit fixed-point magnitude F = trunc(|v| 2^(56 - e)) of a finite v
+// with |v| < 2^e, from v's bits (integer shifts only), and its sign.
+__device__ __forceinline__ unsigned long long fixed56(double v, int e, bool* neg)
+{
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  *neg = (bits >> 63) != 0;
+  const int ef = (int)((bits >> 52) & 0x7FF);
+  const unsigned long long frac = bits & 0xFFFFFFFFFFFFFull;
+  if (ef == 0 && frac == 0) return 0;
+  const unsigned long long m = ef ? (frac | (1ull << 52)) : frac;   // |v| = m 2^(E), E = max(ef, 1) - 1075
+  const int shift = (ef ? ef : 1) - 1075 - e + 56;                  // F = m 2^shift < 2^56: shift <= 55
+  if (shift >= 0) return m << shift;
+  return shift <= -64 ? 0ull : (m >> (-shift));
+}
+
+// Digit i (most significant first) of F: F = sum_i d_i 2^(7 (7 - i)).
+__device__ __forceinline__ __nv_bfloat16 digit_bf16(unsigned long long F, bool neg, int i)
+{
+  const int d = (int)((F >> (OZ_DIGIT * (OZ_SLICES - 1 - i))) & ((1u << OZ_DIGIT) - 1));
+  return __float2bfloat16_rn((float)(neg ? -d : d));    // |d| <= 127: exact
 }
 
 // Row maxima of |A| as bit patterns (for non-negative doubles the bit order is
-// the value order; NaN and infinities compare above every finite value).
-// 32 x 32 tiles; general: each element counts for its row; symmetric: each
-// stored element of the lower triangle counts for its row and its column.
-__global__ void oz_row_absmax_kernel(int n, const double* __restrict__ A, int64_t lda, int sym,
+// the value order; NaN and infinities compare above every finite value).  One
+// thread per row over a range of columns (coalesced down the columns), one
+// atomic per thread.
+__global__ void oz_row_absmax_kernel(int n, const double* __restrict__ A, int64_t lda, int kspan,
                                      unsigned long long* __restrict__ rowmax)
 {
-  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
-  if (sym && r0 + 31 < k0) return;                       // tile strictly above the diagonal
-  const int tx = threadIdx.x, ty = threadIdx.y;          // 32 x 8
-  const int r = r0 + tx;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int k0 = blockIdx.y * kspan, k1 = min(n, k0 + kspan);
   unsigned long long m = 0;
-  __shared__ unsigned long long colm[32][33];
-  for (int yy = ty; yy < 32; yy += 8) {
-    const int k = k0 + yy;
-    unsigned long long b = 0;
-    if (r < n && k < n && (!sym || r >= k)) b = (unsigned long long)__double_as_longlong(fabs(A[(int64_t)k * lda + r]));
-    m = max(m, b);
-    colm[yy][tx] = b;
-  }
-  if (r < n) atomicMax(&rowmax[r], m);
-  if (sym) {                                             // the mirrored element A(k, r) belongs to row k
-    __syncthreads();
-    for (int yy = ty; yy < 32; yy += 8) {
-      unsigned long long mm = 0;
-      for (int x = 0; x < 32; ++x) mm = max(mm, colm[yy][x]);
-      const int k = k0 + yy;
-      if (tx == 0 && k < n) atomicMax(&rowmax[k], mm);
-    }
-  }
+  for (int k = k0; k < k1; ++k)
+    m = max(m, (unsigned long long)__double_as_longlong(A[(int64_t)k * lda + r]) & 0x7FFFFFFFFFFFFFFFull);
+  atomicMax(&rowmax[r], m);
 }
 
 // Digit slices of A: out[i][r][k] (bf16, K-major, ld ldk, mp rows per slice),
 // zero in the padding (r >= n or k >= n).  32 x 32 tiles through shared memory:
 // reads along rows of the column-major source, writes along k.
-__global__ void oz_slice_a_kernel(int n, int mp, int64_t ldk, const double* __restrict__ A, int64_t lda, int sym,
+__global__ void oz_slice_a_kernel(int n, int mp, int64_t ldk, const double* __restrict__ A, int64_t lda,
                                   const unsigned long long* __restrict__ rowmax, int* __restrict__ row_exp,
                                   __nv_bfloat16* __restrict__ out)
 {
@@ -124,34 +131,17 @@ __global__ void oz_slice_a_kernel(int n, int mp, int64_t ldk, const double* __re
   }
   for (int yy = ty; yy < 32; yy += 8) {
     const int r = r0 + tx, k = k0 + yy;
-    double v = 0.0;
-    if (r < n && k < n) {
-      if (sym && r < k) v = 0.0;                         // filled from the transposed read below
-      else v = A[(int64_t)k * lda + r];
-    }
-    tile[tx][yy] = v;
-  }
-  if (sym) {                                             // A(r, k) for r < k = A(k, r), read along k
-    __syncthreads();                                     // after the zeros above
-    for (int yy = ty; yy < 32; yy += 8) {
-      const int r = r0 + yy, k = k0 + tx;
-      if (r < n && k < n && r < k) tile[yy][tx] = A[(int64_t)r * lda + k];
-    }
+    tile[tx][yy] = (r < n && k < n) ? A[(int64_t)k * lda + r] : 0.0;
   }
   __syncthreads();
   for (int yy = ty; yy < 32; yy += 8) {
     const int r = r0 + yy, k = k0 + tx;
     if (r >= mp || k >= ldk) continue;
-    double v = tile[yy][tx];
-    const bool finite = isfinite(v);
-    v = finite ? scalbn(v, -sexp[yy]) : 0.0;             // |v| < 1, exact
+    const double v = tile[yy][tx];
+    bool neg = false;
+    const unsigned long long F = isfinite(v) ? fixed56(v, sexp[yy], &neg) : 0ull;
 #pragma unroll
-    for (int i = 0; i < OZ_SLICES; ++i) {
-      v *= (double)(1 << OZ_DIGIT);
-      const double d = trunc(v);
-      v -= d;
-      out[((int64_t)i * mp + r) * ldk + k] = __double2bfloat16(d);   // |d| <= 127: exact
-    }
+    for (int i = 0; i < OZ_SLICES; ++i) out[((int64_t)i * mp + r) * ldk + k] = digit_bf16(F, neg, i);
   }
 }
 
@@ -177,15 +167,11 @@ __global__ void oz_slice_x_kernel(int n, int nrhs, int64_t ldk, const double* __
   const int e = c < nrhs ? bound_exponent(colmax[c]) : 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) col_exp[c] = e;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ldk; k += (int64_t)gridDim.x * blockDim.x) {
-    double v = (c < nrhs && k < n) ? X[(int64_t)c * ldx + k] : 0.0;
-    v = isfinite(v) ? scalbn(v, -e) : 0.0;
+    const double v = (c < nrhs && k < n) ? X[(int64_t)c * ldx + k] : 0.0;
+    bool neg = false;
+    const unsigned long long F = isfinite(v) ? fixed56(v, e, &neg) : 0ull;
 #pragma unroll
-    for (int j = 0; j < OZ_SLICES; ++j) {
-      v *= (double)(1 << OZ_DIGIT);
-      const double d = trunc(v);
-      v -= d;
-      out[(int64_t)(j * OZ_RHS + c) * ldk + k] = __double2bfloat16(d);
-    }
+    for (int j = 0; j < OZ_SLICES; ++j) out[(int64_t)(j * OZ_RHS + c) * ldk + k] = digit_bf16(F, neg, j);
   }
 }
 
@@ -385,7 +371,7 @@ inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
 
-int OzakiMatrix::prepare(cudaStream_t s, int n_, const double* A, int64_t lda, int sym)
+int OzakiMatrix::prepare(cudaStream_t s, int n_, const double* A, int64_t lda)
 {
   ready = false;
   if (n_ <= 0) return GBS_SUCCESS;
@@ -396,14 +382,17 @@ int OzakiMatrix::prepare(cudaStream_t s, int n_, const double* A, int64_t lda, i
   GBS_TRY(rowmax.reserve(sizeof(unsigned long long) * (size_t)mp));
   GBS_TRY(row_exp.reserve(sizeof(int) * (size_t)mp));
   GBS_CUDA_TRY(cudaMemsetAsync(rowmax.p, 0, sizeof(unsigned long long) * (size_t)mp, s));
-  PhaseScope ps(s, PH_RESIDUAL, 0.0, 8.0 * (double)n * n * (sym ? 1.5 : 2.0) + 16.0 * (double)mp * ldk);
-  const dim3 blk(32, 8), grid(cdiv(n, 32), cdiv(n, 32));
-  oz_row_absmax_kernel<<<grid, blk, 0, s>>>(n, A, lda, sym, rowmax.as<unsigned long long>());
+  PhaseScope ps(s, PH_RESIDUAL, 0.0, 16.0 * (double)n * n + 16.0 * (double)mp * ldk);
+  const int rblocks = cdiv(n, 256);
+  const int ksplit = std::max(1, std::min(cdiv(n, 64), 4 * device_sm_count() / rblocks));
+  const int kspan = cdiv(n, ksplit);
+  oz_row_absmax_kernel<<<dim3(rblocks, cdiv(n, kspan)), 256, 0, s>>>(n, A, lda, kspan,
+                                                                      rowmax.as<unsigned long long>());
   GBS_CUDA_TRY(cudaGetLastError());
   count_launch();
-  const dim3 grid2(cdiv(mp, 32), cdiv(ldk, 32));
-  oz_slice_a_kernel<<<grid2, blk, 0, s>>>(n, mp, ldk, A, lda, sym, rowmax.as<unsigned long long>(),
-                                          row_exp.as<int>(), slices.as<__nv_bfloat16>());
+  const dim3 blk(32, 8), grid2(cdiv(mp, 32), cdiv(ldk, 32));
+  oz_slice_a_kernel<<<grid2, blk, 0, s>>>(n, mp, ldk, A, lda, rowmax.as<unsigned long long>(), row_exp.as<int>(),
+                                          slices.as<__nv_bfloat16>());
   GBS_CUDA_TRY(cudaGetLastError());
   GBS_TRY(make_tmap(&tmA, slices.p, 2, (int64_t)OZ_SLICES * mp, ldk, ldk, OZ_BM));
   ready = true;

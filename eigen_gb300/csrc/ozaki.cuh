@@ -18,8 +18,8 @@ struct OzakiMatrix {
   int n = 0, mp = 0;
   int64_t ldk = 0;
   bool ready = false;
-  // sym: A symmetric with its lower triangle stored.
-  int prepare(cudaStream_t s, int n, const double* A, int64_t lda, int sym);
+  // A general, column-major (symmetric matrices are passed as full copies).
+  int prepare(cudaStream_t s, int n, const double* A, int64_t lda);
 };
 
 struct OzakiWork {
