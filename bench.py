@@ -1037,7 +1037,8 @@ def factor_once(args):
     import eigen_gb300 as gb
     n = args.n
     a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(3)).t()
-    b = torch.randn(1, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(4)).t()
+    b = torch.randn(args.nrhs, n, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator("cuda").manual_seed(4)).t()
     torch.cuda.synchronize()
     if args.path == "fp64":
         lu = gb.PartialPivLU(a)

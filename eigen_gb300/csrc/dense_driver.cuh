@@ -89,9 +89,12 @@ constexpr int kPanelNB = 32;   // columns factored per panel launch
 // is null when it did not).  With trsm_done, may also interchange the
 // trsm_cols columns right of the panel and solve their top rows with L11
 // (*trsm_done says whether it did; the caller then skips those columns).
+// tournament: the mixed-precision path's panels may take tournament pivoting
+// (panel_lu_tournament_kernel) instead of the reference's partial pivoting.
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                 DeviceStatus* st, const int** map_out = nullptr, int trsm_cols = 0, bool* trsm_done = nullptr);
+                 DeviceStatus* st, const int** map_out = nullptr, int trsm_cols = 0, bool* trsm_done = nullptr,
+                 bool tournament = false);
 // CTAs of the cluster panel_factor launches for a panel of m rows (one per SM).
 int panel_cluster_ctas(int m);
 

@@ -39,6 +39,7 @@ extern "C" void gbs_refine_options_default(gbs_refine_options* o)
   o->shift_factor = d.shift_factor;
   o->lookahead = d.lookahead;
   o->residual = d.residual;
+  o->pivoting = d.pivoting;
 }
 
 static int to_options(const gbs_refine_options* o, MixedOptions* m)
@@ -54,10 +55,12 @@ static int to_options(const gbs_refine_options* o, MixedOptions* m)
     d.shift_factor = o->shift_factor;
     d.lookahead = o->lookahead;
     d.residual = o->residual;
+    d.pivoting = o->pivoting;
   }
   if (d.tier < GBS_TIER_FP64 || d.tier > GBS_TIER_FP16 || d.refine < GBS_REFINE_AUTO || d.refine > GBS_REFINE_GMRES ||
       d.max_iter < 0 || d.gmres_restart < 1 || d.gmres_restart > 200 || !(d.tol >= 0) || !(d.shift_factor >= 0) ||
-      d.residual < GBS_RESID_AUTO || d.residual > GBS_RESID_OZAKI) {
+      d.residual < GBS_RESID_AUTO || d.residual > GBS_RESID_OZAKI || d.pivoting < GBS_PIVOT_AUTO ||
+      d.pivoting > GBS_PIVOT_PARTIAL) {
     gbs_set_last_message("invalid gbs_refine_options");
     return GBS_INVALID_ARGUMENT;
   }

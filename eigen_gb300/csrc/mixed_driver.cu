@@ -157,6 +157,34 @@ __global__ void row_abs_sum_kernel(int n, const double* __restrict__ A, int64_t 
   rows[i] = s;
 }
 
+// Row sums of |A| (general A) over the column range [k0, k0 + kspan) of
+// blockIdx.y, one thread per row: part[blockIdx.y][i].  Summed over the ranges
+// in a fixed order by row_abs_reduce_kernel, so the norm is deterministic.
+__global__ void row_abs_partial_kernel(int n, const double* __restrict__ A, int64_t lda, int kspan,
+                                       double* __restrict__ part)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k0 = blockIdx.y * kspan, k1 = min(n, k0 + kspan);
+  double s0 = 0.0, s1 = 0.0;
+  int k = k0;
+  for (; k + 1 < k1; k += 2) {                       // two independent chains
+    s0 += fabs(A[(int64_t)k * lda + i]);
+    s1 += fabs(A[(int64_t)(k + 1) * lda + i]);
+  }
+  if (k < k1) s0 += fabs(A[(int64_t)k * lda + i]);
+  part[(int64_t)blockIdx.y * n + i] = s0 + s1;
+}
+
+__global__ void row_abs_reduce_kernel(int n, int splits, const double* __restrict__ part, double* __restrict__ rows)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int k = 0; k < splits; ++k) s += part[(int64_t)k * n + i];
+  rows[i] = s;
+}
+
 // W32 = fp32(R / s_c), s_c = max_i |R(i,c)| (1 when zero); W packed n x nrhs
 // W = R / s_c in FP32; with perm, rows are gathered: W(i) = R(perm[i]) / s_c
 // (the row interchanges of P A = L U applied on the way)
@@ -518,7 +546,7 @@ diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int n
 // caller applies the whole block's interchanges to the other columns later
 // (row interchanges commute with the row-wise trailing updates in between).
 static int block_panels(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
-                        int kind, TcWorkspace& tcw, DevBuf& map, int k, int kb, bool defer)
+                        int kind, TcWorkspace& tcw, DevBuf& map, int k, int kb, bool defer, bool tournament)
 {
   const int lo = defer ? k : 0, hi = defer ? k + kb : n;
   for (int j = k; j < k + kb; j += kPanelNB) {
@@ -527,7 +555,7 @@ static int block_panels(cudaStream_t s, int n, float* A, int64_t lda, int* tr, D
     const int rest = k + kb - (j + jb);
     const int* pmap = nullptr;
     bool fused = false;       // interchanges + U12 of the block's columns right of the panel done in the panel
-    GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap, rest, &fused));
+    GBS_TRY(panel_factor<float>(s, Ajj, lda, n - j, jb, j, tr + j, scratch, st, &pmap, rest, &fused, tournament));
     if (pmap && fused) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, lo, j, k + kb, hi));
     else if (pmap) GBS_TRY(laswp_map_apply<float>(s, A, lda, pmap, lo, j, j + jb, hi));
     else GBS_TRY(laswp_gather_device<float>(s, A, lda, tr, j, j + jb, lo, j, j + jb, hi, map));
@@ -581,12 +609,13 @@ static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int
 // Every element sees the same operations in the same order as in the plain
 // schedule, so both give identical factors and interchanges.
 static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
-                           int kind, TcWorkspace& tcw, DevBuf& map, float* minv, Lookahead& la)
+                           int kind, TcWorkspace& tcw, DevBuf& map, float* minv, Lookahead& la, bool tournament)
 {
   cudaStream_t ss = la.side;
   GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
   GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
-  GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, 0, std::min(kMixedNB, n), true));
+  GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, 0, std::min(kMixedNB, n), true,
+                       tournament));
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
     const int nr = n - k - kb;
@@ -604,7 +633,7 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
     GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, c1, minv, st, kind, tcw, 0));
     GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
     GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
-    GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, k + kb, nb1, true));
+    GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, k + kb, nb1, true, tournament));
     GBS_TRY(laswp_map_apply<float>(s, A, lda, map.as<int>(), 0, k, c1, n));
     // the panel's cluster and the panels' small kernels keep 2 clusters' worth of SMs
     const int keep = std::min(2 * panel_cluster_ctas(nr), device_sm_count() / 2);
@@ -614,7 +643,7 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
 }
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
-                TcWorkspace& tcw, DevBuf& map, DevBuf& minv, Lookahead* la)
+                TcWorkspace& tcw, DevBuf& map, DevBuf& minv, Lookahead* la, bool tournament)
 {
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -623,13 +652,13 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
                                     (int)kInvSmem));
   if (la && n > kMixedNB) {
     GBS_TRY(la->init());
-    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, map, minv.as<float>(), *la);
+    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, map, minv.as<float>(), *la, tournament);
     if (rc != GBS_SUCCESS) cudaStreamSynchronize(la->side);   // nothing of the side stream outlives the call
     return rc;
   }
   for (int k = 0; k < n; k += kMixedNB) {
     const int kb = std::min(kMixedNB, n - k);
-    GBS_TRY(block_panels(s, n, A, lda, tr, st, scratch, kind, tcw, map, k, kb, false));
+    GBS_TRY(block_panels(s, n, A, lda, tr, st, scratch, kind, tcw, map, k, kb, false, tournament));
     if (n - k - kb > 0) {
       GBS_TRY(block_inverse(s, A, lda, k, kb, minv.as<float>()));
       GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, n, minv.as<float>(), st, kind, tcw, 0));
@@ -994,8 +1023,20 @@ static int reserve_common(MixedWork& w, int n, int nrhs)
 
 static int inf_norm(cudaStream_t s, const Problem& P, MixedWork& w, double* anorm)
 {
-  count_launch();
-  row_abs_sum_kernel<<<cdiv(P.n, 256), 256, 0, s>>>(P.n, P.A, P.lda, P.sym, w.rows.as<double>());
+  const int rblocks = cdiv(P.n, 256);
+  const int splits = P.sym ? 1 : std::max(1, std::min(cdiv(P.n, 64), 4 * device_sm_count() / rblocks));
+  if (splits == 1) {
+    count_launch();
+    row_abs_sum_kernel<<<rblocks, 256, 0, s>>>(P.n, P.A, P.lda, P.sym, w.rows.as<double>());
+  } else {
+    const int kspan = cdiv(P.n, splits);
+    const int used = cdiv(P.n, kspan);
+    GBS_TRY(w.part.reserve(sizeof(double) * (size_t)used * P.n));
+    count_launch();
+    row_abs_partial_kernel<<<dim3(rblocks, used), 256, 0, s>>>(P.n, P.A, P.lda, kspan, w.part.as<double>());
+    count_launch();
+    row_abs_reduce_kernel<<<rblocks, 256, 0, s>>>(P.n, used, w.part.as<double>(), w.rows.as<double>());
+  }
   GBS_CUDA_TRY(cudaGetLastError());
   std::vector<double> h((size_t)P.n);
   GBS_CUDA_TRY(cudaMemcpyAsync(h.data(), w.rows.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
@@ -1080,7 +1121,8 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
       GBS_CUDA_TRY(cudaGetLastError());
     }
     GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.map,
-                        w.minv, opt.lookahead ? &w.la : nullptr));
+                        w.minv, opt.lookahead ? &w.la : nullptr,
+                        opt.pivoting == GBS_PIVOT_TOURNAMENT));
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {

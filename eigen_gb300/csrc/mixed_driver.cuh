@@ -18,6 +18,7 @@ struct MixedOptions {
   double shift_factor = 4.0;     // LLT tiers: initial diagonal shift = shift_factor * u_factorization
   int lookahead = 0;             // LU: overlap each block's panels with the previous block's trailing update
   int residual = GBS_RESID_AUTO; // how the FP64 residuals are computed (gbs_residual_mode)
+  int pivoting = GBS_PIVOT_AUTO; // LU panels: tournament or the reference's partial pivoting (gbs_pivoting)
 };
 
 // R = B - A X (B null: R = A X), FP64-accurate, nrhs columns, on device

@@ -3,7 +3,7 @@
 
 namespace gbs {
 template int panel_factor<float>(cudaStream_t, float*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
-                                  const int**, int, bool*);
+                                  const int**, int, bool*, bool);
 template int panel_preload<float>();
 
 int panel_cluster_ctas(int m)

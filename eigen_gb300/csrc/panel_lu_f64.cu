@@ -3,6 +3,6 @@
 
 namespace gbs {
 template int panel_factor<double>(cudaStream_t, double*, int64_t, int, int, int, int*, DevBuf&, DeviceStatus*,
-                                  const int**, int, bool*);
+                                  const int**, int, bool*, bool);
 template int panel_preload<double>();
 }  // namespace gbs

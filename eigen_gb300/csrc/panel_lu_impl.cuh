@@ -92,6 +92,63 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
   return GBS_SUCCESS;
 }
 
+// Largest cluster (power of two, <= 16) the device schedules for the
+// tournament-pivoting kernel.
+template <typename T>
+static int tournament_panel_limit()
+{
+  static const int limit = [] {
+    int lim = 0;
+    const void* k = (const void*)panel_lu_tournament_kernel<T, kPanelNB>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) cudaGetLastError();
+    const int dyn = (int)tournament_dyn_smem<T, kPanelNB>();
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    for (int c = kMaxPanelCluster; c >= 2 && lim == 0; c /= 2) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(kClusterPanelThreads);
+      cfg.dynamicSmemBytes = dyn;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters > 0) lim = c;
+      else cudaGetLastError();
+    }
+    return lim;
+  }();
+  return limit;
+}
+
+template <typename T>
+static int launch_tournament_panel(cudaStream_t s, T* a, int64_t lda, int m, int k0, int* tr, DeviceStatus* st,
+                                   int C, int* map, int trsm_cols)
+{
+  PhaseScope ps(s, PH_PANEL, (double)m * kPanelNB * kPanelNB, sizeof(T) * 2.0 * m * kPanelNB);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kClusterPanelThreads);
+  cfg.dynamicSmemBytes = tournament_dyn_smem<T, kPanelNB>();
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_tournament_kernel<T, kPanelNB>, a, lda, m, k0, tr, st, map,
+                                  trsm_cols));
+  return GBS_SUCCESS;
+}
+
 // The panel on one cluster when its rows fit (one row per thread, two for
 // FP32), else on the cooperative grid kernel.  With map_out, the cluster
 // kernel also leaves the panel's interchanges as a row map in scratch and
@@ -100,10 +157,24 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
 // trsm_cols columns right of the panel; *trsm_done says whether it did.
 template <typename T>
 int panel_factor(cudaStream_t s, T* a, int64_t lda, int m, int nbc, int k0, int* tr, DevBuf& scratch,
-                        DeviceStatus* st, const int** map_out, int trsm_cols, bool* trsm_done)
+                        DeviceStatus* st, const int** map_out, int trsm_cols, bool* trsm_done, bool tournament)
 {
   if (map_out) *map_out = nullptr;
   if (trsm_done) *trsm_done = false;
+  if (tournament && nbc == kPanelNB && m > kClusterPanelThreads && m <= kMaxPanelCluster * kClusterPanelThreads) {
+    const int C = panel_cluster_ctas(m);
+    if (C <= tournament_panel_limit<T>()) {
+      int* map = nullptr;
+      if (map_out) {
+        GBS_TRY(scratch.reserve(sizeof(int) * kLaswpMapInts));
+        map = scratch.as<int>();
+        *map_out = map;
+      }
+      const int tc = trsm_done ? trsm_cols : 0;
+      if (trsm_done) *trsm_done = tc > 0;
+      return launch_tournament_panel<T>(s, a, lda, m, k0, tr, st, C, map, tc);
+    }
+  }
   {
     constexpr int rpt_max = sizeof(T) == 8 ? 1 : 2;
     int C = 1;

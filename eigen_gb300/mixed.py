@@ -24,7 +24,7 @@ REFINE_NAMES = {v: k for k, v in REFINE.items()}
 class RefineOptions(C.Structure):
     _fields_ = [("tier", C.c_int), ("refine", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("gmres_restart", C.c_int), ("gmres_tol", C.c_double), ("shift_factor", C.c_double),
-                ("residual", C.c_int), ("lookahead", C.c_int)]
+                ("residual", C.c_int), ("pivoting", C.c_int), ("lookahead", C.c_int)]
 
 
 class RefineInfo(C.Structure):
@@ -40,10 +40,11 @@ class RefineInfo(C.Structure):
 
 
 RESIDUAL = {"auto": 0, "fp64": 1, "ozaki": 2}
+PIVOTING = {"auto": 0, "tournament": 1, "partial": 2}
 
 
 def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=40, gmres_tol=1e-10,
-            shift_factor=4.0, lookahead=False, residual="auto") -> RefineOptions:
+            shift_factor=4.0, lookahead=False, residual="auto", pivoting="auto") -> RefineOptions:
     o = RefineOptions()
     L.lib().gbs_refine_options_default(C.byref(o))
     o.tier = TIERS[tier] if isinstance(tier, str) else int(tier)
@@ -52,6 +53,7 @@ def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=
         shift_factor
     o.lookahead = int(bool(lookahead))
     o.residual = RESIDUAL[residual] if isinstance(residual, str) else int(residual)
+    o.pivoting = PIVOTING[pivoting] if isinstance(pivoting, str) else int(pivoting)
     return o
 
 

@@ -354,6 +354,21 @@ typedef enum gbs_refine_mode { GBS_REFINE_AUTO = 0, GBS_REFINE_CLASSIC = 1, GBS_
  *     maximum) at 16 n^2 bytes of device memory for the slices of A;
  *  GBS_RESID_AUTO:  Ozaki from n = 1024, FP64 below. */
 typedef enum gbs_residual_mode { GBS_RESID_AUTO = 0, GBS_RESID_FP64 = 1, GBS_RESID_OZAKI = 2 } gbs_residual_mode;
+/* Row pivoting of the mixed-precision LU's panels:
+ *  GBS_PIVOT_TOURNAMENT: tournament pivoting (CALU, Grigori, Demmel & Xiang
+ *     2011) -- every CTA of the panel's cluster proposes 32 rows by partial
+ *     pivoting on its own rows, one CTA picks the panel's pivots among them;
+ *     two cluster barriers per 32-column panel instead of 32, but three
+ *     32-step eliminations (the CTAs', the final one, the rows of L) instead
+ *     of one: on GB300 a panel's time is its per-step CTA work, not its
+ *     cluster barriers, so it measures slower (84 against 57 us per panel at
+ *     n = 8192), and its larger growth factor costs accuracy and, with
+ *     16-bit factors, GMRES iterations.
+ *  GBS_PIVOT_PARTIAL: the reference's partial pivoting (PartialPivLU's pivot
+ *     order).
+ *  GBS_PIVOT_AUTO: partial pivoting.
+ * The refinement and its FP64 fallback guard the result whichever is used. */
+typedef enum gbs_pivoting { GBS_PIVOT_AUTO = 0, GBS_PIVOT_TOURNAMENT = 1, GBS_PIVOT_PARTIAL = 2 } gbs_pivoting;
 
 typedef struct gbs_refine_options {
   int tier;               /* gbs_tier */
@@ -364,6 +379,7 @@ typedef struct gbs_refine_options {
   double gmres_tol;       /* relative target of one GMRES correction (default 1e-10) */
   double shift_factor;    /* SPD tiers: diagonal shift = shift_factor * u of the tier (default 4) */
   int residual;           /* gbs_residual_mode of the FP64 residuals (default GBS_RESID_AUTO) */
+  int pivoting;           /* gbs_pivoting of the general-A panels (default GBS_PIVOT_AUTO) */
   int lookahead;          /* general A: 1 factors each 128-column block's panels on a second,
                              high-priority stream while the previous block's wide trailing update runs;
                              0 (default) runs every step on the caller's stream.  Same results either

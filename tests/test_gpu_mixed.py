@@ -163,3 +163,44 @@ def test_lookahead_gives_identical_results(tier, n):
     assert np.array_equal(x1, x0)
     assert i1["iterations"] == i0["iterations"] and i1["fell_back"] == i0["fell_back"]
     assert O.backward_error(a, x1, b) <= BAR
+
+
+@pytest.mark.parametrize("tier", ["tf32x3", "bf16"])
+@pytest.mark.parametrize("n", [600, 2048, 5000])
+def test_tournament_and_partial_pivoting_both_converge(tier, n):
+    """Tournament pivoting (an option of the mixed LU's panels) against the
+    reference's partial pivoting: both reach the bound and agree to the
+    conditioning.  Classic refinement needs the same number of steps
+    (within one); GMRES on 16-bit factors may need more inner iterations with
+    tournament pivoting (its growth factor is larger), but at most 1.6x."""
+    a = O.gauss(700 + n, n, n)
+    b = O.gauss(800 + n, n, 3)
+    x_t, i_t = solve_mixed(a, b, tier=tier, pivoting="tournament")
+    x_p, i_p = solve_mixed(a, b, tier=tier, pivoting="partial")
+    for x, info in ((x_t, i_t), (x_p, i_p)):
+        assert O.backward_error(a, x, b) <= BAR, info
+        if tier == "tf32x3":
+            assert not info["fell_back"], info
+    if tier == "tf32x3":
+        assert abs(i_t["iterations"] - i_p["iterations"]) <= 1, (i_t, i_p)
+    elif not i_t["fell_back"] and not i_p["fell_back"]:
+        assert i_t["inner_iterations"] <= 1.6 * i_p["inner_iterations"] + 5, (i_t, i_p)
+    assert np.linalg.norm(x_t - x_p) / np.linalg.norm(x_p) <= 1e-9
+
+
+def test_tournament_pivoting_on_hard_panels():
+    """Panels that defeat a careless candidate choice: rows whose magnitudes
+    span 30 orders, a block of exactly dependent rows (rank-deficient
+    candidates in one CTA), and a lower-triangular matrix (every pivot sits
+    on the diagonal).  Each solve meets the bound, by refinement or by the
+    FP64 fallback."""
+    n = 3000
+    rng = np.random.default_rng(4)
+    a1 = O.gauss(41, n, n) * (10.0 ** rng.uniform(-15, 15, n))[:, None]
+    a2 = O.gauss(42, n, n)
+    a2[100:900] = a2[100] * rng.uniform(0.5, 2.0, 800)[:, None] + 1e-3 * a2[100:900]
+    a3 = np.tril(O.gauss(43, n, n)) + 50.0 * np.eye(n)
+    for a in (a1, a2, a3):
+        b = O.gauss(44, n, 2)
+        x, info = solve_mixed(a, b, tier="tf32x3", pivoting="tournament")
+        assert O.backward_error(a, x, b) <= BAR, info
