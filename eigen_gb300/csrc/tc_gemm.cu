@@ -55,6 +55,20 @@ __device__ __forceinline__ bool skip_tile(const TcParams& p, int tm, int tn)
   return p.lower && (tn * BN >= tm * BM + BM);    // tile strictly above the diagonal
 }
 
+// L2 prefetch of this warp's 32 rows of C tile t (one 128-byte line per column,
+// eight columns per lane), so that the epilogue's reads of C hit L2.
+__device__ __forceinline__ void prefetch_c_tile(const TcParams& p, int t, int q, int lane)
+{
+  const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+  if (skip_tile(p, tm, tn)) return;
+  const int row0 = tm * BM + 32 * q;
+  if (row0 >= p.M) return;
+  for (int c = lane; c < BN; c += 32) {
+    const int col = tn * BN + c;
+    if (col < p.N) asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + (int64_t)col * p.ldc + row0));
+  }
+}
+
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
 {
@@ -151,9 +165,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   } else {
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
     int tc = 0;
+    if (blockIdx.x < num_tiles) prefetch_c_tile(p, blockIdx.x, q, lane);
     for (int t = blockIdx.x; t < num_tiles; t += gridDim.x) {
       const int tm = t % p.tiles_m, tn = t / p.tiles_m;
       if (skip_tile(p, tm, tn)) continue;
+      // the next tile's C streams into L2 while this tile's accumulator completes
+      if (t + (int)gridDim.x < num_tiles) prefetch_c_tile(p, t + (int)gridDim.x, q, lane);
       const int b = tc & 1;
       const uint32_t tph = (uint32_t)(tc >> 1) & 1u;
       // one lane waits, the warp follows: tcgen05.ld below is .sync.aligned
