@@ -82,8 +82,8 @@ def args_parse():
     p.add_argument("--nrhs", type=int, default=16)
     p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--lookahead", type=int, default=0, choices=[0, 1],
-                   help="LU: factor block k+1's panels on a second stream during block k's update (default 0)")
+    p.add_argument("--lookahead", type=int, default=1, choices=[0, 1],
+                   help="LU: factor block k+1's panels on a second stream during block k's update (default 1)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
                    help="factor one seeded system and exit (small ncu captures)")

@@ -45,6 +45,7 @@ static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 // coalesced over rows.  Partial sums per split are added in split order by
 // residual_reduce (deterministic).
 constexpr int kResRows = 128, kResRC = 16, kResKC = 64;
+constexpr int kMixedNB = 128;                  // outer block width of the mixed LU
 constexpr int kOzakiMinN = 1024;      // GBS_RESID_AUTO: tensor-core residuals from this order
 
 template <int RC>
@@ -313,32 +314,131 @@ __global__ void gmres_scale_kernel(int n, int nrhs, const double* __restrict__ W
   Vout[t] = W[t] * inv[t / n];
 }
 
+// ------------------------------------------------------------------ SM partition
+// Two disjoint SM partitions of the device as green contexts (CUDA driver API,
+// resolved at run time like the tensor-map encoder): 32 SMs for the look-ahead
+// LU's panels, whose 16-CTA clusters must find their SMs free within one GPC,
+// and the rest for the wide trailing updates.  Created once per process; when
+// the driver cannot make them, the look-ahead runs on plain streams.
+constexpr unsigned int kPanelPartitionSms = 64;   // the panels' cluster plus room for their block updates
+
+struct SmPartition {
+  bool ok = false;
+  CUgreenCtx panel = nullptr, update = nullptr;
+  int panel_sms = 0, update_sms = 0;
+};
+
+namespace {
+
+template <typename F>
+F driver_fn(const char* name)
+{
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12050, cudaEnableDefault, &q) != cudaSuccess ||   // green streams: 12.5
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (F)p;
+}
+
+typedef CUresult (*DeviceGetFn)(CUdevice*, int);
+typedef CUresult (*GetDevResourceFn)(CUdevice, CUdevResource*, CUdevResourceType);
+typedef CUresult (*SplitByCountFn)(CUdevResource*, unsigned int*, const CUdevResource*, CUdevResource*, unsigned int,
+                                   unsigned int);
+typedef CUresult (*GenerateDescFn)(CUdevResourceDesc*, CUdevResource*, unsigned int);
+typedef CUresult (*GreenCtxCreateFn)(CUgreenCtx*, CUdevResourceDesc, CUdevice, unsigned int);
+typedef CUresult (*GreenStreamCreateFn)(CUstream*, CUgreenCtx, unsigned int, int);
+
+const SmPartition& sm_partition()
+{
+  static SmPartition part;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    auto dev_get = driver_fn<DeviceGetFn>("cuDeviceGet");
+    auto get_res = driver_fn<GetDevResourceFn>("cuDeviceGetDevResource");
+    auto split = driver_fn<SplitByCountFn>("cuDevSmResourceSplitByCount");
+    auto gen = driver_fn<GenerateDescFn>("cuDevResourceGenerateDesc");
+    auto create = driver_fn<GreenCtxCreateFn>("cuGreenCtxCreate");
+    if (!dev_get || !get_res || !split || !gen || !create) return;
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) return;
+    CUdevice dev;
+    CUdevResource all, group[1], rest;
+    unsigned int ngroups = 1;
+    CUdevResourceDesc da, db;
+    if (dev_get(&dev, d) != CUDA_SUCCESS || get_res(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return;
+    if (split(group, &ngroups, &all, &rest, CU_DEV_SM_RESOURCE_SPLIT_MAX_POTENTIAL_CLUSTER_SIZE, kPanelPartitionSms) !=
+            CUDA_SUCCESS ||
+        ngroups != 1 || rest.sm.smCount < 64)
+      return;
+    if (gen(&da, group, 1) != CUDA_SUCCESS || gen(&db, &rest, 1) != CUDA_SUCCESS) return;
+    if (create(&part.panel, da, dev, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS ||
+        create(&part.update, db, dev, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS)
+      return;
+    part.panel_sms = (int)group[0].sm.smCount;
+    part.update_sms = (int)rest.sm.smCount;
+    part.ok = true;
+  });
+  return part;
+}
+
+int partition_stream(CUgreenCtx g, int priority, cudaStream_t* out)
+{
+  auto create = driver_fn<GreenStreamCreateFn>("cuGreenCtxStreamCreate");
+  CUstream st = nullptr;
+  if (!create || create(&st, g, CU_STREAM_NON_BLOCKING, priority) != CUDA_SUCCESS) {
+    gbs_set_last_message("cuGreenCtxStreamCreate failed");
+    return GBS_CUDA_ERROR;
+  }
+  *out = (cudaStream_t)st;
+  return GBS_SUCCESS;
+}
+
+}  // namespace
+
 // ------------------------------------------------------------------ workspace pool
-// Second stream of the look-ahead LU: the panels of block k+1 run on it while
-// the caller's stream applies block k's wide trailing update.  It has the
-// highest stream priority, so that when both become ready the panel's cluster
-// is placed before the update's persistent CTAs take the SMs.
+// Streams of the look-ahead LU: the panels of block k+1 run on `side` while
+// `wide` applies block k's interchanges to the other columns and its wide
+// trailing update; the caller's stream does the short serial part in between.
+// With an SM partition, side and wide live in its two green contexts (disjoint
+// SMs); otherwise side is a highest-priority stream and wide is the caller's.
 struct Lookahead {
-  cudaStream_t side = nullptr;
-  cudaEvent_t ready = nullptr, panels = nullptr;
-  TcWorkspace tc;
-  DevBuf map;
+  cudaStream_t side = nullptr, wide = nullptr;
+  int wide_sms = 0;
+  cudaEvent_t ready = nullptr, panels = nullptr, wide_done = nullptr;
+  TcWorkspace tc_side, tc_wide;
+  DevBuf map_side, map[2], minv[2];
   int init()
   {
     if (!side) {
       int least = 0, greatest = 0;
       GBS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-      GBS_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, greatest));
+      const SmPartition& part = sm_partition();
+      if (part.ok && partition_stream(part.panel, greatest, &side) == GBS_SUCCESS &&
+          partition_stream(part.update, 0, &wide) == GBS_SUCCESS) {
+        wide_sms = part.update_sms;
+      } else {
+        if (side) cudaStreamDestroy(side);
+        side = wide = nullptr;
+        wide_sms = 0;
+        GBS_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, greatest));
+      }
     }
     if (!ready) GBS_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     if (!panels) GBS_CUDA_TRY(cudaEventCreateWithFlags(&panels, cudaEventDisableTiming));
+    if (!wide_done) GBS_CUDA_TRY(cudaEventCreateWithFlags(&wide_done, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) GBS_TRY(minv[i].reserve(sizeof(float) * kMixedNB * kMixedNB));
     return GBS_SUCCESS;
   }
   ~Lookahead()
   {
     if (ready) cudaEventDestroy(ready);
     if (panels) cudaEventDestroy(panels);
+    if (wide_done) cudaEventDestroy(wide_done);
     if (side) cudaStreamDestroy(side);
+    if (wide) cudaStreamDestroy(wide);
   }
 };
 
@@ -413,7 +513,6 @@ static int tc_kind(int tier)
 }
 
 // ------------------------------------------------------------------ factorizations
-constexpr int kMixedNB = 128;
 constexpr int kPermSmemMax = 56 * 1024;          // perm_from_transpositions_kernel: n ints of shared memory
 
 // M = I - L^-1 for the lower nb x nb block L (nb <= kMixedNB, ld; unit != 0:
@@ -598,46 +697,63 @@ static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int
   return GBS_SUCCESS;
 }
 
-// The look-ahead schedule (la != null).  Caller's stream s, side stream ss:
+// The look-ahead schedule (la != null).  Caller's stream s, side stream ss
+// (panels), wide stream ws (the caller's own without an SM partition):
 //   ss: panels of block 0
 //   for each block k:
-//     s:  wait for block k's panels; its interchanges on block k+1's
-//         columns; I - L11^-1; update of block k+1's columns (narrow)
+//     s:  wait for block k's panels and block k-1's wide update; block k's
+//         interchanges on block k+1's columns; I - L11^-1; update of block
+//         k+1's columns (narrow)
 //     ss: wait for the narrow update; panels of block k+1
-//     s:  block k's interchanges on the other columns; update of the columns
-//         right of block k+1 (wide), on the SMs the panels leave free
-// Every element sees the same operations in the same order as in the plain
-// schedule, so both give identical factors and interchanges.
+//     ws: wait for the narrow update; block k's interchanges on the other
+//         columns; update of the columns right of block k+1 (wide)
+// The row maps and L11 inverses alternate between two buffers by block, so
+// that s never rewrites one that ws may still read.  Every element sees the
+// same operations in the same order as in the plain schedule, so both give
+// identical factors and interchanges.
 static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
-                           int kind, TcWorkspace& tcw, DevBuf& map, float* minv, Lookahead& la, bool tournament)
+                           int kind, TcWorkspace& tcw, Lookahead& la, bool tournament)
 {
   cudaStream_t ss = la.side;
+  const bool split = la.wide != nullptr;
+  cudaStream_t ws = split ? la.wide : s;
   GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
   GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
-  GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, 0, std::min(kMixedNB, n), true,
+  GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, 0, std::min(kMixedNB, n), true,
                        tournament));
-  for (int k = 0; k < n; k += kMixedNB) {
+  bool wide_pending = false;
+  for (int k = 0, blk = 0; k < n; k += kMixedNB, ++blk) {
     const int kb = std::min(kMixedNB, n - k);
     const int nr = n - k - kb;
+    DevBuf& mapk = la.map[blk & 1];
+    float* minv = la.minv[blk & 1].as<float>();
     GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
     GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.panels, 0));
+    if (wide_pending) GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.wide_done, 0));
     if (nr == 0) {
-      GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, 0, k, k + kb, k + kb, map));
+      GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, 0, k, k + kb, k + kb, mapk));
       break;
     }
     const int nb1 = std::min(kMixedNB, nr), c1 = k + kb + nb1;
     // the interchanges on block k+1's columns gate its panels; the left and
     // wide columns get them (same map) while those panels run
-    GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, map));
+    GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, mapk));
     GBS_TRY(block_inverse(s, A, lda, k, kb, minv));
     GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, c1, minv, st, kind, tcw, 0));
     GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
     GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
-    GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc, la.map, k + kb, nb1, true, tournament));
-    GBS_TRY(laswp_map_apply<float>(s, A, lda, map.as<int>(), 0, k, c1, n));
-    // the panel's cluster and the panels' small kernels keep 2 clusters' worth of SMs
-    const int keep = std::min(2 * panel_cluster_ctas(nr), device_sm_count() / 2);
-    GBS_TRY(block_update(s, n, A, lda, k, kb, c1, n, minv, st, kind, tcw, device_sm_count() - keep));
+    if (split) GBS_CUDA_TRY(cudaStreamWaitEvent(ws, la.ready, 0));
+    GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, k + kb, nb1, true, tournament));
+    GBS_TRY(laswp_map_apply<float>(ws, A, lda, mapk.as<int>(), 0, k, c1, n));
+    // without a partition, the panel's cluster and its small kernels keep two
+    // clusters' worth of SMs from the wide update's persistent grid
+    const int ctas = split ? la.wide_sms
+                           : device_sm_count() - std::min(2 * panel_cluster_ctas(nr), device_sm_count() / 2);
+    GBS_TRY(block_update(ws, n, A, lda, k, kb, c1, n, minv, st, kind, split ? la.tc_wide : tcw, ctas));
+    if (split) {
+      GBS_CUDA_TRY(cudaEventRecord(la.wide_done, ws));
+      wide_pending = true;
+    }
   }
   return GBS_SUCCESS;
 }
@@ -652,8 +768,11 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
                                     (int)kInvSmem));
   if (la && n > kMixedNB) {
     GBS_TRY(la->init());
-    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, map, minv.as<float>(), *la, tournament);
-    if (rc != GBS_SUCCESS) cudaStreamSynchronize(la->side);   // nothing of the side stream outlives the call
+    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, *la, tournament);
+    if (rc != GBS_SUCCESS) {                    // nothing of the other streams outlives the call
+      cudaStreamSynchronize(la->side);
+      if (la->wide) cudaStreamSynchronize(la->wide);
+    }
     return rc;
   }
   for (int k = 0; k < n; k += kMixedNB) {

@@ -16,7 +16,7 @@ struct MixedOptions {
   int gmres_restart = 40;        // Krylov vectors per GMRES-IR correction
   double gmres_tol = 1e-10;      // relative preconditioned-residual target of one correction
   double shift_factor = 4.0;     // LLT tiers: initial diagonal shift = shift_factor * u_factorization
-  int lookahead = 0;             // LU: overlap each block's panels with the previous block's trailing update
+  int lookahead = 1;             // LU: overlap each block's panels with the previous block's trailing update
   int residual = GBS_RESID_AUTO; // how the FP64 residuals are computed (gbs_residual_mode)
   int pivoting = GBS_PIVOT_AUTO; // LU panels: tournament or the reference's partial pivoting (gbs_pivoting)
 };

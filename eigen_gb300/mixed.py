@@ -44,7 +44,7 @@ PIVOTING = {"auto": 0, "tournament": 1, "partial": 2}
 
 
 def options(tier="tf32x3", tol=1e-13, max_iter=30, refine="auto", gmres_restart=40, gmres_tol=1e-10,
-            shift_factor=4.0, lookahead=False, residual="auto", pivoting="auto") -> RefineOptions:
+            shift_factor=4.0, lookahead=True, residual="auto", pivoting="auto") -> RefineOptions:
     o = RefineOptions()
     L.lib().gbs_refine_options_default(C.byref(o))
     o.tier = TIERS[tier] if isinstance(tier, str) else int(tier)

@@ -380,11 +380,12 @@ typedef struct gbs_refine_options {
   double shift_factor;    /* SPD tiers: diagonal shift = shift_factor * u of the tier (default 4) */
   int residual;           /* gbs_residual_mode of the FP64 residuals (default GBS_RESID_AUTO) */
   int pivoting;           /* gbs_pivoting of the general-A panels (default GBS_PIVOT_AUTO) */
-  int lookahead;          /* general A: 1 factors each 128-column block's panels on a second,
-                             high-priority stream while the previous block's wide trailing update runs;
-                             0 (default) runs every step on the caller's stream.  Same results either
-                             way; on GB300 the panel's 16-CTA cluster seldom finds a free GPC while
-                             the update runs, so the overlap is small and 0 is as fast. */
+  int lookahead;          /* general A: 1 (default) factors each 128-column block's panels on a second
+                             stream while a third applies the previous block's wide trailing update,
+                             in two disjoint SM partitions (green contexts: 64 SMs for the panels,
+                             whose 16-CTA clusters then always find their GPC, the rest for the
+                             update; plain streams when the driver cannot partition); 0 runs every
+                             step on the caller's stream.  Same results either way. */
 } gbs_refine_options;
 
 typedef struct gbs_refine_info {
