@@ -407,7 +407,7 @@ int partition_stream(CUgreenCtx g, int priority, cudaStream_t* out)
 struct Lookahead {
   cudaStream_t side = nullptr, wide = nullptr;
   int wide_sms = 0;
-  cudaEvent_t ready = nullptr, panels = nullptr, wide_done = nullptr;
+  cudaEvent_t ready = nullptr, panels = nullptr, inv = nullptr, wide_done = nullptr;
   TcWorkspace tc_side, tc_wide;
   DevBuf map_side, map[2], minv[2];
   int init()
@@ -428,6 +428,7 @@ struct Lookahead {
     }
     if (!ready) GBS_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     if (!panels) GBS_CUDA_TRY(cudaEventCreateWithFlags(&panels, cudaEventDisableTiming));
+    if (!inv) GBS_CUDA_TRY(cudaEventCreateWithFlags(&inv, cudaEventDisableTiming));
     if (!wide_done) GBS_CUDA_TRY(cudaEventCreateWithFlags(&wide_done, cudaEventDisableTiming));
     for (int i = 0; i < 2; ++i) GBS_TRY(minv[i].reserve(sizeof(float) * kMixedNB * kMixedNB));
     return GBS_SUCCESS;
@@ -436,6 +437,7 @@ struct Lookahead {
   {
     if (ready) cudaEventDestroy(ready);
     if (panels) cudaEventDestroy(panels);
+    if (inv) cudaEventDestroy(inv);
     if (wide_done) cudaEventDestroy(wide_done);
     if (side) cudaStreamDestroy(side);
     if (wide) cudaStreamDestroy(wide);
@@ -699,12 +701,13 @@ static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int
 
 // The look-ahead schedule (la != null).  Caller's stream s, side stream ss
 // (panels), wide stream ws (the caller's own without an SM partition):
-//   ss: panels of block 0
+//   ss: panels of block 0, I - L11^-1 of block 0
 //   for each block k:
 //     s:  wait for block k's panels and block k-1's wide update; block k's
-//         interchanges on block k+1's columns; I - L11^-1; update of block
-//         k+1's columns (narrow)
-//     ss: wait for the narrow update; panels of block k+1
+//         interchanges on block k+1's columns; wait for block k's I - L11^-1;
+//         update of block k+1's columns (narrow)
+//     ss: wait for the narrow update; panels of block k+1, then its I - L11^-1
+//         (it overlaps the interchanges on s)
 //     ws: wait for the narrow update; block k's interchanges on the other
 //         columns; update of the columns right of block k+1 (wide)
 // The row maps and L11 inverses alternate between two buffers by block, so
@@ -721,13 +724,15 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
   GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
   GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, 0, std::min(kMixedNB, n), true,
                        tournament));
+  GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
+  if (n > kMixedNB) GBS_TRY(block_inverse(ss, A, lda, 0, kMixedNB, la.minv[0].as<float>()));
+  GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
   bool wide_pending = false;
   for (int k = 0, blk = 0; k < n; k += kMixedNB, ++blk) {
     const int kb = std::min(kMixedNB, n - k);
     const int nr = n - k - kb;
     DevBuf& mapk = la.map[blk & 1];
     float* minv = la.minv[blk & 1].as<float>();
-    GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
     GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.panels, 0));
     if (wide_pending) GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.wide_done, 0));
     if (nr == 0) {
@@ -738,12 +743,15 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
     // the interchanges on block k+1's columns gate its panels; the left and
     // wide columns get them (same map) while those panels run
     GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, mapk));
-    GBS_TRY(block_inverse(s, A, lda, k, kb, minv));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.inv, 0));
     GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, c1, minv, st, kind, tcw, 0));
     GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
     GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
     if (split) GBS_CUDA_TRY(cudaStreamWaitEvent(ws, la.ready, 0));
     GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, k + kb, nb1, true, tournament));
+    GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
+    if (c1 < n) GBS_TRY(block_inverse(ss, A, lda, k + kb, nb1, la.minv[(blk + 1) & 1].as<float>()));
+    GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
     GBS_TRY(laswp_map_apply<float>(ws, A, lda, mapk.as<int>(), 0, k, c1, n));
     // without a partition, the panel's cluster and its small kernels keep two
     // clusters' worth of SMs from the wide update's persistent grid
