@@ -796,8 +796,82 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
 
 // Cholesky of the lower triangle of As (FP32, ld = lda) with the reference's
 // block size; diagonal blocks and TRSM on FP32 cores, SYRK on tensor cores.
+// Block k of the Cholesky: the diagonal block's factor, then
+// A21 <- A21 L11^-T = A21 - A21 (I - L11^-T) (W = I - L11^-1 read transposed
+// as the GEMM's B), for b <= kMixedNB.
+static int potrf_block(cudaStream_t s, int n, float* As, int64_t lda, int k, int b, DeviceStatus* st, int kind,
+                       TcWorkspace& tcw, float* minv)
+{
+  const int rs = n - k - b;
+  float* Akk = As + (int64_t)k * lda + k;
+  {
+    PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
+    potrf_diag_kernel<float><<<1, 256, potrf_diag_smem<float>(b), s>>>(Akk, lda, b, k, st);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  if (rs <= 0) return GBS_SUCCESS;
+  float* A21 = Akk + b;
+  {
+    PhaseScope ps(s, PH_TRSM_LLT, (double)b * b * b / 3.0, 8.0 * b * b);
+    unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, b, minv, 0);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  return tc_gemm_sub(s, kind, rs, b, b, A21, 1, lda, minv, kMixedNB, 1, A21, lda, 0, st, tcw);
+}
+
+// The SYRK of block k restricted to the columns [c0, c1): the lower part of
+// A(c0:n, c0:c1) -= A(c0:n, k:k+b) A(c0:c1, k:k+b)^T.
+static int potrf_syrk(cudaStream_t s, int n, float* As, int64_t lda, int k, int b, int c0, int c1, DeviceStatus* st,
+                      int kind, TcWorkspace& tcw, int max_ctas)
+{
+  if (c1 <= c0) return GBS_SUCCESS;
+  const float* P = As + (int64_t)k * lda + c0;             // rows c0.. of block k's columns
+  return tc_gemm_sub(s, kind, n - c0, c1 - c0, b, P, 1, lda, P, lda, 1, As + (int64_t)c0 * lda + c0, lda, 1, st,
+                     tcw, max_ctas);
+}
+
+// Look-ahead Cholesky (same streams as the LU's): block k+1's diagonal
+// factor and TRSM on the panel stream while the wide stream applies block k's
+// SYRK to the columns right of block k+1; the caller's stream applies block
+// k's SYRK to block k+1's columns in between.  Same operations per element in
+// the same order as the single-stream loop.
+static int potrf_lookahead(cudaStream_t s, int n, float* As, int64_t lda, int b, DeviceStatus* st, int kind,
+                           TcWorkspace& tcw, Lookahead& la)
+{
+  cudaStream_t ss = la.side;
+  const bool split = la.wide != nullptr;
+  cudaStream_t ws = split ? la.wide : s;
+  float* minv = la.minv[0].as<float>();
+  GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
+  GBS_TRY(potrf_block(ss, n, As, lda, 0, std::min(b, n), st, kind, la.tc_side, minv));
+  GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
+  bool wide_pending = false;
+  for (int k = 0; k < n; k += b) {
+    const int kb = std::min(b, n - k);
+    const int rs = n - k - kb;
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.panels, 0));
+    if (wide_pending) GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.wide_done, 0));
+    if (rs == 0) break;
+    const int nb1 = std::min(b, rs), c1 = k + kb + nb1;
+    GBS_TRY(potrf_syrk(s, n, As, lda, k, kb, k + kb, c1, st, kind, tcw, 0));
+    GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
+    if (split) GBS_CUDA_TRY(cudaStreamWaitEvent(ws, la.ready, 0));
+    GBS_TRY(potrf_block(ss, n, As, lda, k + kb, nb1, st, kind, la.tc_side, minv));
+    GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
+    const int ctas = split ? la.wide_sms : 0;
+    GBS_TRY(potrf_syrk(ws, n, As, lda, k, kb, c1, n, st, kind, split ? la.tc_wide : tcw, ctas));
+    if (split) {
+      GBS_CUDA_TRY(cudaEventRecord(la.wide_done, ws));
+      wide_pending = true;
+    }
+  }
+  return GBS_SUCCESS;
+}
+
 int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st, int kind, TcWorkspace& tcw,
-                DevBuf& minv)
+                DevBuf& minv, Lookahead* la)
 {
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -813,33 +887,35 @@ int mixed_potrf(cudaStream_t s, int n, float* As, int64_t lda, DeviceStatus* st,
   }();
   GBS_CUDA_TRY(attr);
   int bs = n < 32 ? n : std::min(std::max((n / 8 / 16) * 16, 8), max_bs);
+  if (la && bs == kMixedNB && n > 2 * kMixedNB) {
+    GBS_TRY(la->init());
+    const int rc = potrf_lookahead(s, n, As, lda, bs, st, kind, tcw, *la);
+    if (rc != GBS_SUCCESS) {                    // nothing of the other streams outlives the call
+      cudaStreamSynchronize(la->side);
+      if (la->wide) cudaStreamSynchronize(la->wide);
+    }
+    return rc;
+  }
   for (int k = 0; k < n; k += bs) {
     const int b = std::min(bs, n - k);
     const int rs = n - k - b;
-    float* Akk = As + (int64_t)k * lda + k;
-    {
-      PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
-      potrf_diag_kernel<float><<<1, 256, potrf_diag_smem<float>(b), s>>>(Akk, lda, b, k, st);
-      GBS_CUDA_TRY(cudaGetLastError());
-    }
-    if (rs > 0) {
-      float* A21 = Akk + b;
-      if (b <= kMixedNB) {
-        // A21 L11^-T = A21 - A21 (I - L11^-T): W = I - L11^-1, read transposed as the GEMM's B
-        {
-          PhaseScope ps(s, PH_TRSM_LLT, (double)b * b * b / 3.0, 8.0 * b * b);
-          unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, b, minv.as<float>(), 0);
-          GBS_CUDA_TRY(cudaGetLastError());
-        }
-        GBS_TRY(tc_gemm_sub(s, kind, rs, b, b, A21, 1, lda, minv.as<float>(), kMixedNB, 1, A21, lda, 0, st, tcw));
-      } else {
-        PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, 8.0 * rs * b);
-        trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64 + b), s>>>(Akk, lda, b, A21,
-                                                                                                   lda, rs, st);
+    if (b <= kMixedNB) {
+      GBS_TRY(potrf_block(s, n, As, lda, k, b, st, kind, tcw, minv.as<float>()));
+    } else {
+      float* Akk = As + (int64_t)k * lda + k;
+      {
+        PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
+        potrf_diag_kernel<float><<<1, 256, potrf_diag_smem<float>(b), s>>>(Akk, lda, b, k, st);
         GBS_CUDA_TRY(cudaGetLastError());
       }
-      GBS_TRY(tc_gemm_sub(s, kind, rs, rs, b, A21, 1, lda, A21, lda, 1, A21 + (int64_t)b * lda, lda, 1, st, tcw));
+      if (rs > 0) {
+        PhaseScope ps(s, PH_TRSM_LLT, (double)rs * b * b, 8.0 * rs * b);
+        trsm_rlt_kernel<float, 64><<<cdiv(rs, 64), 64, sizeof(float) * (b * (b + 1) + b * 64 + b), s>>>(
+            Akk, lda, b, Akk + b, lda, rs, st);
+        GBS_CUDA_TRY(cudaGetLastError());
+      }
     }
+    if (rs > 0) GBS_TRY(potrf_syrk(s, n, As, lda, k, b, k + b, n, st, kind, tcw, 0));
   }
   return GBS_SUCCESS;
 }
@@ -1373,7 +1449,8 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
                                                                    w.a32.as<float>());
         GBS_CUDA_TRY(cudaGetLastError());
       }
-      GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc, w.minv));
+      GBS_TRY(mixed_potrf(s, n, w.a32.as<float>(), n, st, tc_kind(opt.tier), w.tc, w.minv,
+                          opt.lookahead ? &w.la : nullptr));
       DeviceStatus h;
       GBS_TRY(read_status(st, &h, s));
       out.shift = sigma;

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from eigen_gb300 import PartialPivLU, solve_mixed
+from eigen_gb300 import PartialPivLU, solve_mixed, solve_spd_mixed
 
 pytestmark = pytest.mark.gpu
 BAR = 1e-13
@@ -204,3 +204,17 @@ def test_tournament_pivoting_on_hard_panels():
         b = O.gauss(44, n, 2)
         x, info = solve_mixed(a, b, tier="tf32x3", pivoting="tournament")
         assert O.backward_error(a, x, b) <= BAR, info
+
+
+@pytest.mark.parametrize("tier", ["tf32x3", "fp16"])
+@pytest.mark.parametrize("n", [1500, 3000])
+def test_spd_lookahead_gives_identical_results(tier, n):
+    """The Cholesky's look-ahead schedule (block k+1's diagonal factor and
+    TRSM beside block k's wide SYRK) gives the single-stream results exactly."""
+    a = O.spd(900 + n, n)
+    b = O.gauss(901 + n, n, 2)
+    x1, i1 = solve_spd_mixed(a, b, tier=tier, lookahead=True)
+    x0, i0 = solve_spd_mixed(a, b, tier=tier, lookahead=False)
+    assert np.array_equal(x1, x0)
+    assert i1["iterations"] == i0["iterations"] and i1["fell_back"] == i0["fell_back"]
+    assert O.backward_error(a, x1, b) <= BAR
