@@ -66,8 +66,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Solves/s and TFLOP/s at ≤1e-13 backward err: mixed/batched vs plain FP64"
 BE_BAR = 1e-13
-# DRAM traffic / algorithmic bytes of one launch, from the ncu captures summarised in profiles/
-TRAFFIC_OVER_ALGORITHMIC = {"gemm": 533.6 / 588.4, "tc_gemm": 237.2 / 289.5}
+# DRAM traffic / algorithmic bytes of one launch, from the ncu captures summarised in profiles/ (the
+# panel's and the tcgen05 GEMM's captured at n = 6144, scaled by the bytes each launch processes)
+TRAFFIC_OVER_ALGORITHMIC = {"gemm": 533.6 / 588.4, "tc_gemm": 257.0 / 289.5, "panel": 1.17 / 1.56,
+                            "residual": 609.3 / 604.0}
 COMPANIONS = ("llt512", "llt16384", "batched", "router")
 
 
@@ -339,10 +341,14 @@ def phase_roofline(name, ph, step_s, note_latency=True):
              "achieved": ph["flops"] / t / 1e12 if t else 0.0, "peak": tf32_peak(), "unit": "TFLOP/s",
              "peak_source": "of measured: cuBLAS TF32 GEMM 8192^3 timed in this run",
              "note": "algorithmic flops 2 M N K; a 3xTF32 update issues three such products"}
-    elif name in ("gemm", "syrk", "residual", "batched"):
+    elif name == "residual":
+        e = {"bound": "hbm", "kernel": "oz_product_kernel (FP64-accurate r = b - A x on bf16 tcgen05, Ozaki "
+                                       "slices) + the slicing of A",
+             "achieved": ph["bytes"] / t / 1e9 if t else 0.0, "peak": measured_hbm_gbs(), "unit": "GB/s",
+             "peak_source": "of measured: MEASURED_PEAKS.json hbm_gbs"}
+    elif name in ("gemm", "syrk", "batched"):
         e = {"bound": "fp64", "kernel": {"gemm": "gemm_sub_kernel<double> (trailing update)",
                                          "syrk": "gemm_sub_kernel<double> lower (SYRK)",
-                                         "residual": "mv_partial_kernel (FP64 r = b - A x)",
                                          "batched": "batched LLT / LU kernels"}[name],
              "achieved": ph["flops"] / t / 1e12 if t else 0.0, "peak": fp64_peak(), "unit": "TFLOP/s",
              "peak_source": "of measured: cuBLAS DGEMM 8192^3 timed in this run (FP64 has no entry in "
@@ -1046,7 +1052,7 @@ def factor_once(args):
         ok = lu.first_zero_pivot() < 0
         out = {"first_zero_pivot": lu.first_zero_pivot()}
     else:
-        x, info = gb.solve_mixed(a, b, tier=args.path)
+        x, info = gb.solve_mixed(a, b, tier=args.path, lookahead=bool(args.lookahead))
         torch.cuda.synchronize()
         ok = info["backward_error"] <= BE_BAR
         out = info
