@@ -748,9 +748,8 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
         const int c = ag + q * G;
         if (ar < ni && c < nrhs) B[(int64_t)c * ldb + i0 + ar] = out[q];
       }
-      __threadfence();
       __syncthreads();
-      if (tid == 0) atomicExch(&flags[bi], 1);
+      if (tid == 0) st_release_u32((unsigned int*)&flags[bi], 1u);
       continue;
     }
     __syncthreads();
@@ -802,9 +801,8 @@ trsm_persistent_kernel(int n, int nrhs, const T* __restrict__ tri, int64_t rs, i
       const int r = e % NB, c = e / NB;
       if (r < ni && c < nrhs) B[(int64_t)c * ldb + i0 + r] = sY[r][c];
     }
-    __threadfence();
     __syncthreads();
-    if (tid == 0) atomicExch(&flags[bi], 1);
+    if (tid == 0) st_release_u32((unsigned int*)&flags[bi], 1u);
   }
 }
 

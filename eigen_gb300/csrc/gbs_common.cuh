@@ -55,6 +55,14 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
   return v;
 }
 
+// Release store at GPU scope: after a CTA barrier, it publishes the writes
+// every thread of the CTA made before the barrier (the barrier orders them
+// before this store, and release is cumulative).
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v)
+{
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ int ld_volatile_i32(const int* p)
 {
   return *(const volatile int*)p;
