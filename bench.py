@@ -500,18 +500,32 @@ def run_ours(args):
                 _lib.check(L.gbs_dgesv_mixed(n, nrhs, pa, n, pb, n, px, n, C.byref(opt), C.byref(einfo)),
                            "gbs_dgesv_mixed")
 
+        # the host link's rate for this buffer: one plain copy of A (not part of the measurement)
+        Ad = torch.empty_like(Ah, device="cuda")
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        Ad.copy_(Ah, non_blocking=True)
+        h0.record(stream)
+        Ad.copy_(Ah, non_blocking=True)
+        h1.record(stream)
+        torch.cuda.synchronize()
+        h2d_gbs = Ah.numel() * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
+        del Ad
         for _ in range(max(1, args.warmup)):
             e2e_step()
         torch.cuda.synchronize()
         barrier(world)
+        per_step = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ts = time.perf_counter()
             e2e_step()
+            per_step.append(time.perf_counter() - ts)
         torch.cuda.synchronize()
         t_e2e = max_over_ranks(world, time.perf_counter() - t0)
         be2 = backward_error_gpu(A, Xh.to("cuda").t(), B)
         e2e = {"value": (world * args.steps / t_e2e) if be2 <= BE_BAR else 0.0, "unit": "solves/s",
                "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs,
+               "ms_per_step_median": 1e3 * statistics.median(per_step), "h2d_gbs_of_A": h2d_gbs,
                "backward_error": be2,
                "api": ("gbs_dgesv_mixed" if args.path != "fp64" else "gbs_lu_compute + gbs_lu_solve") +
                       " on pinned host buffers"}

@@ -46,6 +46,7 @@ static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 // residual_reduce (deterministic).
 constexpr int kResRows = 128, kResRC = 16, kResKC = 64;
 constexpr int kMixedNB = 128;                  // outer block width of the mixed LU
+constexpr int kInflowMaxChunks = 16;           // column chunks of the streamed host input (LU)
 constexpr int kOzakiMinN = 1024;      // GBS_RESID_AUTO: tensor-core residuals from this order
 
 template <int RC>
@@ -410,6 +411,7 @@ struct Lookahead {
   cudaEvent_t ready = nullptr, panels = nullptr, inv = nullptr, wide_done = nullptr;
   TcWorkspace tc_side, tc_wide;
   DevBuf map_side, map[2], minv[2];
+  DevBuf minv_all, srcmap;   // streamed input: every block's I - L11^-1; the composed row map of a join
   int init()
   {
     if (!side) {
@@ -448,7 +450,7 @@ struct Lookahead {
 // slices of A), so that it runs beside the factorization.
 struct AuxStream {
   cudaStream_t s = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, norm = nullptr;
   bool pending = false;      // join recorded and not yet waited for
   int init()
   {
@@ -459,12 +461,44 @@ struct AuxStream {
     }
     if (!fork) GBS_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
     if (!join) GBS_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    if (!norm) GBS_CUDA_TRY(cudaEventCreateWithFlags(&norm, cudaEventDisableTiming));
+    return GBS_SUCCESS;
+  }
+  // the auxiliary stream starts after `ready`, or after what s has issued so far
+  int fork_from(cudaStream_t from, cudaEvent_t ready)
+  {
+    GBS_TRY(init());
+    if (!ready) {
+      GBS_CUDA_TRY(cudaEventRecord(fork, from));
+      ready = fork;
+    }
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, ready, 0));
     return GBS_SUCCESS;
   }
   ~AuxStream()
   {
+    if (norm) cudaEventDestroy(norm);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+// The copy stream of the streamed host input and one event per chunk.
+struct CopyLane {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev[kInflowMaxChunks] = {};
+  int init()
+  {
+    if (!s) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ev)
+      if (!e) GBS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return GBS_SUCCESS;
+  }
+  ~CopyLane()
+  {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
     if (s) cudaStreamDestroy(s);
   }
 };
@@ -472,14 +506,15 @@ struct AuxStream {
 struct MixedWork {
   cudaStream_t stream = nullptr;
   DevBuf a32, tr, st, scratch, r, part, w32, stats, rows, a64, map, d32, d64, afull, z, v, w, coef, perm, minv,
-      dinv;
+      dinv, npart;   // npart: the norm's partial sums (its stream may run beside the residuals')
   SolveWork sw;
   TcWorkspace tc;
   Lookahead la;
   OzakiMatrix oz;          // A's digit slices when the residuals run on the tensor cores
   OzakiWork ozw;
   AuxStream aux;
-  HostBuf hstats;
+  CopyLane copy;
+  HostBuf hstats, hrows;
 };
 
 static std::mutex g_mpool_mu;
@@ -641,6 +676,168 @@ diag_block_inverse_kernel(const float* __restrict__ A, int64_t lda, int n, int n
   }
 }
 
+// ------------------------------------------------------------------ streamed input
+// The host-buffer LU solve copies A over the host link in column chunks (one
+// cudaMemcpy2DAsync per chunk, on a copy stream), so that the factorization
+// starts on the first chunk while the others are still in flight: the link
+// moves about 210 GB/s, which makes A's transfer 2.6 ms of a 33 ms solve at
+// n = 8192.  Chunk 0 holds the first blocks.  The next chunks join the
+// look-ahead schedule at a planned iteration k, on the wide stream and before
+// that iteration's wide update: their FP64 columns are gathered into the FP32
+// working matrix through the interchanges of blocks 0..k-1 (composed into one
+// row map), then the trailing updates of blocks 0..k-1 are replayed on them in
+// block order.  The last chunk, the bulk of A, rolls in instead: after the
+// wide update of its landing iteration it is gathered through the
+// interchanges so far, and from then on it takes every iteration's
+// interchanges with the wide columns and, after each wide update, replays a
+// few of the updates it missed, in block order, in the wide stream's slack.
+// Once it has caught up it is part of the wide updates.  Either way the
+// result is the same as with every column present from the start: an
+// interchange only moves a row's values, the factored columns carry the
+// interchanges of their rows the same way, and each replayed update computes
+// every element from the same operands in the same order.
+constexpr int kInflowMinN = 2048;              // below this the copy is short next to its fixed costs
+constexpr int kInflowMaxN = (int)(kBlockMapSmemMax / (2 * sizeof(int)));   // the row map's shared memory
+constexpr int kInflowFirstBlocks = 4;          // chunk 0: the first four blocks
+constexpr int kInflowChunkBlocks = 8;          // chunks that join at once: eight blocks each
+constexpr int kInflowRollPerIteration = 2;     // updates the rolling chunk replays after each wide update
+// Planning figures, as measured at n = 8192: the link's rate and the length
+// of one look-ahead iteration.
+constexpr double kInflowLinkBytesPerUs = 200e3;
+constexpr double kInflowIterationUs = 450.0;
+
+struct Inflow {
+  const double* host = nullptr;        // column-major n x n source, leading dimension ldh
+  int64_t ldh = 0;
+  double* dev = nullptr;               // its FP64 device copy (the refinement's A), leading dimension ldd
+  int64_t ldd = 0;
+  int chunks = 0;
+  int col[kInflowMaxChunks + 1] = {};  // chunk j holds the columns [col[j], col[j + 1])
+  int iter[kInflowMaxChunks] = {};     // look-ahead iteration at which chunk j joins (rolling: is gathered)
+  int rolling = -1;                    // the rolling chunk (the last one), or -1
+  cudaEvent_t arrived[kInflowMaxChunks] = {};
+};
+
+// Chunks and iterations for order n (n >= kInflowMinN).  A chunk whose first
+// block is b must be in the wide updates by iteration b - 2: iteration b - 1's
+// narrow update works on block b.  The rolling chunk, gathered at iteration
+// g with blocks 0..g already applied, has replayed R (k - g) blocks when
+// iteration k starts, so it is in from iteration ceil(R g / (R - 1)).
+static void plan_inflow(int n, Inflow& in)
+{
+  const int nblk = cdiv(n, kMixedNB);
+  const double bytes_per_col = sizeof(double) * (double)n;
+  auto landed = [&](int col) { return col * bytes_per_col / kInflowLinkBytesPerUs; };
+  const double t0 = landed(std::min(n, kInflowFirstBlocks * kMixedNB));
+  // iteration k's wide update starts near t0 + (k + 1) kInflowIterationUs
+  auto first_after = [&](double t) { return std::max(0, (int)std::ceil((t - t0) / kInflowIterationUs) - 1); };
+  const int R = kInflowRollPerIteration;
+  const int g = first_after(landed(n));
+  const int ready = std::max(g + 1, cdiv((int64_t)R * g, R - 1));
+  const int roll_block = ready + 2;            // the rolling chunk's first block
+  in.col[0] = 0;
+  in.chunks = 1;
+  in.rolling = -1;
+  int c = std::min(n, kInflowFirstBlocks * kMixedNB);
+  const int at_once_end = roll_block + kInflowChunkBlocks <= nblk ? roll_block * kMixedNB : n;
+  // at least eight blocks a chunk, and few enough chunks to leave one for the rolling chunk
+  const int per = std::max(kInflowChunkBlocks, cdiv(cdiv(at_once_end - c, kMixedNB), kInflowMaxChunks - 2)) * kMixedNB;
+  while (c < at_once_end) {
+    in.col[in.chunks++] = c;
+    c = std::min(at_once_end, c + per);
+  }
+  if (c < n) {                                 // the rest rolls
+    in.rolling = in.chunks;
+    in.col[in.chunks++] = c;
+  }
+  in.col[in.chunks] = n;
+  in.iter[0] = 0;
+  for (int j = 1; j < in.chunks; ++j) {
+    if (j == in.rolling) {
+      in.iter[j] = std::max(g, in.iter[j - 1]);
+    } else {
+      in.iter[j] = std::min(first_after(landed(in.col[j + 1])), in.col[j] / kMixedNB - 2);
+    }
+  }
+  const int last_at_once = in.rolling >= 0 ? in.rolling - 1 : in.chunks - 1;
+  for (int j = last_at_once - 1; j >= 1; --j) in.iter[j] = std::min(in.iter[j], in.iter[j + 1]);
+}
+
+// The source row of every row of [0, n) after the interchanges tr[0, i1),
+// applied in order: one thread replays them on a map in shared memory (the
+// transpositions staged beside it), then the map is written out whole.
+__global__ void __launch_bounds__(1024)
+row_source_map_kernel(const int* __restrict__ tr, int i1, int n, int* __restrict__ src)
+{
+  extern __shared__ int smap[];
+  int* s_src = smap;            // [n]
+  int* s_tr = smap + n;         // [i1]
+  for (int r = threadIdx.x; r < n; r += blockDim.x) s_src[r] = r;
+  for (int i = threadIdx.x; i < i1; i += blockDim.x) s_tr[i] = tr[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < i1; ++i) {
+      const int p = s_tr[i];
+      if (p > i && p < n) {
+        const int t = s_src[i];
+        s_src[i] = s_src[p];
+        s_src[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) src[r] = s_src[r];
+}
+
+// out(r, c) = (float) a(src[r], c) for an m x nc block (src null: the
+// identity).  Grid (row groups of 256, columns).
+__global__ void __launch_bounds__(256)
+gather_rows_f32_kernel(const double* __restrict__ a, int64_t lda, const int* __restrict__ src,
+                       float* __restrict__ out, int64_t ldo, int m)
+{
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  const int64_t c = blockIdx.y;
+  out[c * ldo + r] = (float)a[c * lda + (src ? src[r] : r)];
+}
+
+static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int kb, int c0, int c1,
+                        const float* minv, DeviceStatus* st, int kind, TcWorkspace& tcw, int max_ctas);
+
+// Chunk j on stream ws (see the section comment): gathered through the
+// interchanges of blocks 0..swapped-1, then the updates of blocks
+// 0..replay-1 replayed on it.
+static int inflow_join(cudaStream_t ws, int n, float* A, int64_t lda, const int* tr, const Inflow& in, int j,
+                       int swapped, int replay, const float* minv_all, DevBuf& srcmap, DeviceStatus* st, int kind,
+                       TcWorkspace& tcw, int max_ctas)
+{
+  const int c0 = in.col[j], nc = in.col[j + 1] - c0;
+  GBS_CUDA_TRY(cudaStreamWaitEvent(ws, in.arrived[j], 0));
+  const int* map = nullptr;
+  const int i1 = std::min(n, swapped * kMixedNB);
+  if (i1 > 0) {
+    const size_t smem = sizeof(int) * ((size_t)n + i1);
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        row_source_map_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBlockMapSmemMax);
+    GBS_CUDA_TRY(attr);
+    GBS_TRY(srcmap.reserve(sizeof(int) * (size_t)n));
+    PhaseScope ps(ws, PH_LASWP, 0.0, sizeof(int) * (2.0 * n + i1));
+    row_source_map_kernel<<<1, 1024, smem, ws>>>(tr, i1, n, srcmap.as<int>());
+    GBS_CUDA_TRY(cudaGetLastError());
+    map = srcmap.as<int>();
+  }
+  {
+    PhaseScope ps(ws, PH_COPY, 0.0, 12.0 * (double)n * nc);
+    gather_rows_f32_kernel<<<dim3(cdiv(n, 256), nc), 256, 0, ws>>>(in.dev + (int64_t)c0 * in.ldd, in.ldd, map,
+                                                                 A + (int64_t)c0 * lda, lda, n);
+    GBS_CUDA_TRY(cudaGetLastError());
+  }
+  for (int b = 0; b < replay; ++b)
+    GBS_TRY(block_update(ws, n, A, lda, b * kMixedNB, kMixedNB, c0, c0 + nc,
+                         minv_all + (size_t)b * kMixedNB * kMixedNB, st, kind, tcw, max_ctas));
+  return GBS_SUCCESS;
+}
+
 // Panels of the outer block [k, k+kb): each 32-column panel, its row
 // interchanges and the block-internal update of the block's columns right of
 // it.  defer: the interchanges are applied inside the block only, and the
@@ -708,31 +905,50 @@ static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int
 //         update of block k+1's columns (narrow)
 //     ss: wait for the narrow update; panels of block k+1, then its I - L11^-1
 //         (it overlaps the interchanges on s)
-//     ws: wait for the narrow update; block k's interchanges on the other
-//         columns; update of the columns right of block k+1 (wide)
+//     ws: wait for the narrow update; the streamed chunks that join at
+//         iteration k (in != null); block k's interchanges on the other
+//         columns; update of the columns right of block k+1 (wide), up to
+//         the last joined chunk; then the rolling chunk's gather and replays
 // The row maps and L11 inverses alternate between two buffers by block, so
-// that s never rewrites one that ws may still read.  Every element sees the
+// that s never rewrites one that ws may still read (with streamed input every
+// block keeps its inverse, which the joins replay).  Every element sees the
 // same operations in the same order as in the plain schedule, so both give
 // identical factors and interchanges.
 static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch,
-                           int kind, TcWorkspace& tcw, Lookahead& la, bool tournament)
+                           int kind, TcWorkspace& tcw, Lookahead& la, bool tournament, const Inflow* in)
 {
   cudaStream_t ss = la.side;
   const bool split = la.wide != nullptr;
   cudaStream_t ws = split ? la.wide : s;
+  const int nblk = cdiv(n, kMixedNB);
+  if (in) GBS_TRY(la.minv_all.reserve(sizeof(float) * (size_t)nblk * kMixedNB * kMixedNB));
+  auto minv_of = [&](int blk) -> float* {
+    return in ? la.minv_all.as<float>() + (size_t)blk * kMixedNB * kMixedNB : la.minv[blk & 1].as<float>();
+  };
+  int joined = 1;                              // chunks in the schedule (chunk 0 from the start)
+  int frontier = in ? in->col[1] : n;          // columns [0, frontier) take the wide updates
+  int gathered = frontier;                     // columns [0, gathered) take the interchanges
+  const int at_once = in ? (in->rolling >= 0 ? in->rolling : in->chunks) : 1;
+  bool rolled_in = in == nullptr || in->rolling < 0;
+  int replayed = -1;                           // blocks the rolling chunk has taken (-1: not gathered)
+  // without a partition, the panel's cluster and its small kernels keep two
+  // clusters' worth of SMs from the wide update's persistent grid
+  auto wide_ctas = [&](int rows) {
+    return split ? la.wide_sms : device_sm_count() - std::min(2 * panel_cluster_ctas(rows), device_sm_count() / 2);
+  };
   GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
   GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
   GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, 0, std::min(kMixedNB, n), true,
                        tournament));
   GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
-  if (n > kMixedNB) GBS_TRY(block_inverse(ss, A, lda, 0, kMixedNB, la.minv[0].as<float>()));
+  if (n > kMixedNB) GBS_TRY(block_inverse(ss, A, lda, 0, kMixedNB, minv_of(0)));
   GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
   bool wide_pending = false;
   for (int k = 0, blk = 0; k < n; k += kMixedNB, ++blk) {
     const int kb = std::min(kMixedNB, n - k);
     const int nr = n - k - kb;
     DevBuf& mapk = la.map[blk & 1];
-    float* minv = la.minv[blk & 1].as<float>();
+    float* minv = minv_of(blk);
     GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.panels, 0));
     if (wide_pending) GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.wide_done, 0));
     if (nr == 0) {
@@ -740,6 +956,10 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
       break;
     }
     const int nb1 = std::min(kMixedNB, nr), c1 = k + kb + nb1;
+    if (frontier < c1) {
+      gbs_set_last_message("streamed input: a chunk joins after its columns are needed");
+      return GBS_INVALID_ARGUMENT;
+    }
     // the interchanges on block k+1's columns gate its panels; the left and
     // wide columns get them (same map) while those panels run
     GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, mapk));
@@ -750,24 +970,46 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
     if (split) GBS_CUDA_TRY(cudaStreamWaitEvent(ws, la.ready, 0));
     GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, k + kb, nb1, true, tournament));
     GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
-    if (c1 < n) GBS_TRY(block_inverse(ss, A, lda, k + kb, nb1, la.minv[(blk + 1) & 1].as<float>()));
+    if (c1 < n) GBS_TRY(block_inverse(ss, A, lda, k + kb, nb1, minv_of(blk + 1)));
     GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
-    GBS_TRY(laswp_map_apply<float>(ws, A, lda, mapk.as<int>(), 0, k, c1, n));
-    // without a partition, the panel's cluster and its small kernels keep two
-    // clusters' worth of SMs from the wide update's persistent grid
-    const int ctas = split ? la.wide_sms
-                           : device_sm_count() - std::min(2 * panel_cluster_ctas(nr), device_sm_count() / 2);
-    GBS_TRY(block_update(ws, n, A, lda, k, kb, c1, n, minv, st, kind, split ? la.tc_wide : tcw, ctas));
+    for (; joined < at_once && in->iter[joined] <= blk; ++joined) {
+      GBS_TRY(inflow_join(ws, n, A, lda, tr, *in, joined, blk, blk, la.minv_all.as<float>(), la.srcmap, st, kind,
+                          split ? la.tc_wide : tcw, wide_ctas(nr)));
+      frontier = gathered = in->col[joined + 1];
+    }
+    if (!rolled_in && replayed == blk) {       // the rolling chunk has caught up
+      rolled_in = true;
+      frontier = in->col[in->rolling + 1];
+      joined = in->chunks;
+    }
+    GBS_TRY(laswp_map_apply<float>(ws, A, lda, mapk.as<int>(), 0, k, c1, std::max(c1, gathered)));
+    GBS_TRY(block_update(ws, n, A, lda, k, kb, c1, frontier, minv, st, kind, split ? la.tc_wide : tcw, wide_ctas(nr)));
     if (split) {
       GBS_CUDA_TRY(cudaEventRecord(la.wide_done, ws));
       wide_pending = true;
     }
+    // the rolling chunk works after the wide update's event, so that the next
+    // narrow update does not wait for it
+    if (!rolled_in && replayed < 0 && joined == at_once && in->iter[in->rolling] <= blk) {
+      GBS_TRY(inflow_join(ws, n, A, lda, tr, *in, in->rolling, blk + 1, 0, la.minv_all.as<float>(), la.srcmap, st,
+                          kind, split ? la.tc_wide : tcw, wide_ctas(nr)));
+      replayed = 0;
+      gathered = in->col[in->rolling + 1];
+    }
+    for (int q = 0; !rolled_in && replayed >= 0 && q < kInflowRollPerIteration && replayed <= blk; ++q, ++replayed)
+      GBS_TRY(block_update(ws, n, A, lda, replayed * kMixedNB, kMixedNB, in->col[in->rolling], in->col[in->rolling + 1],
+                           la.minv_all.as<float>() + (size_t)replayed * kMixedNB * kMixedNB, st, kind,
+                           split ? la.tc_wide : tcw, wide_ctas(nr)));
+  }
+  if (in && (joined < in->chunks || !rolled_in)) {
+    gbs_set_last_message("streamed input: a chunk never joined the schedule");
+    return GBS_INVALID_ARGUMENT;
   }
   return GBS_SUCCESS;
 }
 
 int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceStatus* st, DevBuf& scratch, int kind,
-                TcWorkspace& tcw, DevBuf& map, DevBuf& minv, Lookahead* la, bool tournament)
+                TcWorkspace& tcw, DevBuf& map, DevBuf& minv, Lookahead* la, bool tournament, const Inflow* in)
 {
   GBS_TRY(minv.reserve(sizeof(float) * kMixedNB * kMixedNB));
   GBS_CUDA_TRY(cudaFuncSetAttribute(unit_lower_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -776,7 +1018,7 @@ int mixed_getrf(cudaStream_t s, int n, float* A, int64_t lda, int* tr, DeviceSta
                                     (int)kInvSmem));
   if (la && n > kMixedNB) {
     GBS_TRY(la->init());
-    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, *la, tournament);
+    const int rc = getrf_lookahead(s, n, A, lda, tr, st, scratch, kind, tcw, *la, tournament, in);
     if (rc != GBS_SUCCESS) {                    // nothing of the other streams outlives the call
       cudaStreamSynchronize(la->side);
       if (la->wide) cudaStreamSynchronize(la->wide);
@@ -972,14 +1214,14 @@ static int precond_apply(cudaStream_t s, const Precond& M, float* W, int nrhs, S
 // Slices A for the tensor-core residuals when the options ask for them, on
 // the auxiliary stream (joined by the first residual, and by AuxJoin at the
 // end of the call whatever path it took).
-static int prepare_residual(cudaStream_t s, const Problem& P, int mode, MixedWork& w)
+// ready: A is complete in device memory after this event (null: after the
+// work issued on s so far).
+static int prepare_residual(cudaStream_t s, const Problem& P, int mode, MixedWork& w, cudaEvent_t ready = nullptr)
 {
   w.oz.ready = false;
   const bool oz = mode == GBS_RESID_OZAKI || (mode == GBS_RESID_AUTO && P.n >= kOzakiMinN);
   if (!oz || P.sym) return GBS_SUCCESS;        // the residuals of a lower-stored A stay on FP64 FMA
-  GBS_TRY(w.aux.init());
-  GBS_CUDA_TRY(cudaEventRecord(w.aux.fork, s));
-  GBS_CUDA_TRY(cudaStreamWaitEvent(w.aux.s, w.aux.fork, 0));
+  GBS_TRY(w.aux.fork_from(s, ready));
   w.aux.pending = true;
   const int rc = w.oz.prepare(w.aux.s, P.n, P.A, P.lda);
   GBS_CUDA_TRY(cudaEventRecord(w.aux.join, w.aux.s));
@@ -1224,7 +1466,11 @@ static int reserve_common(MixedWork& w, int n, int nrhs)
   return GBS_SUCCESS;
 }
 
-static int inf_norm(cudaStream_t s, const Problem& P, MixedWork& w, double* anorm)
+// ||A||_inf in two steps, so that the factorization is issued without waiting
+// for it: norm_start puts the row sums on stream s (the auxiliary stream for
+// the LU, beside the factorization) with their copy to pinned host memory;
+// norm_wait waits for that copy and takes the maximum.
+static int norm_start(cudaStream_t s, const Problem& P, MixedWork& w)
 {
   const int rblocks = cdiv(P.n, 256);
   const int splits = P.sym ? 1 : std::max(1, std::min(cdiv(P.n, 64), 4 * device_sm_count() / rblocks));
@@ -1234,20 +1480,34 @@ static int inf_norm(cudaStream_t s, const Problem& P, MixedWork& w, double* anor
   } else {
     const int kspan = cdiv(P.n, splits);
     const int used = cdiv(P.n, kspan);
-    GBS_TRY(w.part.reserve(sizeof(double) * (size_t)used * P.n));
+    GBS_TRY(w.npart.reserve(sizeof(double) * (size_t)used * P.n));
     count_launch();
-    row_abs_partial_kernel<<<dim3(rblocks, used), 256, 0, s>>>(P.n, P.A, P.lda, kspan, w.part.as<double>());
+    row_abs_partial_kernel<<<dim3(rblocks, used), 256, 0, s>>>(P.n, P.A, P.lda, kspan, w.npart.as<double>());
     count_launch();
-    row_abs_reduce_kernel<<<rblocks, 256, 0, s>>>(P.n, used, w.part.as<double>(), w.rows.as<double>());
+    row_abs_reduce_kernel<<<rblocks, 256, 0, s>>>(P.n, used, w.npart.as<double>(), w.rows.as<double>());
   }
   GBS_CUDA_TRY(cudaGetLastError());
-  std::vector<double> h((size_t)P.n);
-  GBS_CUDA_TRY(cudaMemcpyAsync(h.data(), w.rows.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
-  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  GBS_TRY(w.aux.init());
+  GBS_TRY(w.hrows.reserve(sizeof(double) * (size_t)P.n));
+  GBS_CUDA_TRY(cudaMemcpyAsync(w.hrows.p, w.rows.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaEventRecord(w.aux.norm, s));
+  return GBS_SUCCESS;
+}
+
+static int norm_wait(MixedWork& w, int n, double* anorm)
+{
+  GBS_CUDA_TRY(cudaEventSynchronize(w.aux.norm));
+  const double* h = static_cast<const double*>(w.hrows.p);
   double a = 0;
-  for (double v : h) a = std::max(a, v);
+  for (int i = 0; i < n; ++i) a = std::max(a, h[i]);
   *anorm = a;
   return GBS_SUCCESS;
+}
+
+static int inf_norm(cudaStream_t s, const Problem& P, MixedWork& w, double* anorm)
+{
+  GBS_TRY(norm_start(s, P, w));
+  return norm_wait(w, P.n, anorm);
 }
 
 // x0 = M^-1 b
@@ -1289,8 +1549,20 @@ static int per_group(int nrhs, MixedResult* res, Fn fn)
 }
 
 // ------------------------------------------------------------------ LU front end
-int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
-                   double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
+// Nothing of the copy stream outlives the call that issued it.
+struct CopyJoin {
+  cudaStream_t s;
+  explicit CopyJoin(cudaStream_t s_) : s(s_) {}
+  ~CopyJoin()
+  {
+    if (s) cudaStreamSynchronize(s);
+  }
+};
+
+// in != null: A (n x n, ld lda) is filled from the host by the streamed
+// input, and in->dev == A.
+static int lu_solve_impl(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
+                         double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res, Inflow* in)
 {
   MixedResult out;
   out.tier = opt.tier;
@@ -1298,10 +1570,12 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
     if (res) *res = out;
     return GBS_SUCCESS;
   }
-  if (nrhs > kResRC)
+  if (nrhs > kResRC) {
+    if (in) return GBS_INVALID_ARGUMENT;       // streamed input carries at most one group
     return per_group(nrhs, res, [&](int c0, int nc, MixedResult* r) {
       return mixed_lu_solve(s, n, nc, A, lda, B + (int64_t)c0 * ldb, ldb, X + (int64_t)c0 * ldx, ldx, opt, r);
     });
+  }
   MixedLease lease;
   if (lease.status != GBS_SUCCESS) return lease.status;
   MixedWork& w = *lease.w;
@@ -1310,22 +1584,44 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
   GBS_TRY(w.tr.reserve(sizeof(int) * (size_t)n));
   DeviceStatus* st = w.st.as<DeviceStatus>();
   Problem P{n, nrhs, A, lda, 0, B, ldb, X, ldx};
-  double anorm = 0;
-  GBS_TRY(inf_norm(s, P, w, &anorm));
+  cudaEvent_t complete = nullptr;              // A is whole in device memory after this event (null: on entry)
+  if (in) GBS_TRY(w.copy.init());
+  CopyJoin copy_join(in ? w.copy.s : nullptr);
+  if (in) {
+    for (int j = 0; j < in->chunks; ++j) {
+      const int c0 = in->col[j], nc = in->col[j + 1] - c0;
+      GBS_CUDA_TRY(cudaMemcpy2DAsync(in->dev + (int64_t)c0 * in->ldd, sizeof(double) * in->ldd,
+                                     in->host + (int64_t)c0 * in->ldh, sizeof(double) * in->ldh, sizeof(double) * n,
+                                     nc, cudaMemcpyHostToDevice, w.copy.s));
+      in->arrived[j] = w.copy.ev[j];
+      GBS_CUDA_TRY(cudaEventRecord(in->arrived[j], w.copy.s));
+    }
+    complete = in->arrived[in->chunks - 1];
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, in->arrived[0], 0));
+  }
+  // ||A||_inf and A's digit slices on the auxiliary stream, beside the factorization
   AuxJoin aux_join(w);
-  GBS_TRY(prepare_residual(s, P, opt.residual, w));
+  GBS_TRY(w.aux.fork_from(s, complete));
+  GBS_TRY(norm_start(w.aux.s, P, w));
+  GBS_CUDA_TRY(cudaEventRecord(w.aux.join, w.aux.s));
+  w.aux.pending = true;
+  GBS_TRY(prepare_residual(s, P, opt.residual, w, complete));
+  double anorm = -1;
+  auto need_anorm = [&]() -> int { return anorm < 0 ? norm_wait(w, n, &anorm) : GBS_SUCCESS; };
   bool converged = false;
   if (opt.tier != GBS_TIER_FP64) {
     GBS_TRY(reset_status(st, s));
     {
-      PhaseScope ps(s, PH_COPY, 0.0, 12.0 * (double)n * n);
-      copy_matrix_kernel<double, float><<<std::min<int64_t>(cdiv((int64_t)n * n, 256), 65535 * 8), 256, 0, s>>>(
-          A, lda, w.a32.as<float>(), n, n, n);
+      const int nc = in ? in->col[1] : n;      // streamed input: the later chunks join inside the factorization
+      PhaseScope ps(s, PH_COPY, 0.0, 12.0 * (double)n * nc);
+      copy_matrix_kernel<double, float><<<std::min<int64_t>(cdiv((int64_t)n * nc, 256), 65535 * 8), 256, 0, s>>>(
+          A, lda, w.a32.as<float>(), n, n, nc);
       GBS_CUDA_TRY(cudaGetLastError());
     }
     GBS_TRY(mixed_getrf(s, n, w.a32.as<float>(), n, w.tr.as<int>(), st, w.scratch, tc_kind(opt.tier), w.tc, w.map,
                         w.minv, opt.lookahead ? &w.la : nullptr,
-                        opt.pivoting == GBS_PIVOT_TOURNAMENT));
+                        opt.pivoting == GBS_PIVOT_TOURNAMENT, in));
+    if (complete) GBS_CUDA_TRY(cudaStreamWaitEvent(s, complete, 0));
     DeviceStatus h;
     GBS_TRY(read_status(st, &h, s));
     if (h.info < 0) {
@@ -1358,12 +1654,14 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
       GBS_TRY(initial_solve(s, P, M, w));
       const bool gm = opt.refine == GBS_REFINE_GMRES || (opt.refine == GBS_REFINE_AUTO && opt.tier != GBS_TIER_TF32X3);
       out.solver = gm ? GBS_REFINE_GMRES : GBS_REFINE_CLASSIC;
+      GBS_TRY(need_anorm());
       GBS_TRY(refine(s, P, M, gm, opt, anorm, w, out, &converged));
     }
   }
   if (!converged) {
     out.fell_back = opt.tier != GBS_TIER_FP64;
     out.tier = GBS_TIER_FP64;
+    if (complete) GBS_CUDA_TRY(cudaStreamWaitEvent(s, complete, 0));
     GBS_TRY(w.a64.reserve(sizeof(double) * (size_t)n * n));
     GBS_TRY(copy_matrix_device<double>(s, A, lda, w.a64.as<double>(), n, n, n));
     GBS_TRY(reset_status(st, s));
@@ -1372,11 +1670,37 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
     GBS_TRY(read_status(st, &h, s));
     GBS_TRY(copy_matrix_device<double>(s, B, ldb, X, ldx, n, nrhs));
     GBS_TRY(lu_solve_device<double>(s, n, nrhs, w.a64.as<double>(), n, w.tr.as<int>(), X, ldx, 0, w.sw));
+    GBS_TRY(need_anorm());
     GBS_TRY(backward_error(s, P, anorm, w, &out.backward_error));
     if (h.info >= 0) out.singular = 1;
   }
   if (res) *res = out;
   return GBS_SUCCESS;
+}
+
+int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
+                   double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
+{
+  return lu_solve_impl(s, n, nrhs, A, lda, B, ldb, X, ldx, opt, res, nullptr);
+}
+
+int mixed_lu_solve_host(cudaStream_t s, int n, int nrhs, const double* a, int64_t lda, double* dA, const double* B,
+                        int64_t ldb, double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res)
+{
+  const bool streamed = n >= kInflowMinN && n <= kInflowMaxN && nrhs <= kResRC && opt.tier != GBS_TIER_FP64 &&
+                        opt.lookahead;
+  if (!streamed) {
+    GBS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
+                                   cudaMemcpyHostToDevice, s));
+    return lu_solve_impl(s, n, nrhs, dA, n, B, ldb, X, ldx, opt, res, nullptr);
+  }
+  Inflow in;
+  in.host = a;
+  in.ldh = lda;
+  in.dev = dA;
+  in.ldd = n;
+  plan_inflow(n, in);
+  return lu_solve_impl(s, n, nrhs, dA, n, B, ldb, X, ldx, opt, res, &in);
 }
 
 int residual_device(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* X, int64_t ldx,

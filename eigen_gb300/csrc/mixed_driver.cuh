@@ -41,5 +41,13 @@ int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda
                    double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
 int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,
                     double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
+// mixed_lu_solve with A in host memory (column-major, leading dimension lda):
+// dA (n x n, leading dimension n) receives it.  For n in [2048, 20480] with up
+// to 16 right-hand sides and look-ahead on, A crosses in column chunks that
+// the factorization takes in as they land; otherwise in one copy first.  The
+// results are identical to mixed_lu_solve's on the same A.  B and X are
+// device buffers.
+int mixed_lu_solve_host(cudaStream_t s, int n, int nrhs, const double* a, int64_t lda, double* dA, const double* B,
+                        int64_t ldb, double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
 
 }  // namespace gbs

@@ -166,6 +166,47 @@ def test_lookahead_gives_identical_results(tier, n):
 
 
 @pytest.mark.parametrize("tier", ["tf32x3", "bf16"])
+@pytest.mark.parametrize("n", [2048, 3000, 8192])
+def test_streamed_host_input_matches_device_buffers(tier, n):
+    """From host buffers the LU solve copies A in column chunks that join the
+    look-ahead factorization as they land: each late chunk is gathered through
+    the interchanges so far, then the earlier blocks' updates are replayed on
+    it.  The solution must be bit-identical to the device-buffer solve."""
+    torch = pytest.importorskip("torch")
+    a = O.gauss(700 + n, n, n)
+    b = O.gauss(800 + n, n, 3)
+    xh, ih = solve_mixed(a, b, tier=tier)
+    A = torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
+    B = torch.from_numpy(np.ascontiguousarray(b.T)).cuda().t()
+    xd, idv = solve_mixed(A, B, tier=tier)
+    assert np.array_equal(xh, xd.cpu().numpy())
+    assert (ih["iterations"], ih["fell_back"]) == (idv["iterations"], idv["fell_back"])
+    assert O.backward_error(a, xh, b) <= BAR
+
+
+def test_streamed_host_input_with_padded_leading_dimension():
+    """A host matrix with lda > n: every chunk's copy strides over the padding."""
+    import ctypes as C
+    from eigen_gb300 import _lib
+    from eigen_gb300.mixed import RefineInfo, options
+    n, pad, nrhs = 3000, 7, 2
+    a = O.gauss(901, n, n)
+    b = O.gauss(902, n, nrhs)
+    ah = np.full((n, n + pad), np.nan)                 # row-major (n, lda): column-major A with lda = n + pad
+    ah[:, :n] = a.T
+    bh = np.asfortranarray(b)
+    x = np.empty((n, nrhs), order="F")
+    info = RefineInfo()
+    opt = options("tf32x3")
+    _lib.check(_lib.lib().gbs_dgesv_mixed(n, nrhs, ah.ctypes.data_as(C.c_void_p), n + pad,
+                                          bh.ctypes.data_as(C.c_void_p), n, x.ctypes.data_as(C.c_void_p), n,
+                                          C.byref(opt), C.byref(info)), "gbs_dgesv_mixed")
+    x0, _ = solve_mixed(a, b, tier="tf32x3")
+    assert np.array_equal(x, x0)
+    assert O.backward_error(a, x, b) <= BAR
+
+
+@pytest.mark.parametrize("tier", ["tf32x3", "bf16"])
 @pytest.mark.parametrize("n", [600, 2048, 5000])
 def test_tournament_and_partial_pivoting_both_converge(tier, n):
     """Tournament pivoting (an option of the mixed LU's panels) against the
