@@ -235,56 +235,6 @@ __device__ __forceinline__ float round_tf32(float x)
   return __uint_as_float(r);
 }
 
-// out[r * ldk + k] (K-major) from src(r, k) = src[r*rs + k*cs], r < R, k < K,
-// converted to the tier's type; x3 tiers write three K-blocks per row with
-// `pattern` selecting hi (0) or lo (1) for each block.  Zero padding up to Kp.
-template <typename TO>
-__device__ __forceinline__ void pack_kmajor_tile(const float* __restrict__ src, int64_t rs, int64_t cs, int R, int K,
-                                                 int Kp, TO* __restrict__ out, int64_t ldk, int kind, int pattern)
-{
-  __shared__ float tile[32][33];
-  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
-  if (r0 >= R) return;                       // uniform over the CTA
-  const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
-  const int nblk = (kind == TC_TF32X3) ? 3 : 1;
-  const int Kt = K * nblk;
-  // load a 32 (r) x 32 (source k) tile; threads run along the unit-stride dimension
-  const int kb0 = k0 % (K > 0 ? K : 1);
-  (void)kb0;
-  for (int yy = ty; yy < 32; yy += 8) {
-    int r, k;
-    if (rs == 1) { r = r0 + tx; k = k0 + yy; }
-    else { r = r0 + yy; k = k0 + tx; }
-    float v = 0.f;
-    const int ks = (nblk == 1) ? k : (K > 0 ? k % K : 0);
-    if (r < R && k < Kt) v = src[(int64_t)r * rs + (int64_t)ks * cs];
-    if (rs == 1) tile[tx][yy] = v;
-    else tile[yy][tx] = v;
-  }
-  __syncthreads();
-  for (int yy = ty; yy < 32; yy += 8) {
-    const int r = r0 + yy, k = k0 + tx;
-    if (r >= R || k >= Kp) continue;
-    float v = tile[yy][tx];
-    float o = 0.f;
-    if (k < Kt) {
-      if (kind == TC_TF32X3) {
-        const int blk = k / K;
-        const int lo = (pattern >> blk) & 1;
-        const float hi = round_tf32(v);
-        o = lo ? round_tf32(v - hi) : hi;
-      } else if (kind == TC_TF32) {
-        o = round_tf32(v);
-      } else {
-        o = v;
-      }
-    }
-    if constexpr (sizeof(TO) == 4) out[(int64_t)r * ldk + k] = o;
-    else if (kind == TC_BF16) ((__nv_bfloat16*)out)[(int64_t)r * ldk + k] = __float2bfloat16_rn(o);
-    else ((__half*)out)[(int64_t)r * ldk + k] = __float2half_rn(o);
-  }
-}
-
 struct PackJob {
   const float* src;
   int64_t rs, cs;
@@ -292,13 +242,62 @@ struct PackJob {
   int pattern;
 };
 
-// Both operands in one launch: blockIdx.z picks A (0) or B (1).
+// out[r * ldk + blk * K + k] (K-major) from src(r, k) = src[r*rs + k*cs],
+// r < R, k < K, converted to the tier's type; x3 tiers write three K-blocks
+// per row, `pattern` selecting hi (0) or lo (1) for each block.  Zero padding
+// from nblk K up to Kp.  One CTA per 32-row tile of A (the first tiles_a
+// CTAs) or of B: it walks the source K in 32-wide slices staged in shared
+// memory (loads along the source's unit stride), reading each element once
+// and writing every block's copy of it.
 template <typename TO>
-__global__ void pack_pair_kernel(PackJob a, PackJob b, int K, int Kp, TO* __restrict__ outa, TO* __restrict__ outb,
-                                 int64_t ldk, int kind)
+__global__ void __launch_bounds__(256)
+pack_pair_kernel(PackJob a, PackJob b, int tiles_a, int K, int Kp, TO* __restrict__ outa, TO* __restrict__ outb,
+                 int64_t ldk, int kind)
 {
-  if (blockIdx.z == 0) pack_kmajor_tile<TO>(a.src, a.rs, a.cs, a.R, K, Kp, outa, ldk, kind, a.pattern);
-  else pack_kmajor_tile<TO>(b.src, b.rs, b.cs, b.R, K, Kp, outb, ldk, kind, b.pattern);
+  __shared__ float tile[32][33];
+  const bool on_b = (int)blockIdx.x >= tiles_a;
+  const PackJob j = on_b ? b : a;
+  TO* __restrict__ out = on_b ? outb : outa;
+  const int r0 = (on_b ? (int)blockIdx.x - tiles_a : (int)blockIdx.x) * 32;
+  if (r0 >= j.R) return;                     // uniform over the CTA
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  const int nblk = (kind == TC_TF32X3) ? 3 : 1;
+  const int Kt = K * nblk;
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    for (int yy = ty; yy < 32; yy += 8) {
+      int r, k;
+      if (j.rs == 1) { r = r0 + tx; k = k0 + yy; }
+      else { r = r0 + yy; k = k0 + tx; }
+      const float v = (r < j.R && k < K) ? j.src[(int64_t)r * j.rs + (int64_t)k * j.cs] : 0.f;
+      if (j.rs == 1) tile[tx][yy] = v;
+      else tile[yy][tx] = v;
+    }
+    __syncthreads();
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int r = r0 + yy, k = k0 + tx;
+      if (r >= j.R || k >= K) continue;
+      const float v = tile[yy][tx];
+      TO* orow = out + (int64_t)r * ldk + k;
+      if (kind == TC_TF32X3) {
+        const float hi = round_tf32(v);
+        const float lo = round_tf32(v - hi);
+#pragma unroll
+        for (int blk = 0; blk < 3; ++blk) ((float*)orow)[blk * K] = ((j.pattern >> blk) & 1) ? lo : hi;
+      } else if constexpr (sizeof(TO) == 4) {
+        *orow = kind == TC_TF32 ? round_tf32(v) : v;
+      } else if (kind == TC_BF16) {
+        *(__nv_bfloat16*)orow = __float2bfloat16_rn(v);
+      } else {
+        *(__half*)orow = __float2half_rn(v);
+      }
+    }
+    __syncthreads();
+  }
+  const int pad = Kp - Kt;
+  for (int e = threadIdx.x; e < 32 * pad; e += blockDim.x) {
+    const int r = r0 + e / pad, k = Kt + e % pad;
+    if (r < j.R) out[(int64_t)r * ldk + k] = (TO)0.f;
+  }
 }
 
 // ------------------------------------------------------------------ host
@@ -359,15 +358,15 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   GBS_TRY(ws.bk.reserve((size_t)N * ldk * esize));
   {
     PhaseScope ps(s, PH_COPY, 0.0, (double)(M + N) * (4.0 * K + esize * (double)Kp));
-    dim3 blk(32, 8);
-    dim3 grid((Kp + 31) / 32, (std::max(M, N) + 31) / 32, 2);
+    const int tiles_a = (M + 31) / 32, grid = tiles_a + (N + 31) / 32;
     // x3 pattern bits (block -> lo?): A = [hi, hi, lo] (0b100), B = [hi, lo, hi] (0b010)
     const PackJob ja{A, a_rs, a_cs, M, esize == 4 ? 4 : 0}, jb{B, b_cs, b_rs, N, esize == 4 ? 2 : 0};
     if (esize == 4)
-      pack_pair_kernel<float><<<grid, blk, 0, s>>>(ja, jb, K, Kp, ws.ak.as<float>(), ws.bk.as<float>(), ldk, kind);
+      pack_pair_kernel<float><<<grid, 256, 0, s>>>(ja, jb, tiles_a, K, Kp, ws.ak.as<float>(), ws.bk.as<float>(), ldk,
+                                                   kind);
     else
-      pack_pair_kernel<uint16_t><<<grid, blk, 0, s>>>(ja, jb, K, Kp, ws.ak.as<uint16_t>(), ws.bk.as<uint16_t>(), ldk,
-                                                      kind);
+      pack_pair_kernel<uint16_t><<<grid, 256, 0, s>>>(ja, jb, tiles_a, K, Kp, ws.ak.as<uint16_t>(),
+                                                      ws.bk.as<uint16_t>(), ldk, kind);
     GBS_CUDA_TRY(cudaGetLastError());
   }
   CUtensorMap tmA, tmB;
