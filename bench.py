@@ -745,7 +745,9 @@ def c3_llt16384(args):
         for _ in range(2):
             e2e_step()
         torch.cuda.synchronize()
-        e2e = {"value": 2 / (time.perf_counter() - t0), "unit": "solves/s", "h2d_bytes_per_step": 8 * (n * n + n * nrhs),
+        # the SPD solve copies the lower trapezoid of each 512-column block (it reads A's lower triangle only)
+        lower = sum((n - c0) * min(512, n - c0) for c0 in range(0, n, 512))
+        e2e = {"value": 2 / (time.perf_counter() - t0), "unit": "solves/s", "h2d_bytes_per_step": 8 * (lower + n * nrhs),
                "d2h_bytes_per_step": 8 * n * nrhs, "api": f"gbs_dposv_mixed ({fastest}) on pinned host buffers, kappa=1e2"}
         del A1, Ah
     # CPU: the oracle's LLT (single-threaded, like the reference's LLT) on a

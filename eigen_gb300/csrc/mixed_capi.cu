@@ -109,6 +109,8 @@ static int run_device(MixedFn fn, int n, int nrhs, const double* d_a, int lda, c
   return rc;
 }
 
+constexpr int kLowerCopyCols = 512;    // column blocks of the SPD solve's lower-triangle copy
+
 static int run_host(MixedFn fn, int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
                     const gbs_refine_options* opt, gbs_refine_info* info)
 {
@@ -131,6 +133,16 @@ static int run_host(MixedFn fn, int n, int nrhs, const double* a, int lda, const
   int rc;
   if (fn == mixed_lu_solve) {     // A's copy overlaps the factorization
     rc = mixed_lu_solve_host(s, n, nrhs, a, lda, dA, dB, n, dX, n, o, &r);
+  } else if (fn == mixed_llt_solve) {
+    // the SPD solve reads A's lower triangle only (LLT.h:50-51, UpLo = Lower): copy the lower
+    // trapezoid of each block of kLowerCopyCols columns, about half of A
+    for (int c0 = 0; c0 < n; c0 += kLowerCopyCols) {
+      const int nc = std::min(kLowerCopyCols, n - c0);
+      GBS_CUDA_TRY(cudaMemcpy2DAsync(dA + (size_t)c0 * n + c0, sizeof(double) * n, a + (size_t)c0 * lda + c0,
+                                     sizeof(double) * lda, sizeof(double) * (n - c0), nc, cudaMemcpyHostToDevice,
+                                     s));
+    }
+    rc = fn(s, n, nrhs, dA, n, dB, n, dX, n, o, &r);
   } else {
     GBS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
                                    cudaMemcpyHostToDevice, s));

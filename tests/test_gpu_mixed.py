@@ -206,6 +206,27 @@ def test_streamed_host_input_with_padded_leading_dimension():
     assert O.backward_error(a, x, b) <= BAR
 
 
+@pytest.mark.parametrize("n", [700, 2500])
+def test_spd_host_solve_reads_the_lower_triangle_only(n):
+    """Like Eigen's LLT (only the lower triangle of A is considered), the SPD
+    host solve copies just the lower trapezoid of each column block: NaN in the
+    strict upper triangle must not change the solution."""
+    a = spd_with_condition(n, 1e3, 77)
+    b = O.gauss(78, n, 2)
+    x0, i0 = solve_spd_mixed(a, b, tier="tf32x3")
+    au = a.copy()
+    au[np.triu_indices(n, 1)] = np.nan
+    x1, i1 = solve_spd_mixed(au, b, tier="tf32x3")
+    assert np.array_equal(x0, x1)
+    assert i0["iterations"] == i1["iterations"]
+    assert O.backward_error(a, x1, b) <= BAR
+    torch = pytest.importorskip("torch")            # and from device buffers holding the NaNs
+    A = torch.from_numpy(np.ascontiguousarray(au.T)).cuda().t()
+    B = torch.from_numpy(np.ascontiguousarray(b.T)).cuda().t()
+    x2, _ = solve_spd_mixed(A, B, tier="tf32x3")
+    assert np.array_equal(x0, x2.cpu().numpy())
+
+
 @pytest.mark.parametrize("tier", ["tf32x3", "bf16"])
 @pytest.mark.parametrize("n", [600, 2048, 5000])
 def test_tournament_and_partial_pivoting_both_converge(tier, n):
