@@ -271,6 +271,8 @@ int trsm_lunit_wide(cudaStream_t s, int kb, int ncols, const T* L, int64_t ldl, 
 // a ballot over the list.
 __global__ void laswp_map_kernel(const int* __restrict__ tr, int i0, int i1, int* __restrict__ map)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   __shared__ int rows[256], src[256];
   const int lane = threadIdx.x;
   int cnt = 0;
@@ -306,6 +308,8 @@ template <typename T>
 __global__ void laswp_gather_kernel(T* __restrict__ a, int64_t lda, const int* __restrict__ map, int c0, int c1,
                                     int c2, int c3)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   __shared__ int rows[256], src[256];
   const int cnt = map[0];
   for (int u = threadIdx.x; u < cnt; u += blockDim.x) {
@@ -342,7 +346,7 @@ int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, i
   if (nc <= 0) return GBS_SUCCESS;
   PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * 2 * kPanelNB);
   const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
-  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map, c0, c1, c2, c3);
+  GBS_CUDA_TRY(launch_pdl(laswp_gather_kernel<T>, dim3(grid), dim3(256), 0, s, A, lda, map, c0, c1, c2, c3));
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }
@@ -353,6 +357,8 @@ int laswp_map_apply(cudaStream_t s, T* A, int64_t lda, const int* map, int c0, i
 // parallel (the gather does not depend on the order of the entries).
 __global__ void laswp_block_map_kernel(const int* __restrict__ tr, int i0, int i1, int m, int* __restrict__ map)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   extern __shared__ int src_of[];          // [m - i0]: source row now at row i0 + r
   __shared__ int s_tr[128];
   __shared__ int cnt;
@@ -401,10 +407,11 @@ int laswp_block_device(cudaStream_t s, T* A, int64_t lda, int m, const int* tr, 
   GBS_CUDA_TRY(attr);
   GBS_TRY(map.reserve(sizeof(int) * kLaswpMapInts));
   PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * 2 * (i1 - i0));
-  laswp_block_map_kernel<<<1, 1024, smem, s>>>(tr, i0, i1, m, map.as<int>());
+  GBS_CUDA_TRY(launch_pdl(laswp_block_map_kernel, dim3(1), dim3(1024), smem, s, tr, i0, i1, m, map.as<int>()));
   count_launch();
   const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
-  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map.as<int>(), c0, c1, c2, c3);
+  GBS_CUDA_TRY(launch_pdl(laswp_gather_kernel<T>, dim3(grid), dim3(256), 0, s, A, lda, (const int*)map.as<int>(), c0, c1,
+                          c2, c3));
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }
@@ -421,10 +428,11 @@ int laswp_gather_device(cudaStream_t s, T* A, int64_t lda, const int* tr, int i0
   }
   GBS_TRY(map.reserve(sizeof(int) * kLaswpMapInts));
   PhaseScope ps(s, PH_LASWP, 0.0, 2.0 * sizeof(T) * (double)nc * (i1 - i0));
-  laswp_map_kernel<<<1, 32, 0, s>>>(tr, i0, i1, map.as<int>());
+  GBS_CUDA_TRY(launch_pdl(laswp_map_kernel, dim3(1), dim3(32), 0, s, tr, i0, i1, map.as<int>()));
   count_launch();
   const int grid = std::min(ceil_div(nc, 8), 8 * device_sm_count());
-  laswp_gather_kernel<T><<<grid, 256, 0, s>>>(A, lda, map.as<int>(), c0, c1, c2, c3);
+  GBS_CUDA_TRY(launch_pdl(laswp_gather_kernel<T>, dim3(grid), dim3(256), 0, s, A, lda, (const int*)map.as<int>(), c0, c1,
+                          c2, c3));
   GBS_CUDA_TRY(cudaGetLastError());
   return GBS_SUCCESS;
 }

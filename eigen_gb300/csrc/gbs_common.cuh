@@ -63,6 +63,35 @@ __device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v)
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may be
+// scheduled while the previous kernel of its stream still runs: it calls
+// griddep_wait() before it reads or writes any global memory, which waits for
+// that kernel's completion and the visibility of its writes.  Every kernel
+// that may precede one calls griddep_launch_dependents() at entry, so that the
+// next kernel's CTAs start their launch and prologue early; that grid is
+// scheduled only once every CTA of this one has started, so its waiting CTAs
+// never keep this grid's CTAs off the SMs.  Both are no-ops without a
+// programmatic dependency.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 __device__ __forceinline__ int ld_volatile_i32(const int* p)
 {
   return *(const volatile int*)p;

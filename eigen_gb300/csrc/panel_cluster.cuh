@@ -271,6 +271,8 @@ panel_lu_cluster_kernel(T* __restrict__ a, int64_t lda, int m, int nbc, int k0, 
                         DeviceStatus* st, int* __restrict__ map, int trsm_cols)
 {
   static_assert(NB == 32, "one lane per panel column");
+  griddep_launch_dependents();
+  griddep_wait();
   typedef typename PivotKey<T>::type K;
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();

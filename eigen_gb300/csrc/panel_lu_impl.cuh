@@ -76,17 +76,19 @@ static int launch_cluster_panel(cudaStream_t s, T* a, int64_t lda, int m, int nb
 {
   PhaseScope ps(s, PH_PANEL, (double)m * nbc * nbc, sizeof(T) * 2.0 * m * nbc);
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = C;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;   // the kernel waits at entry (griddep_wait)
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(kClusterPanelThreads);
   cfg.dynamicSmemBytes = cluster_panel_dyn_smem<T, kPanelNB, RPT>();
   cfg.stream = s;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, panel_lu_cluster_kernel<T, kPanelNB, RPT>, a, lda, m, nbc, k0, tr, st, map,
                                   trsm_cols));
   return GBS_SUCCESS;

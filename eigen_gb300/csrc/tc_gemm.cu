@@ -80,6 +80,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   uint64_t* tempty = tfull + 2;
   uint32_t* tmem_slot = (uint32_t*)(tempty + 2);
 
+  griddep_launch_dependents();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -96,6 +97,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  griddep_wait();                              // the setup above touches no global memory
   const uint32_t tmem_base = *tmem_slot;
   const int num_tiles = p.tiles_m * p.tiles_n;
   const uint64_t LIMIT = effective_limit(p.limit_ns);
@@ -254,6 +256,8 @@ __global__ void __launch_bounds__(256)
 pack_pair_kernel(PackJob a, PackJob b, int tiles_a, int K, int Kp, TO* __restrict__ outa, TO* __restrict__ outb,
                  int64_t ldk, int kind)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   __shared__ float tile[32][33];
   const bool on_b = (int)blockIdx.x >= tiles_a;
   const PackJob j = on_b ? b : a;
@@ -362,12 +366,11 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
     // x3 pattern bits (block -> lo?): A = [hi, hi, lo] (0b100), B = [hi, lo, hi] (0b010)
     const PackJob ja{A, a_rs, a_cs, M, esize == 4 ? 4 : 0}, jb{B, b_cs, b_rs, N, esize == 4 ? 2 : 0};
     if (esize == 4)
-      pack_pair_kernel<float><<<grid, 256, 0, s>>>(ja, jb, tiles_a, K, Kp, ws.ak.as<float>(), ws.bk.as<float>(), ldk,
-                                                   kind);
+      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<float>, dim3(grid), dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
+                              ws.ak.as<float>(), ws.bk.as<float>(), ldk, kind));
     else
-      pack_pair_kernel<uint16_t><<<grid, 256, 0, s>>>(ja, jb, tiles_a, K, Kp, ws.ak.as<uint16_t>(),
-                                                      ws.bk.as<uint16_t>(), ldk, kind);
-    GBS_CUDA_TRY(cudaGetLastError());
+      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<uint16_t>, dim3(grid), dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
+                              ws.ak.as<uint16_t>(), ws.bk.as<uint16_t>(), ldk, kind));
   }
   CUtensorMap tmA, tmB;
   GBS_TRY(make_tmap(&tmA, ws.ak.p, esize, M, Kp, ldk, BM));
@@ -396,8 +399,7 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
   const double flops = 2.0 * M * (double)N * K * (lower ? 0.5 : 1.0);
   const double bytes = 8.0 * M * (double)N * (lower ? 0.5 : 1.0) + (double)(M + N) * Kp * esize;
   PhaseScope ps(s, PH_TC_GEMM, flops, bytes);
-  tc_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
-  GBS_CUDA_TRY(cudaGetLastError());
+  GBS_CUDA_TRY(launch_pdl(tc_gemm_kernel, dim3(grid), dim3(NUM_THREADS), SMEM_BYTES, s, tmA, tmB, p));
   return GBS_SUCCESS;
 }
 
