@@ -408,7 +408,7 @@ int partition_stream(CUgreenCtx g, int priority, cudaStream_t* out)
 struct Lookahead {
   cudaStream_t side = nullptr, wide = nullptr;
   int wide_sms = 0;
-  cudaEvent_t ready = nullptr, panels = nullptr, inv = nullptr, wide_done = nullptr;
+  cudaEvent_t ready = nullptr, panels = nullptr, inv = nullptr, wide_done = nullptr, swapped = nullptr;
   TcWorkspace tc_side, tc_wide;
   DevBuf map_side, map[2], minv[2];
   DevBuf minv_all, srcmap;   // streamed input: every block's I - L11^-1; the composed row map of a join
@@ -432,6 +432,7 @@ struct Lookahead {
     if (!panels) GBS_CUDA_TRY(cudaEventCreateWithFlags(&panels, cudaEventDisableTiming));
     if (!inv) GBS_CUDA_TRY(cudaEventCreateWithFlags(&inv, cudaEventDisableTiming));
     if (!wide_done) GBS_CUDA_TRY(cudaEventCreateWithFlags(&wide_done, cudaEventDisableTiming));
+    if (!swapped) GBS_CUDA_TRY(cudaEventCreateWithFlags(&swapped, cudaEventDisableTiming));
     for (int i = 0; i < 2; ++i) GBS_TRY(minv[i].reserve(sizeof(float) * kMixedNB * kMixedNB));
     return GBS_SUCCESS;
   }
@@ -441,6 +442,7 @@ struct Lookahead {
     if (panels) cudaEventDestroy(panels);
     if (inv) cudaEventDestroy(inv);
     if (wide_done) cudaEventDestroy(wide_done);
+    if (swapped) cudaEventDestroy(swapped);
     if (side) cudaStreamDestroy(side);
     if (wide) cudaStreamDestroy(wide);
   }
@@ -901,10 +903,10 @@ static int block_update(cudaStream_t s, int n, float* A, int64_t lda, int k, int
 //   ss: panels of block 0, I - L11^-1 of block 0
 //   for each block k:
 //     s:  wait for block k's panels and block k-1's wide update; block k's
-//         interchanges on block k+1's columns; wait for block k's I - L11^-1;
-//         update of block k+1's columns (narrow)
-//     ss: wait for the narrow update; panels of block k+1, then its I - L11^-1
-//         (it overlaps the interchanges on s)
+//         interchanges on block k+1's columns (beside block k's I - L11^-1,
+//         which follows the panels on ss)
+//     ss: wait for those interchanges; update of block k+1's columns
+//         (narrow); panels of block k+1, then its I - L11^-1
 //     ws: wait for the narrow update; the streamed chunks that join at
 //         iteration k (in != null); block k's interchanges on the other
 //         columns; update of the columns right of block k+1 (wide), up to
@@ -942,7 +944,6 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
                        tournament));
   GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
   if (n > kMixedNB) GBS_TRY(block_inverse(ss, A, lda, 0, kMixedNB, minv_of(0)));
-  GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
   bool wide_pending = false;
   for (int k = 0, blk = 0; k < n; k += kMixedNB, ++blk) {
     const int kb = std::min(kMixedNB, n - k);
@@ -960,18 +961,18 @@ static int getrf_lookahead(cudaStream_t s, int n, float* A, int64_t lda, int* tr
       gbs_set_last_message("streamed input: a chunk joins after its columns are needed");
       return GBS_INVALID_ARGUMENT;
     }
-    // the interchanges on block k+1's columns gate its panels; the left and
-    // wide columns get them (same map) while those panels run
+    // the interchanges on block k+1's columns gate its panels (they run on s
+    // beside block k's L11 inverse on ss); the left and wide columns get them
+    // (same map) while those panels run
     GBS_TRY(laswp_block_device<float>(s, A, lda, n, tr, k, k + kb, k + kb, c1, c1, c1, mapk));
-    GBS_CUDA_TRY(cudaStreamWaitEvent(s, la.inv, 0));
-    GBS_TRY(block_update(s, n, A, lda, k, kb, k + kb, c1, minv, st, kind, tcw, 0));
-    GBS_CUDA_TRY(cudaEventRecord(la.ready, s));
-    GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.ready, 0));
+    GBS_CUDA_TRY(cudaEventRecord(la.swapped, s));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(ss, la.swapped, 0));
+    GBS_TRY(block_update(ss, n, A, lda, k, kb, k + kb, c1, minv, st, kind, la.tc_side, 0));
+    GBS_CUDA_TRY(cudaEventRecord(la.ready, ss));
     if (split) GBS_CUDA_TRY(cudaStreamWaitEvent(ws, la.ready, 0));
     GBS_TRY(block_panels(ss, n, A, lda, tr, st, scratch, kind, la.tc_side, la.map_side, k + kb, nb1, true, tournament));
     GBS_CUDA_TRY(cudaEventRecord(la.panels, ss));
     if (c1 < n) GBS_TRY(block_inverse(ss, A, lda, k + kb, nb1, minv_of(blk + 1)));
-    GBS_CUDA_TRY(cudaEventRecord(la.inv, ss));
     for (; joined < at_once && in->iter[joined] <= blk; ++joined) {
       GBS_TRY(inflow_join(ws, n, A, lda, tr, *in, joined, blk, blk, la.minv_all.as<float>(), la.srcmap, st, kind,
                           split ? la.tc_wide : tcw, wide_ctas(nr)));
