@@ -523,7 +523,9 @@ static int potrf_lower(cudaStream_t s, int n, T* dA, int64_t lda, DeviceStatus* 
     return GBS_SUCCESS;
   }
   // the reference's block size (LLT.h:338-340): identical blocking keeps the
-  // matrix contents identical to the reference's after an early failure
+  // matrix contents identical to the reference's after an early failure.
+  // Plain launches: programmatic dependent launch measured slower on this
+  // FP64 chain (LLT n = 512: 874 -> 824 solves/s).
   int bs = n / 8;
   bs = (bs / 16) * 16;
   bs = std::min(std::max(bs, 8), max_bs);

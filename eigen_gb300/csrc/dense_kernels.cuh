@@ -259,6 +259,8 @@ gemm_sub_kernel(int M, int N, int K, const T* __restrict__ A, int64_t a_rs, int6
                 const T* __restrict__ B, int64_t b_rs, int64_t b_cs, T* __restrict__ C, int64_t ldc,
                 int lower, const int* stop_flag)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   constexpr int TX = BN / TN, TY = BM / TM, NT = TX * TY;
   const int bm = blockIdx.y * BM, bn = blockIdx.x * BN;
   if (lower && bn >= bm + BM) return;                 // tile strictly above the diagonal
@@ -365,6 +367,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 potrf_diag_kernel(T* __restrict__ a, int64_t lda, int bs, int k0, DeviceStatus* st)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   if (st->info >= 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = (T*)smem_raw;
@@ -507,6 +511,8 @@ __global__ void __launch_bounds__(256)
 trsm_rlt_blocked_kernel(const T* __restrict__ L, int64_t ldl, int bs, T* __restrict__ X, int64_t ldx, int m,
                         const DeviceStatus* st)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   constexpr int W = 16;
   constexpr bool kRecip = std::is_same<T, double>::value;
   if (st && ld_volatile_i32(&st->info) >= 0) return;

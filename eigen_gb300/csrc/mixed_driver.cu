@@ -647,6 +647,8 @@ __device__ void tri_inverse_smem(const float* __restrict__ L, int64_t ld, int nb
 __global__ void __launch_bounds__(4 * kMixedNB)
 unit_lower_inverse_kernel(const float* __restrict__ L, int64_t ld, int nb, float* __restrict__ M, int unit)
 {
+  griddep_launch_dependents();
+  griddep_wait();
   extern __shared__ float sm[];
   tri_inverse_smem(L, ld, nb, unit, 0, sm);
   const float(*X)[kInvLd] = reinterpret_cast<const float(*)[kInvLd]>(sm + kMixedNB * kInvLd);
@@ -878,8 +880,8 @@ static int block_panels(cudaStream_t s, int n, float* A, int64_t lda, int* tr, D
 static int block_inverse(cudaStream_t s, const float* A, int64_t lda, int k, int kb, float* minv)
 {
   PhaseScope ps(s, PH_TRSM_LU, (double)kb * kb * kb / 3.0, sizeof(float) * 2.0 * kb * kb);
-  unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(A + (int64_t)k * lda + k, lda, kb, minv, 1);
-  GBS_CUDA_TRY(cudaGetLastError());
+  GBS_CUDA_TRY(launch_pdl(unit_lower_inverse_kernel, dim3(1), dim3(4 * kMixedNB), kInvSmem, s,
+                          (const float*)(A + (int64_t)k * lda + k), lda, kb, minv, 1));
   return GBS_SUCCESS;
 }
 
@@ -1049,15 +1051,15 @@ static int potrf_block(cudaStream_t s, int n, float* As, int64_t lda, int k, int
   float* Akk = As + (int64_t)k * lda + k;
   {
     PhaseScope ps(s, PH_POTRF_DIAG, (double)b * b * b / 3.0, 4.0 * b * b);
-    potrf_diag_kernel<float><<<1, 256, potrf_diag_smem<float>(b), s>>>(Akk, lda, b, k, st);
-    GBS_CUDA_TRY(cudaGetLastError());
+    GBS_CUDA_TRY(launch_pdl(potrf_diag_kernel<float>, dim3(1), dim3(256), potrf_diag_smem<float>(b), s, Akk, lda, b, k,
+                            st));
   }
   if (rs <= 0) return GBS_SUCCESS;
   float* A21 = Akk + b;
   {
     PhaseScope ps(s, PH_TRSM_LLT, (double)b * b * b / 3.0, 8.0 * b * b);
-    unit_lower_inverse_kernel<<<1, 4 * kMixedNB, kInvSmem, s>>>(Akk, lda, b, minv, 0);
-    GBS_CUDA_TRY(cudaGetLastError());
+    GBS_CUDA_TRY(launch_pdl(unit_lower_inverse_kernel, dim3(1), dim3(4 * kMixedNB), kInvSmem, s, (const float*)Akk, lda,
+                            b, minv, 0));
   }
   return tc_gemm_sub(s, kind, rs, b, b, A21, 1, lda, minv, kMixedNB, 1, A21, lda, 0, st, tcw);
 }
