@@ -413,7 +413,11 @@ int gbs_dgeresid_device(int n, int nrhs, const double* d_a, int lda, const doubl
  * NULL: defaults. */
 int gbs_dgesv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
                            int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
-/* Host buffers (copied in and out inside the call). */
+/* Host buffers (copied in and out inside the call).  For 2048 <= n <= 20480,
+ * nrhs <= 16 and look-ahead on, A crosses in column chunks that the
+ * factorization takes in as they land (pinned host memory lets the copies
+ * overlap it); the results are bit-identical to gbs_dgesv_mixed_device's on the
+ * same A. */
 int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
                     const gbs_refine_options* opt, gbs_refine_info* info);
 /* SPD A, lower triangle read (LLT<MatrixXd, Lower>).  Returns
@@ -421,6 +425,8 @@ int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, 
  * FP64 either. */
 int gbs_dposv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
                            int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
+/* Host buffers: only the lower trapezoid of each 512-column block of A is
+ * copied (the strict upper triangle is never read, as in LLT). */
 int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
                     const gbs_refine_options* opt, gbs_refine_info* info);
 
