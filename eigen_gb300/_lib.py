@@ -172,6 +172,7 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_profile_reset": (c_int, []),
     "gbs_profile_collect": (c_int, [c_int, c_dp, C.POINTER(c_i64), c_dp, c_dp]),
     "gbs_profile_timeline": (c_int, [c_ip, c_ip, c_dp, c_dp, c_int]),
+    "gbs_streamed_input_plan": (c_int, [c_int, c_int, c_ip, c_ip, c_ip]),
 }
 
 PHASES = {"panel": 0, "laswp": 1, "trsm_lu": 2, "gemm": 3, "potrf_diag": 4, "trsm_llt": 5, "syrk": 6,

@@ -194,3 +194,9 @@ extern "C" int gbs_dgeresid_device(int n, int nrhs, const double* d_a, int lda, 
   GBS_TRY(ensure_device());
   return residual_device((cudaStream_t)stream, n, nrhs, d_a, lda, d_x, ldx, d_b, ldb, d_r, ldr, method);
 }
+
+extern "C" int gbs_streamed_input_plan(int n, int cap, int* col, int* iter, int* rolling)
+{
+  if (cap < 0) return -(100 + GBS_INVALID_ARGUMENT);
+  return streamed_input_plan(n, cap, col, iter, rolling);
+}

@@ -408,7 +408,7 @@ int partition_stream(CUgreenCtx g, int priority, cudaStream_t* out)
 struct Lookahead {
   cudaStream_t side = nullptr, wide = nullptr;
   int wide_sms = 0;
-  cudaEvent_t ready = nullptr, panels = nullptr, inv = nullptr, wide_done = nullptr, swapped = nullptr;
+  cudaEvent_t ready = nullptr, panels = nullptr, wide_done = nullptr, swapped = nullptr;
   TcWorkspace tc_side, tc_wide;
   DevBuf map_side, map[2], minv[2];
   DevBuf minv_all, srcmap;   // streamed input: every block's I - L11^-1; the composed row map of a join
@@ -430,7 +430,6 @@ struct Lookahead {
     }
     if (!ready) GBS_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     if (!panels) GBS_CUDA_TRY(cudaEventCreateWithFlags(&panels, cudaEventDisableTiming));
-    if (!inv) GBS_CUDA_TRY(cudaEventCreateWithFlags(&inv, cudaEventDisableTiming));
     if (!wide_done) GBS_CUDA_TRY(cudaEventCreateWithFlags(&wide_done, cudaEventDisableTiming));
     if (!swapped) GBS_CUDA_TRY(cudaEventCreateWithFlags(&swapped, cudaEventDisableTiming));
     for (int i = 0; i < 2; ++i) GBS_TRY(minv[i].reserve(sizeof(float) * kMixedNB * kMixedNB));
@@ -440,7 +439,6 @@ struct Lookahead {
   {
     if (ready) cudaEventDestroy(ready);
     if (panels) cudaEventDestroy(panels);
-    if (inv) cudaEventDestroy(inv);
     if (wide_done) cudaEventDestroy(wide_done);
     if (swapped) cudaEventDestroy(swapped);
     if (side) cudaStreamDestroy(side);
@@ -1679,6 +1677,19 @@ static int lu_solve_impl(cudaStream_t s, int n, int nrhs, const double* A, int64
   }
   if (res) *res = out;
   return GBS_SUCCESS;
+}
+
+int streamed_input_plan(int n, int cap, int* col, int* iter, int* rolling)
+{
+  if (n < kInflowMinN || n > kInflowMaxN) return 0;
+  Inflow in;
+  plan_inflow(n, in);
+  for (int j = 0; j <= in.chunks && j <= cap; ++j) {
+    if (col) col[j] = in.col[j];
+    if (iter && j < in.chunks && j < cap) iter[j] = in.iter[j];
+  }
+  if (rolling) *rolling = in.rolling;
+  return in.chunks;
 }
 
 int mixed_lu_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t lda, const double* B, int64_t ldb,

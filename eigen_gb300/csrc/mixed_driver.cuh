@@ -49,5 +49,7 @@ int mixed_llt_solve(cudaStream_t s, int n, int nrhs, const double* A, int64_t ld
 // device buffers.
 int mixed_lu_solve_host(cudaStream_t s, int n, int nrhs, const double* a, int64_t lda, double* dA, const double* B,
                         int64_t ldb, double* X, int64_t ldx, const MixedOptions& opt, MixedResult* res);
+// The chunk plan mixed_lu_solve_host uses for order n (see gbs_streamed_input_plan).
+int streamed_input_plan(int n, int cap, int* col, int* iter, int* rolling);
 
 }  // namespace gbs

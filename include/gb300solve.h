@@ -425,6 +425,14 @@ int gbs_dgesv_mixed(int n, int nrhs, const double* a, int lda, const double* b, 
  * FP64 either. */
 int gbs_dposv_mixed_device(int n, int nrhs, const double* d_a, int lda, const double* d_b, int ldb, double* d_x,
                            int ldx, const gbs_refine_options* opt, gbs_refine_info* info, void* stream);
+/* The column chunks gbs_dgesv_mixed copies A in, for order n (a diagnostic;
+ * no GPU work).  Returns the number of chunks m (0: A is copied whole), fills
+ * col[0..m] (chunk j holds the columns [col[j], col[j+1])) and iter[0..m-1]
+ * (the look-ahead iteration at which chunk j joins the wide updates, or, for
+ * the rolling chunk, at which it is gathered), and *rolling (the rolling
+ * chunk's index, or -1).  col holds cap + 1 entries and iter cap; entries
+ * beyond them are not written.  Any pointer may be NULL. */
+int gbs_streamed_input_plan(int n, int cap, int* col, int* iter, int* rolling);
 /* Host buffers: only the lower trapezoid of each 512-column block of A is
  * copied (the strict upper triangle is never read, as in LLT). */
 int gbs_dposv_mixed(int n, int nrhs, const double* a, int lda, const double* b, int ldb, double* x, int ldx,
