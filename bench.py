@@ -829,11 +829,8 @@ def c4_batched(args):
         Ih = torch.empty(len(sizes), dtype=torch.int32).pin_memory()
 
         def e2e_step():
-            A.copy_(Ah, non_blocking=True)
-            B.copy_(Bh, non_blocking=True)
-            bs.solve(A, B, info, piv)
-            Xh.copy_(B, non_blocking=True)
-            Ih.copy_(info, non_blocking=True)
+            # the library's host-buffer solve: parts of the batch cross in and out while others are solved
+            bs.solve_host(Ah, Bh, Ih, x=Xh)
         for _ in range(warmup):
             e2e_step()
         torch.cuda.synchronize()
@@ -887,7 +884,8 @@ def c4_batched(args):
             "summary": {"f32_solves_per_s": out["f32"]["solves_per_s"], "failures_f64": f64["failures"]},
             "e2e": {"value": f64["e2e_solves_per_s"], "unit": "solves/s",
                     "h2d_bytes_per_step": f64["h2d_bytes_per_step"], "d2h_bytes_per_step": f64["d2h_bytes_per_step"],
-                    "api": "host->device copies + gbs_batched_solve + device->host copies, every step"},
+                    "api": "gbs_batched_solve_host on pinned host buffers (the batch in four parts: each part's "
+                           "copies overlap the other parts' solves), every step"},
             "cpu_baseline": {"value": f64["cpu_oracle_solves_per_s"], "unit": "solves/s", "cores": f64["cpu_cores"],
                              "kind": "port", "sample": "the whole FP64 batch, one oracle factor + solve per item, "
                                                        "OpenMP over items"},

@@ -139,6 +139,7 @@ PROTOTYPES: dict[str, tuple] = {
     "gbs_batched_rhs_elements": (c_i64, [c_vp]),
     "gbs_batched_offsets": (c_int, [c_vp, c_vp, c_vp]),
     "gbs_batched_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "gbs_batched_solve_host": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "gbs_batched_autotune": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
     "gbs_batched_config": (c_int, [c_vp, c_ip, c_ip]),
     "gbs_batched_buckets": (c_int, [c_vp, c_int, c_ip, c_ip]),

@@ -56,6 +56,19 @@ class BatchedSolver:
                                           C.c_void_p(d_info.data_ptr()), C.c_void_p(d_piv.data_ptr()),
                                           C.c_void_p(s)), "batched.solve")
 
+    def solve_host(self, a, b, info, piv=None, x=None):
+        """Host buffers (numpy arrays or CPU torch tensors, flat, packed): the
+        solutions go to x (default: b, in place), info (int32) gets the
+        per-item status, piv (int32, optional) the LU items' transpositions;
+        a is read only.  The copies overlap the solve when the buffers are
+        pinned."""
+        def ptr(t):
+            if t is None:
+                return None
+            return C.c_void_p(t.data_ptr() if hasattr(t, "data_ptr") else t.ctypes.data)
+        L.check(L.lib().gbs_batched_solve_host(self._h, ptr(a), ptr(b), ptr(b if x is None else x), ptr(info),
+                                               ptr(piv)), "batched.solve_host")
+
     def autotune(self, d_a, d_b, d_info, d_piv, persist=False):
         """Chooses each size group's kernel variant by timing the whole batch
         on these buffers; every run starts from their contents, which are

@@ -390,6 +390,13 @@ struct gbs_batched {
   void* g_info = nullptr;
   void* g_piv = nullptr;
   int use_graph = 1;
+  // gbs_batched_solve_host: parts of consecutive items, each with a plan of
+  // its own, the batch's device copy, and the streams that move it
+  std::vector<gbs_batched*> parts;
+  std::vector<int64_t> part_first;     // part q holds the items [part_first[q], part_first[q + 1])
+  DevBuf da, db, dinfo, dpiv;
+  cudaStream_t hin = nullptr, hrun = nullptr, hout = nullptr;
+  std::vector<cudaEvent_t> ev_in, ev_run;
 };
 
 static void drop_graph(gbs_batched* p)
@@ -594,6 +601,15 @@ extern "C" int gbs_batched_create(gbs_batched** out, int dtype, int64_t count, c
 extern "C" int gbs_batched_destroy(gbs_batched* p)
 {
   if (!p) return GBS_SUCCESS;
+  for (cudaStream_t hs : {p->hin, p->hrun, p->hout})
+    if (hs) cudaStreamSynchronize(hs);
+  for (gbs_batched* q : p->parts) gbs_batched_destroy(q);
+  for (cudaEvent_t e : p->ev_in)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_run)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t hs : {p->hin, p->hrun, p->hout})
+    if (hs) cudaStreamDestroy(hs);
   if (p->stream) cudaStreamSynchronize(p->stream);
   for (int k = 0; k < kSideStreams; ++k)
     if (p->side[k]) cudaStreamSynchronize(p->side[k]);
@@ -772,4 +788,140 @@ extern "C" int gbs_batched_set_variant(gbs_batched* p, int bucket, int lanes, in
   }
   drop_graph(p);
   return GBS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ host buffers
+namespace {
+constexpr int kHostParts = 4;                         // parts of a large batch
+constexpr int64_t kHostPartMinBytes = 16 << 20;       // smaller batches use fewer parts
+
+// The parts' plans run the variants of the whole plan's buckets, so every item
+// is solved by the same kernel as by gbs_batched_solve.
+int sync_part_variants(gbs_batched* p)
+{
+  for (gbs_batched* q : p->parts)
+    for (size_t i = 0; i < q->buckets.size(); ++i) {
+      const BucketPlan& qb = q->buckets[i];
+      for (const BucketPlan& b : p->buckets)
+        if (b.kind == qb.kind && b.hi == qb.hi && (b.lanes != qb.lanes || b.warps != qb.warps))
+          GBS_TRY(gbs_batched_set_variant(q, (int)i, b.lanes, b.warps));
+    }
+  return GBS_SUCCESS;
+}
+
+void drop_parts(gbs_batched* p)
+{
+  for (gbs_batched* q : p->parts) gbs_batched_destroy(q);
+  for (cudaEvent_t e : p->ev_in)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_run)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t* hs : {&p->hin, &p->hrun, &p->hout}) {
+    if (*hs) cudaStreamDestroy(*hs);
+    *hs = nullptr;
+  }
+  p->parts.clear();
+  p->part_first.clear();
+  p->ev_in.clear();
+  p->ev_run.clear();
+}
+
+int build_parts(gbs_batched* p);
+
+int make_parts(gbs_batched* p)
+{
+  const int rc = build_parts(p);
+  if (rc != GBS_SUCCESS) drop_parts(p);
+  return rc;
+}
+
+int build_parts(gbs_batched* p)
+{
+  const size_t es = p->dtype == GBS_F64 ? sizeof(double) : sizeof(float);
+  const int64_t bytes = (p->total_a + p->total_b) * (int64_t)es;
+  const int nparts = (int)std::max<int64_t>(1, std::min<int64_t>(kHostParts, bytes / kHostPartMinBytes));
+  p->part_first.assign(1, 0);
+  for (int q = 1; q < nparts; ++q) {            // equal bytes per part, cut at item boundaries
+    const int64_t target = (p->total_a + p->total_b) * q / nparts;
+    int64_t i = p->part_first.back();
+    while (i < p->count && p->a_off[(size_t)i] + p->b_off[(size_t)i] < target) ++i;
+    if (i > p->part_first.back() && i < p->count) p->part_first.push_back(i);
+  }
+  p->part_first.push_back(p->count);
+  for (size_t q = 0; q + 1 < p->part_first.size(); ++q) {
+    const int64_t i0 = p->part_first[q], i1 = p->part_first[q + 1];
+    gbs_batched* part = nullptr;
+    GBS_TRY(gbs_batched_create(&part, p->dtype, i1 - i0, p->sizes.data() + i0, p->kinds.data() + i0, p->use_graph));
+    p->parts.push_back(part);
+    cudaEvent_t ei = nullptr, er = nullptr;
+    GBS_CUDA_TRY(cudaEventCreateWithFlags(&ei, cudaEventDisableTiming));
+    p->ev_in.push_back(ei);
+    GBS_CUDA_TRY(cudaEventCreateWithFlags(&er, cudaEventDisableTiming));
+    p->ev_run.push_back(er);
+  }
+  for (cudaStream_t* hs : {&p->hin, &p->hrun, &p->hout})
+    GBS_CUDA_TRY(cudaStreamCreateWithFlags(hs, cudaStreamNonBlocking));
+  return GBS_SUCCESS;
+}
+}  // namespace
+
+extern "C" int gbs_batched_solve_host(gbs_batched* p, const void* a, const void* b, void* x, int* info, int* piv)
+{
+  if (!p || (p->count > 0 && (!a || !b || !x || !info))) return GBS_INVALID_ARGUMENT;
+  if (p->count == 0) return GBS_SUCCESS;
+  const size_t es = p->dtype == GBS_F64 ? sizeof(double) : sizeof(float);
+  if (p->parts.empty()) GBS_TRY(make_parts(p));
+  GBS_TRY(sync_part_variants(p));
+  GBS_TRY(p->da.reserve(es * (size_t)p->total_a));
+  GBS_TRY(p->db.reserve(es * (size_t)p->total_b));
+  GBS_TRY(p->dinfo.reserve(sizeof(int) * (size_t)p->count));
+  GBS_TRY(p->dpiv.reserve(sizeof(int) * (size_t)p->total_b));
+  char* da = (char*)p->da.p;
+  char* db = (char*)p->db.p;
+  const char* ha = (const char*)a;
+  const char* hb = (const char*)b;
+  char* hx = (char*)x;
+  int rc = GBS_SUCCESS;
+  for (size_t q = 0; q < p->parts.size() && rc == GBS_SUCCESS; ++q) {
+    const int64_t i0 = p->part_first[q], i1 = p->part_first[q + 1];
+    const int64_t a0 = p->a_off[(size_t)i0], a1 = i1 < p->count ? p->a_off[(size_t)i1] : p->total_a;
+    const int64_t b0 = p->b_off[(size_t)i0], b1 = i1 < p->count ? p->b_off[(size_t)i1] : p->total_b;
+    // part q crosses in while part q - 1 is solved, and out while part q + 1 is
+    cudaError_t e = cudaMemcpyAsync(da + es * a0, ha + es * a0, es * (a1 - a0), cudaMemcpyHostToDevice, p->hin);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(db + es * b0, hb + es * b0, es * (b1 - b0), cudaMemcpyHostToDevice, p->hin);
+    if (e == cudaSuccess) e = cudaEventRecord(p->ev_in[q], p->hin);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(p->hrun, p->ev_in[q], 0);
+    if (e != cudaSuccess) {
+      gbs_set_last_cuda_error(e, "gbs_batched_solve_host", __FILE__, __LINE__);
+      rc = GBS_CUDA_ERROR;
+      break;
+    }
+    rc = gbs_batched_solve(p->parts[q], da + es * a0, db + es * b0, p->dinfo.as<int>() + i0, p->dpiv.as<int>() + b0,
+                           p->hrun);
+    if (rc != GBS_SUCCESS) break;
+    e = cudaEventRecord(p->ev_run[q], p->hrun);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(p->hout, p->ev_run[q], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hx + es * b0, db + es * b0, es * (b1 - b0), cudaMemcpyDeviceToHost, p->hout);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(info + i0, p->dinfo.as<int>() + i0, sizeof(int) * (i1 - i0), cudaMemcpyDeviceToHost,
+                          p->hout);
+    if (e == cudaSuccess && piv)
+      e = cudaMemcpyAsync(piv + b0, p->dpiv.as<int>() + b0, sizeof(int) * (b1 - b0), cudaMemcpyDeviceToHost,
+                          p->hout);
+    if (e != cudaSuccess) {
+      gbs_set_last_cuda_error(e, "gbs_batched_solve_host", __FILE__, __LINE__);
+      rc = GBS_CUDA_ERROR;
+    }
+  }
+  // nothing of the three streams outlives the call
+  for (cudaStream_t hs : {p->hin, p->hrun, p->hout}) {
+    const cudaError_t e = cudaStreamSynchronize(hs);
+    if (e != cudaSuccess && rc == GBS_SUCCESS) {
+      gbs_set_last_cuda_error(e, "gbs_batched_solve_host", __FILE__, __LINE__);
+      rc = GBS_CUDA_ERROR;
+    }
+  }
+  return rc;
 }

@@ -467,6 +467,14 @@ int64_t gbs_batched_matrix_elements(const gbs_batched* plan);
 int64_t gbs_batched_rhs_elements(const gbs_batched* plan);
 int gbs_batched_offsets(const gbs_batched* plan, int64_t* a_offsets, int64_t* b_offsets);
 int gbs_batched_solve(gbs_batched* plan, void* d_a, void* d_b, int* d_info, int* d_piv, void* stream);
+/* The same solve from host buffers: a and b (read only; the factors stay on
+ * the device), the solutions into x (may be b), info and piv (may be NULL),
+ * in the layouts above.  A large batch is split into up to four parts of
+ * consecutive items; each part crosses to the device while the previous one
+ * is solved and back while the next one is (with pinned host memory).  Every
+ * item is solved by the same kernel as in gbs_batched_solve, with the same
+ * results.  Returns once b, info and piv are written. */
+int gbs_batched_solve_host(gbs_batched* plan, const void* a, const void* b, void* x, int* info, int* piv);
 /* The plan groups the items into buckets by kind and size class (LLT: n <= 8,
  * 12, 16, 20, 24, 32, 64; LU: n <= 8, 12, 16, 24, 32, 48, 64).  Each bucket
  * runs one variant: G lanes per system (G in {1, 2, 4, 8, 16}; 32 / G systems

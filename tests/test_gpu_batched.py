@@ -159,3 +159,59 @@ def test_batched_autotune_keeps_results():
     for i in range(0, len(sizes), 37):
         _, xi = bs.unpack(d_a.cpu().numpy(), x, i)
         assert O.backward_error(mats[i], xi.reshape(-1, 1), rhs[i].reshape(-1, 1)) < 1e-14
+
+
+def test_host_buffers_match_the_device_solve():
+    """gbs_batched_solve_host splits a large batch into parts of consecutive
+    items, each copied in while the previous part is solved and copied back
+    while the next one is: solutions, status and pivots bit-identical to the
+    device solve, and the host matrices left as they were."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    nl, ng = 24000, 6000                        # ~113 MB in FP64: four parts
+    sizes = np.concatenate([rng.integers(3, 25, nl), rng.integers(4, 65, ng)]).astype(np.int32)
+    kinds = np.concatenate([np.zeros(nl), np.ones(ng)]).astype(np.int32)
+    order = rng.permutation(len(sizes))
+    sizes, kinds = sizes[order], kinds[order]
+    bs = BatchedSolver(sizes, kinds, dtype=np.float64)
+    a = rng.standard_normal(bs.a_elems)
+    b = rng.standard_normal(bs.b_elems)
+    n = sizes.astype(np.int64)
+    within = np.arange(n.sum()) - np.repeat(np.cumsum(n) - n, n)
+    a[np.repeat(bs.a_off[:len(sizes)], n) + within * (np.repeat(n, n) + 1)] += 3.0 * np.repeat(n, n)  # dominant diagonals
+    d_a, d_b = torch.from_numpy(a.copy()).cuda(), torch.from_numpy(b.copy()).cuda()
+    d_info = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    d_piv = torch.zeros(bs.b_elems, dtype=torch.int32, device="cuda")
+    bs.solve(d_a, d_b, d_info, d_piv)
+    torch.cuda.synchronize()
+    x, info, piv = d_b.cpu().numpy(), d_info.cpu().numpy(), d_piv.cpu().numpy()
+    assert (info == -1).all()
+    lu_entries = np.repeat(kinds == 1, sizes)
+    ha = torch.from_numpy(a.copy()).pin_memory()
+    hb = torch.from_numpy(b.copy()).pin_memory()
+    hx = torch.empty(bs.b_elems, dtype=torch.float64).pin_memory()
+    hi = torch.empty(len(sizes), dtype=torch.int32).pin_memory()
+    hp = torch.empty(bs.b_elems, dtype=torch.int32).pin_memory()
+    for _ in range(2):                          # the second call replays the parts' graphs
+        hx.fill_(0.0)
+        hi.fill_(-7)
+        bs.solve_host(ha, hb, hi, hp, x=hx)
+        assert np.array_equal(hx.numpy(), x)
+        assert np.array_equal(hi.numpy(), info)
+        assert np.array_equal(hp.numpy()[lu_entries], piv[lu_entries])
+    assert np.array_equal(ha.numpy(), a) and np.array_equal(hb.numpy(), b)
+
+
+def test_host_buffers_small_batch_pageable():
+    """A small batch (one part) from pageable numpy arrays, with failing items."""
+    sizes, kinds, mats, rhs = make_batch(150, 60, seed=23)
+    bs, fa, fb, info, piv = run_batch(np.float64, sizes, kinds, mats, rhs)
+    a, b = bs.pack(mats, rhs)
+    hinfo = np.full(len(sizes), -7, dtype=np.int32)
+    hpiv = np.zeros(max(bs.b_elems, 1), dtype=np.int32)
+    bs.solve_host(a, b, hinfo, hpiv)
+    assert np.array_equal(hinfo, info)
+    ok = np.repeat(info < 0, sizes)             # failed LLT items keep their right-hand side
+    assert np.array_equal(b[ok], fb[ok])
+    lu_entries = np.repeat(np.asarray(kinds) == 1, sizes)
+    assert np.array_equal(hpiv[lu_entries], piv[lu_entries])
