@@ -247,10 +247,12 @@ struct PackJob {
 // out[r * ldk + blk * K + k] (K-major) from src(r, k) = src[r*rs + k*cs],
 // r < R, k < K, converted to the tier's type; x3 tiers write three K-blocks
 // per row, `pattern` selecting hi (0) or lo (1) for each block.  Zero padding
-// from nblk K up to Kp.  One CTA per 32-row tile of A (the first tiles_a
-// CTAs) or of B: it walks the source K in 32-wide slices staged in shared
-// memory (loads along the source's unit stride), reading each element once
-// and writing every block's copy of it.
+// from nblk K up to Kp.  One CTA per (32-row tile, 32-wide slice of the
+// source K): blockIdx.x runs over the tiles of A (the first tiles_a) and then
+// of B, blockIdx.y over the K slices (striding when K has more slices than
+// the grid).  Each slice is staged in shared memory (loads along the source's
+// unit stride), each element read once and written to every block; the CTAs
+// with blockIdx.y == 0 also write the padding.
 template <typename TO>
 __global__ void __launch_bounds__(256)
 pack_pair_kernel(PackJob a, PackJob b, int tiles_a, int K, int Kp, TO* __restrict__ outa, TO* __restrict__ outb,
@@ -267,7 +269,7 @@ pack_pair_kernel(PackJob a, PackJob b, int tiles_a, int K, int Kp, TO* __restric
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
   const int nblk = (kind == TC_TF32X3) ? 3 : 1;
   const int Kt = K * nblk;
-  for (int k0 = 0; k0 < K; k0 += 32) {
+  for (int k0 = blockIdx.y * 32; k0 < K; k0 += gridDim.y * 32) {
     for (int yy = ty; yy < 32; yy += 8) {
       int r, k;
       if (j.rs == 1) { r = r0 + tx; k = k0 + yy; }
@@ -297,6 +299,7 @@ pack_pair_kernel(PackJob a, PackJob b, int tiles_a, int K, int Kp, TO* __restric
     }
     __syncthreads();
   }
+  if (blockIdx.y != 0) return;
   const int pad = Kp - Kt;
   for (int e = threadIdx.x; e < 32 * pad; e += blockDim.x) {
     const int r = r0 + e / pad, k = Kt + e % pad;
@@ -365,11 +368,12 @@ int tc_gemm_sub(cudaStream_t s, int kind, int M, int N, int K, const float* A, i
     const int tiles_a = (M + 31) / 32, grid = tiles_a + (N + 31) / 32;
     // x3 pattern bits (block -> lo?): A = [hi, hi, lo] (0b100), B = [hi, lo, hi] (0b010)
     const PackJob ja{A, a_rs, a_cs, M, esize == 4 ? 4 : 0}, jb{B, b_cs, b_rs, N, esize == 4 ? 2 : 0};
+    const dim3 g2(grid, std::min((K + 31) / 32, 65535));
     if (esize == 4)
-      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<float>, dim3(grid), dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
+      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<float>, g2, dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
                               ws.ak.as<float>(), ws.bk.as<float>(), ldk, kind));
     else
-      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<uint16_t>, dim3(grid), dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
+      GBS_CUDA_TRY(launch_pdl(pack_pair_kernel<uint16_t>, g2, dim3(256), 0, s, ja, jb, tiles_a, K, Kp,
                               ws.ak.as<uint16_t>(), ws.bk.as<uint16_t>(), ldk, kind));
   }
   CUtensorMap tmA, tmB;
