@@ -85,3 +85,18 @@ def test_headline_order():
 def test_every_chunk_joins_before_its_columns_are_needed(lo, hi):
     for n in range(lo, hi):
         check(n)
+
+
+def test_plan_respects_the_capacity_and_null_pointers():
+    """cap bounds what is written (col gets cap + 1 entries, iter cap); NULL
+    pointers are allowed; the count is returned either way."""
+    m, col_full, it_full, rolling = plan(16384)
+    assert m > 3
+    col = (C.c_int * 4)(*([-5] * 4))
+    it = (C.c_int * 4)(*([-5] * 4))
+    lib = _lib.lib()
+    assert lib.gbs_streamed_input_plan(16384, 2, col, it, None) == m
+    assert list(col) == col_full[:3] + [-5]
+    assert list(it) == it_full[:2] + [-5, -5]
+    assert lib.gbs_streamed_input_plan(16384, 0, None, None, None) == m
+    assert lib.gbs_streamed_input_plan(16384, -1, None, None, None) < 0
