@@ -89,6 +89,9 @@ def args_parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--factor-once", action="store_true",
                    help="factor one seeded system and exit (small ncu captures)")
+    p.add_argument("--timeline", default="",
+                   help="write the library's per-launch timeline (phase, stream, start, end in ms) of one "
+                        "device-buffer and one host-buffer headline solve to this CSV file, print a summary, exit")
     p.add_argument("--config", default="lu8192", choices=["lu8192", "llt512", "llt16384", "batched", "router", "mbatch"],
                    help="lu8192: the headline line (with the companions); the others print one line of their own")
     p.add_argument("--companions", default=",".join(COMPANIONS),
@@ -1088,8 +1091,87 @@ def run_mbatch(args):
     return 0
 
 
+PHASE_NAMES = ("panel", "laswp", "trsm_lu", "gemm", "potrf_diag", "trsm_llt", "syrk", "tri_solve", "norm", "mixed",
+               "tc_gemm", "residual", "batched", "router", "copy")
+
+
+def timeline(args):
+    """One device-buffer and one host-buffer solve of the headline workload
+    (after warm-up), each with the library's per-launch CUDA events on: every
+    launch's phase, stream (0, 1, ... in order of first use) and start / end
+    time goes to the CSV file, and a summary per stream (launches, busy time,
+    span) and of the panel chain's block period is printed.  The events sit
+    between the kernels, so programmatic dependent launch is off in this run
+    and its times are not the bench's."""
+    import ctypes as C
+    import numpy as np
+    import torch
+
+    import eigen_gb300 as gb
+    from eigen_gb300 import _lib
+    from eigen_gb300.mixed import RefineInfo, options
+    L = gb.lib()
+    n, nrhs = args.n, args.nrhs
+    a_host, b_host = headline_inputs(n, nrhs)
+    A = torch.from_numpy(np.ascontiguousarray(a_host.T)).cuda().t()
+    B = torch.from_numpy(np.ascontiguousarray(b_host.T)).cuda().t()
+    X = torch.empty(nrhs, n, dtype=torch.float64, device="cuda").t()
+    Ah = torch.from_numpy(np.ascontiguousarray(a_host.T)).pin_memory()
+    Bh = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
+    Xh = torch.empty((nrhs, n), dtype=torch.float64).pin_memory()
+    opt = options(args.path, tol=BE_BAR, lookahead=bool(args.lookahead))
+    info = RefineInfo()
+    s = torch.cuda.current_stream()
+
+    def dev():
+        _lib.check(L.gbs_dgesv_mixed_device(n, nrhs, C.c_void_p(A.data_ptr()), n, C.c_void_p(B.data_ptr()), n,
+                                            C.c_void_p(X.data_ptr()), n, C.byref(opt), C.byref(info),
+                                            C.c_void_p(s.cuda_stream)), "gbs_dgesv_mixed_device")
+
+    def host():
+        _lib.check(L.gbs_dgesv_mixed(n, nrhs, C.c_void_p(Ah.data_ptr()), n, C.c_void_p(Bh.data_ptr()), n,
+                                     C.c_void_p(Xh.data_ptr()), n, C.byref(opt), C.byref(info)), "gbs_dgesv_mixed")
+
+    cap = 1 << 16
+    with open(args.timeline, "w") as f:
+        f.write("api,phase,stream,start_ms,end_ms\n")
+        for name, fn in (("device", dev), ("host", host)):
+            for _ in range(max(1, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            L.gbs_profile_reset()
+            L.gbs_profile_enable(1)
+            fn()
+            torch.cuda.synchronize()
+            ph, st = (C.c_int * cap)(), (C.c_int * cap)()
+            t0, t1 = (C.c_double * cap)(), (C.c_double * cap)()
+            m = L.gbs_profile_timeline(ph, st, t0, t1, cap)
+            L.gbs_profile_enable(0)
+            if m < 0:
+                raise RuntimeError(f"gbs_profile_timeline failed ({m})")
+            m = min(m, cap)
+            rec = [(ph[i], st[i], t0[i], t1[i]) for i in range(m)]
+            for p_, s_, a_, b_ in rec:
+                f.write(f"{name},{PHASE_NAMES[p_] if 0 <= p_ < len(PHASE_NAMES) else p_},{s_},{a_:.4f},{b_:.4f}\n")
+            first = min(r[2] for r in rec)
+            summary = {"api": name, "launches": m, "span_ms": round(max(r[3] for r in rec) - first, 3), "streams": {}}
+            for sid in sorted({r[1] for r in rec}):
+                rs = [r for r in rec if r[1] == sid]
+                summary["streams"][sid] = {"launches": len(rs), "busy_ms": round(sum(r[3] - r[2] for r in rs), 3),
+                                           "first_ms": round(min(r[2] for r in rs) - first, 3),
+                                           "last_ms": round(max(r[3] for r in rs) - first, 3)}
+            panels = sorted(r[2] for r in rec if r[0] == 0)
+            starts = panels[::4]                        # four 32-column panels per 128-column block
+            if len(starts) > 8:
+                summary["block_period_us"] = round(1e3 * (starts[-4] - starts[4]) / (len(starts) - 8), 1)
+            print(json.dumps(summary), flush=True)
+    return 0
+
+
 def main():
     args = args_parse()
+    if args.timeline:
+        return timeline(args)
     if args.factor_once:
         return factor_once(args)
     if args.impl == "reference":
